@@ -1,0 +1,178 @@
+/*
+ * whir_gb300.h -- C ABI of the GB300 (sm_103a) WHIR commit-and-open prover.
+ *
+ * This is the drop-in boundary for the reference's prover hot path
+ * (kilic/whir, Rust): plain pointers and sizes, no C++ or torch types.  Each
+ * group below names the reference interface it replaces.
+ *
+ * Conventions
+ *  - A field element is a uint32_t holding the Montgomery word of a KoalaBear
+ *    element (x * 2^32 mod p, p = 2^31 - 2^24 + 1): the in-memory layout of
+ *    Plonky3's KoalaBear, so a Rust &[KoalaBear] can be passed as is.  An
+ *    extension element is 4 such words (BinomialExtensionField<_, 4>), a
+ *    digest 8 ([KoalaBear; 8]).  Every input word must be < p.
+ *  - Pointers documented "device" point to memory of the context's GPU
+ *    (whir_device_alloc or any cudaMalloc'd memory); all others are host.
+ *  - Every function returns WHIR_OK (0) or a negative WHIR_ERR_* code;
+ *    whir_last_error() then describes the failure (per calling thread).
+ *    No C++ exception crosses this boundary.
+ *  - Entry points that take a whir_ctx run on the context's stream and
+ *    return after their results are complete.  A context, and every object
+ *    made from it, must be used by one host thread at a time.
+ */
+#ifndef WHIR_GB300_H
+#define WHIR_GB300_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#if defined(__GNUC__)
+#define WHIR_API __attribute__((visibility("default")))
+#else
+#define WHIR_API
+#endif
+
+#define WHIR_OK 0
+#define WHIR_ERR_ARG (-1)      /* invalid argument or parameters */
+#define WHIR_ERR_CUDA (-2)     /* CUDA runtime error */
+#define WHIR_ERR_NOMEM (-3)    /* device or host allocation failed */
+#define WHIR_ERR_CAPACITY (-4) /* caller buffer too small */
+#define WHIR_ERR_INTERNAL (-5)
+
+typedef struct whir_ctx whir_ctx;
+typedef struct whir_transcript whir_transcript;
+typedef struct whir_prover whir_prover;
+typedef struct whir_tree whir_tree;
+
+/* Whir::new arguments (crates/whir/src/whir.rs:104-125).  soundness:
+ * 0 UniqueDecoding, 1 JohnsonBound, 2 CapacityBound (params.rs:6-21). */
+typedef struct {
+  int32_t k;
+  int32_t folding;
+  int32_t rate; /* log_inv_rate */
+  int32_t initial_reduction;
+  int32_t soundness;
+  int32_t security_level;
+} whir_params;
+
+WHIR_API const char *whir_last_error(void);
+
+/* ---- context: one GPU, one stream, constant tables, staging ---- */
+WHIR_API int whir_ctx_create(int device, whir_ctx **out);
+WHIR_API int whir_ctx_destroy(whir_ctx *ctx);
+WHIR_API int whir_ctx_stream(whir_ctx *ctx, void **cuda_stream);
+WHIR_API int whir_device_alloc(whir_ctx *ctx, size_t bytes, void **out);
+WHIR_API int whir_device_free(whir_ctx *ctx, void *ptr);
+WHIR_API int whir_copy_to_device(whir_ctx *ctx, void *dst_device, const void *src, size_t bytes);
+WHIR_API int whir_copy_to_host(whir_ctx *ctx, void *dst, const void *src_device, size_t bytes);
+
+/* ---- Reed-Solomon encoding.  Replaces TwoAdicSubgroupDft::dft_batch and
+ * dft_algebra_batch as called by commit_base / commit_ext
+ * (crates/whir/src/whir.rs:31-34, 56-59).  in: h_in rows of `width` words
+ * (device), zero-padded to 2^log_h rows; out: 2^log_h rows (device).  An
+ * extension matrix of w columns is the word matrix of 4w columns. ---- */
+WHIR_API int whir_dft_batch(whir_ctx *ctx, const uint32_t *in, size_t h_in, size_t width, int log_h,
+                   uint32_t *out);
+
+/* ---- Merkle commitment.  Replaces MerkleTree / MerkleTreeExt ::commit and
+ * ::query of PackedPoseidonMerkleTree (crates/merkle/src/lib.rs:19-83,
+ * crates/merkle/src/poseidon_packed.rs:145-233,259-384): leaves hashed by
+ * PaddingFreeSponge<Poseidon2<24>,24,16,8>, nodes by
+ * TruncatedPermutation<Poseidon2<16>,2,8,16>, node i of a level paired with
+ * node i + n/2.  rows (device) must outlive the tree. ---- */
+WHIR_API int whir_merkle_commit(whir_ctx *ctx, const uint32_t *rows, int log_h, size_t row_len,
+                       whir_tree **out, uint32_t root[8]);
+/* all levels, leaves first: (2^(log_h+1) - 1) digests */
+WHIR_API int whir_merkle_levels(whir_tree *tree, uint32_t *out);
+/* per index: the leaf row (row_len words) then log_h sibling digests
+ * bottom-up, i.e. the hints query() writes */
+WHIR_API int whir_merkle_open(whir_tree *tree, const size_t *idx, size_t n, uint32_t *out);
+WHIR_API int whir_merkle_free(whir_tree *tree);
+
+/* ---- polynomial and sumcheck passes (crates/poly/src/{point,eq,poly}.rs,
+ * crates/whir/src/sumcheck/{svo,expr,combine}.rs) ---- */
+/* Point::eq (point.rs:159-175): 2^k extension words at out (device) */
+WHIR_API int whir_eq_table(whir_ctx *ctx, const uint32_t *point, int k, const uint32_t scale[4],
+                  uint32_t *out);
+/* SplitEq::compress_hi (eq.rs:290-398): fix the high kz variables of a base
+ * poly (device, 2^k words) to point (kz ext); out: 2^(k-kz) ext (host) */
+WHIR_API int whir_compress_hi(whir_ctx *ctx, const uint32_t *poly, int k, const uint32_t *point, int kz,
+                     uint32_t *out);
+/* SplitEq::compress_lo (eq.rs:400-489): fix the low kz variables; out (device) */
+WHIR_API int whir_compress_lo(whir_ctx *ctx, const uint32_t *poly, int k, const uint32_t *point, int kz,
+                     uint32_t *out);
+/* Poly::eval_ext (poly.rs:312-318) of an extension poly (device) */
+WHIR_API int whir_eval_ext(whir_ctx *ctx, const uint32_t *poly, int k, const uint32_t *point,
+                  uint32_t out[4]);
+/* coeffs (expr.rs:14-27) of extension poly and weights (device, 2^k each) */
+WHIR_API int whir_sumcheck_coeffs(whir_ctx *ctx, const uint32_t *poly, const uint32_t *weights, int k,
+                         uint32_t c0[4], uint32_t c2[4]);
+/* fix_lo_var_mut (poly.rs:354-365) of both arrays into poly_out/w_out
+ * (device, 2^(k-1) each; must not alias the inputs) */
+WHIR_API int whir_sumcheck_fold(whir_ctx *ctx, const uint32_t *poly, const uint32_t *weights, int k,
+                       const uint32_t r[4], uint32_t *poly_out, uint32_t *weights_out);
+/* eq::combine_eqs (combine.rs:179-203): w += sum_i alpha^i eq(z_i) */
+WHIR_API int whir_combine_eqs(whir_ctx *ctx, uint32_t *weights, int k, const uint32_t *points, int n,
+                     const uint32_t alpha[4]);
+/* pow::combine_pows (combine.rs:408-438): w[j] += sum_i alpha^(shift+i) var_i^j */
+WHIR_API int whir_combine_pows(whir_ctx *ctx, uint32_t *weights, int k, const uint32_t *vars, int n,
+                      const uint32_t alpha[4], int shift);
+/* pow::combine_pows_scaled (combine.rs:441-468): w[j] += sum_i s_i var_i^j */
+WHIR_API int whir_combine_pows_scaled(whir_ctx *ctx, uint32_t *weights, int k, const uint32_t *vars,
+                             int n, const uint32_t *scales);
+
+/* Poseidon2KoalaBear<width>::permute_mut on the host (width 16 or 24), with
+ * the constants of new_from_rng_128(&mut rng(1000)) used by the harness
+ * (crates/whir/src/test.rs:195-196). */
+WHIR_API int whir_poseidon2_permute(int width, uint32_t *state);
+
+/* ---- Fiat-Shamir transcript.  Replaces PoseidonWriter<Vec<u8>, KoalaBear,
+ * DuplexChallenger<_, Poseidon2<16>, 16, 8>> (crates/transcript/src/poseidon.rs:13-87)
+ * with the challenger permutation of the harness (test.rs:195-200). ---- */
+WHIR_API int whir_transcript_new(whir_transcript **out);
+WHIR_API int whir_transcript_free(whir_transcript *t);
+WHIR_API int whir_transcript_write(whir_transcript *t, const uint32_t e[4]);   /* Writer<Ext>::write */
+WHIR_API int whir_transcript_write_base(whir_transcript *t, uint32_t v);       /* Writer<F>::write */
+WHIR_API int whir_transcript_draw(whir_transcript *t, uint32_t out[4]);        /* Challenge<F,Ext>::draw */
+WHIR_API int whir_transcript_draw_base(whir_transcript *t, uint32_t *out);     /* Challenge<F,F>::draw */
+WHIR_API int whir_transcript_draw_bits(whir_transcript *t, int bits, size_t *out); /* ChallengeBits */
+WHIR_API int whir_transcript_size(whir_transcript *t, size_t *len);
+WHIR_API int whir_transcript_bytes(whir_transcript *t, uint8_t *out, size_t cap);  /* finalize() */
+
+/* ---- protocol.  Replaces Whir::new / Whir::commit / ProverStack /
+ * Whir::open (crates/whir/src/whir.rs:104-359, sumcheck/prover.rs:32-125) ---- */
+WHIR_API int whir_prover_new(whir_ctx *ctx, const whir_params *params, whir_prover **out);
+WHIR_API int whir_prover_free(whir_prover *p);
+/* commit the stacked layout of n_polys polys given back to back (sizes
+ * 2^poly_k[i]; host, or device when on_device != 0); the stacked size must
+ * equal 2^params.k.  Writes the root.  Each later whir_stack_eval refers to
+ * a poly by its index here. */
+WHIR_API int whir_commit(whir_prover *p, whir_transcript *t, const uint32_t *polys, int on_device,
+                const int32_t *poly_k, int n_polys);
+/* ProverStack::eval: claim on poly id at point (2^0.. poly_k[id] ext), writes eval */
+WHIR_API int whir_stack_eval(whir_prover *p, whir_transcript *t, int id, const uint32_t *point,
+                    uint32_t eval[4]);
+/* Whir::open over the committed layout and the claims made so far */
+WHIR_API int whir_open(whir_prover *p, whir_transcript *t);
+/* The reference harness in one call (crates/whir/src/test.rs:218-235 up to
+ * the checkpoint draw): commit, then for each claim group g draw one point,
+ * expand it to k_g variables and evaluate it on group_ids[off_g ..
+ * off_g + group_n[g]), then open. */
+WHIR_API int whir_prove(whir_prover *p, whir_transcript *t, const uint32_t *polys, int on_device,
+               const int32_t *poly_k, int n_polys, const int32_t *group_n, int n_groups,
+               const int32_t *group_ids);
+
+/* ---- per-kernel-class timing with CUDA events on the context stream:
+ * klass 0 DFT, 1 leaf hash, 2 tree, 3 sumcheck passes.  read returns and
+ * clears total ms, launches and algorithmic bytes since enabling. ---- */
+WHIR_API int whir_prof_enable(whir_ctx *ctx, int on);
+WHIR_API int whir_prof_read(whir_ctx *ctx, int klass, double *ms, long *launches, double *bytes);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

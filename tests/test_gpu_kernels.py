@@ -1,0 +1,124 @@
+"""GPU kernels through the C ABI against the oracle, bit for bit.
+
+Each test mirrors one of the reference's equivalence tests for the same
+routine (crates/poly/src/test.rs, crates/whir/src/sumcheck/combine.rs tests,
+crates/merkle/src/lib.rs tests) and compares the CUDA result with the CPU
+restatement on seeded inputs.  Field arithmetic is exact, so the tolerance is
+zero.
+"""
+import numpy as np
+import pytest
+
+import whir_gb300 as W
+
+pytestmark = pytest.mark.gpu
+
+
+def rand(oracle, seed, n):
+    return oracle.rand_fe(seed, n)
+
+
+@pytest.mark.parametrize("log_h,width,h_in", [
+    (0, 16, 1), (1, 16, 1), (3, 2, 4), (5, 4, 8), (8, 16, 64), (11, 16, 1024), (11, 64, 512),
+    (12, 16, 1024), (13, 8, 8192), (16, 64, 8192), (17, 16, 65536), (20, 16, 262144),
+    (21, 64, 65536), (22, 16, 1 << 20)])
+def test_dft_batch(ctx, oracle, log_h, width, h_in):
+    x = rand(oracle, 7 + log_h, h_in * width)
+    want = oracle.dft_batch(x, h_in, width, log_h)
+    got = W.dft_batch(ctx, ctx.to_device(x), h_in, width, log_h).download(width << log_h)
+    assert np.array_equal(got, want)
+
+
+@pytest.mark.parametrize("log_h,row_len", [(0, 16), (1, 16), (2, 3), (3, 16), (5, 64), (7, 8),
+                                           (10, 16), (12, 64), (16, 16)])
+def test_merkle_commit_and_open(ctx, oracle, log_h, row_len):
+    rows = rand(oracle, 100 + log_h, row_len << log_h)
+    want = oracle.merkle_tree(rows, log_h, row_len)
+    t = W.MerkleTree(ctx, ctx.to_device(rows), log_h, row_len)
+    got = t.levels()
+    assert np.array_equal(got, want)
+    assert np.array_equal(t.root, want[-8:])
+    n = 1 << log_h
+    idx = sorted(set([0, n - 1, n // 2, (7 * n) // 11 % n]))
+    op = t.open(idx)
+    for q, i in enumerate(idx):
+        assert np.array_equal(op[q, :row_len], rows[i * row_len:(i + 1) * row_len])
+        a = i
+        for lvl in range(log_h):
+            mid = 1 << (log_h - lvl - 1)
+            off = ((2 << log_h) - (2 << (log_h - lvl))) * 8
+            sib = want[off + (a ^ mid) * 8: off + (a ^ mid) * 8 + 8]
+            assert np.array_equal(op[q, row_len + 8 * lvl: row_len + 8 * lvl + 8], sib)
+            a &= mid - 1
+    t.close()
+
+
+@pytest.mark.parametrize("k", [0, 1, 5, 12, 20])
+def test_eq_table(ctx, oracle, k):
+    pt = rand(oracle, 3, 4 * k)
+    scale = rand(oracle, 4, 4)
+    got = W.eq_table(ctx, pt, k, scale).download(4 << k)
+    assert np.array_equal(got, oracle.eq_table(pt, k, scale))
+
+
+@pytest.mark.parametrize("k,ks", [(4, 4), (5, 1), (8, 4), (14, 4), (20, 4), (24, 4), (16, 5)])
+def test_compress_hi(ctx, oracle, k, ks):
+    poly = rand(oracle, 11, 1 << k)
+    kz = k - ks
+    pt = rand(oracle, 12, 4 * kz)
+    got = W.compress_hi(ctx, ctx.to_device(poly), k, pt, kz)
+    assert np.array_equal(got, oracle.compress_hi(poly, k, pt, kz))
+
+
+@pytest.mark.parametrize("k,kz", [(4, 4), (6, 1), (10, 4), (20, 4), (24, 4)])
+def test_compress_lo(ctx, oracle, k, kz):
+    poly = rand(oracle, 13, 1 << k)
+    pt = rand(oracle, 14, 4 * kz)
+    got = W.compress_lo(ctx, ctx.to_device(poly), k, pt, kz).download(4 << (k - kz))
+    assert np.array_equal(got, oracle.compress_lo(poly, k, pt, kz))
+
+
+@pytest.mark.parametrize("k", [0, 1, 4, 9, 16, 20])
+def test_eval_ext(ctx, oracle, k):
+    poly = rand(oracle, 15, 4 << k)
+    pt = rand(oracle, 16, 4 * k)
+    got = W.eval_ext(ctx, ctx.to_device(poly), k, pt)
+    assert np.array_equal(got, oracle.eval_ext(poly, k, pt))
+
+
+@pytest.mark.parametrize("k", [1, 2, 7, 16, 20])
+def test_coeffs_and_fold(ctx, oracle, k):
+    p = rand(oracle, 17, 4 << k)
+    w = rand(oracle, 18, 4 << k)
+    dp, dw = ctx.to_device(p), ctx.to_device(w)
+    c0, c2 = W.sumcheck_coeffs(ctx, dp, dw, k)
+    e0, e2 = oracle.coeffs(p, w, k)
+    assert np.array_equal(c0, e0) and np.array_equal(c2, e2)
+    r = rand(oracle, 19, 4)
+    po, wo = W.sumcheck_fold(ctx, dp, dw, k, r)
+    assert np.array_equal(po.download(4 << (k - 1)), oracle.fix_lo(p, k, r))
+    assert np.array_equal(wo.download(4 << (k - 1)), oracle.fix_lo(w, k, r))
+
+
+@pytest.mark.parametrize("k,n", [(2, 1), (5, 2), (9, 10), (9, 11), (16, 2)])
+def test_combine_eqs(ctx, oracle, k, n):
+    w = rand(oracle, 20, 4 << k)
+    pts = rand(oracle, 21, 4 * k * n)
+    alpha = rand(oracle, 22, 4)
+    dw = ctx.to_device(w)
+    W.combine_eqs(ctx, dw, k, pts, n, alpha)
+    assert np.array_equal(dw.download(4 << k), oracle.combine_eqs(w, k, pts, n, alpha))
+
+
+@pytest.mark.parametrize("k,n,shift", [(2, 1, 0), (5, 2, 11), (9, 10, 3), (9, 11, 11), (16, 52, 2)])
+def test_combine_pows(ctx, oracle, k, n, shift):
+    w = rand(oracle, 23, 4 << k)
+    vars_ = rand(oracle, 24, n)
+    alpha = rand(oracle, 25, 4)
+    dw = ctx.to_device(w)
+    W.combine_pows(ctx, dw, k, vars_, n, alpha, shift)
+    assert np.array_equal(dw.download(4 << k), oracle.combine_pows(w, k, vars_, n, alpha, shift))
+    scales = rand(oracle, 26, 4 * n)
+    dw2 = ctx.to_device(w)
+    W.combine_pows_scaled(ctx, dw2, k, vars_, n, scales)
+    assert np.array_equal(dw2.download(4 << k), oracle.combine_pows_scaled(w, k, vars_, n, scales))

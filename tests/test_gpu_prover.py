@@ -1,0 +1,79 @@
+"""Full GPU proofs through the C ABI, byte-identical to the oracle prover and
+accepted by the oracle verifier.
+
+The parameter sweep follows the reference's test_whir_poseidon
+(crates/whir/src/test.rs:256-282: three soundness assumptions, k = 4..12,
+folding 1..3, initial_reduction 1..folding, 1..4 claims, rate 1, 32-bit
+security) on a subset that keeps the run short, plus the benchmark shapes
+(k = 20 and k = 24, folding 4) and stacked multi-polynomial layouts.
+"""
+import itertools
+
+import numpy as np
+import pytest
+
+import whir_gb300 as W
+
+pytestmark = pytest.mark.gpu
+
+SWEEP = [(s, k, f, ir, n)
+         for s in (1, 2, 0) for k in (4, 5, 7, 9, 12) for f in (1, 2, 3)
+         for ir in range(1, f + 1) for n in (1, 4)
+         if (k + f + ir + n + s) % 3 == 0 or k == 12]
+
+
+def check(ctx, oracle, params, polys, poly_k, groups):
+    proof, cp = W.prove_harness(ctx, params, polys, poly_k, groups)
+    want, wcp = oracle.prove(params, polys, poly_k, groups)
+    assert len(proof) == len(want)
+    assert proof == want
+    assert cp == wcp
+    rc, vcp = oracle.verify(params, poly_k, groups, proof)
+    assert rc == 0 and vcp == cp
+
+
+@pytest.mark.parametrize("s,k,f,ir,n", SWEEP)
+def test_whir_sweep(ctx, oracle, s, k, f, ir, n):
+    poly = oracle.rand_fe(1, 1 << k)
+    check(ctx, oracle, (k, f, 1, ir, s, 32), [poly], [k], [[0]] * n)
+
+
+@pytest.mark.parametrize("k,rate,n", [(10, 2, 2), (16, 1, 1), (20, 1, 1), (18, 2, 4)])
+def test_whir_folding4_security100(ctx, oracle, k, rate, n):
+    poly = oracle.rand_fe(1, 1 << k)
+    check(ctx, oracle, (k, 4, rate, 1, 1, 100), [poly], [k], [[0]] * n)
+
+
+def test_stacked_layout(ctx, oracle):
+    # several polynomials of different sizes in one layout (ProverStack::layout)
+    ks = [8, 6, 6, 8, 5]
+    polys = [oracle.rand_fe(10 + i, 1 << k) for i, k in enumerate(ks)]
+    k = int(np.ceil(np.log2(sum(1 << x for x in ks))))
+    groups = [[0, 3], [1, 2], [4], [3]]
+    check(ctx, oracle, (k, 3, 1, 1, 1, 32), polys, ks, groups)
+
+
+def test_proof_is_deterministic_across_calls(ctx, oracle):
+    poly = oracle.rand_fe(5, 1 << 12)
+    w = W.Whir(ctx, 12, 4, 1, 1, 1, 100)
+    a = W.prove_harness(ctx, None, [poly], [12], [[0]], whir=w)
+    b = W.prove_harness(ctx, None, [poly], [12], [[0]], whir=w)
+    assert a == b
+
+
+def test_device_resident_input(ctx, oracle):
+    k = 14
+    poly = oracle.rand_fe(3, 1 << k)
+    w = W.Whir(ctx, k, 4, 2, 1, 1, 100)
+    t = W.PoseidonWriter()
+    w.prove(t, ctx.to_device(poly), [k], [[0], [0]])
+    cp = t.draw_base()
+    want, wcp = oracle.prove((k, 4, 2, 1, 1, 100), [poly], [k], [[0], [0]])
+    assert t.finalize() == want and cp == wcp
+
+
+def test_bench_shape_k24(ctx, oracle):
+    # the benchmark workload: k = 24, rate 1/4, folding 4, 4 claims, 100-bit JB
+    k = 24
+    poly = oracle.rand_fe(1, 1 << k)
+    check(ctx, oracle, (k, 4, 2, 1, 1, 100), [poly], [k], [[0]] * 4)

@@ -1,0 +1,408 @@
+"""GB300-native WHIR prover: Python mirror of the C ABI in include/whir_gb300.h.
+
+The compute path is libwhir_gb300.so (hand-written sm_103a CUDA kernels and a
+C++ host); this module only binds it with ctypes and mirrors the reference's
+prover interface (kilic/whir ``Whir::{new, commit, open}``, ``ProverStack``,
+``PoseidonWriter``) so tests and benchmarks read like the reference's own.
+There is no CPU fallback: every call fails loudly when the library or a GPU is
+missing.
+
+Field elements are numpy uint32 arrays of Montgomery words (Plonky3's
+KoalaBear representation); an extension element is 4 words.
+"""
+
+import ctypes
+import os
+
+import numpy as np
+
+from . import build as _build
+
+P = 0x7F000001
+SOUNDNESS = {"UniqueDecoding": 0, "JohnsonBound": 1, "CapacityBound": 2}
+PROF_DFT, PROF_LEAF, PROF_TREE, PROF_SUMCHECK = 0, 1, 2, 3
+
+_lib = None
+u32p = ctypes.POINTER(ctypes.c_uint32)
+i32p = ctypes.POINTER(ctypes.c_int32)
+vp = ctypes.c_void_p
+
+
+class WhirError(RuntimeError):
+    pass
+
+
+class Params(ctypes.Structure):
+    _fields_ = [(n, ctypes.c_int32) for n in
+                ("k", "folding", "rate", "initial_reduction", "soundness", "security_level")]
+
+
+_SIGS = {
+    "whir_last_error": (ctypes.c_char_p, []),
+    "whir_ctx_create": (ctypes.c_int, [ctypes.c_int, ctypes.POINTER(vp)]),
+    "whir_ctx_destroy": (ctypes.c_int, [vp]),
+    "whir_ctx_stream": (ctypes.c_int, [vp, ctypes.POINTER(vp)]),
+    "whir_device_alloc": (ctypes.c_int, [vp, ctypes.c_size_t, ctypes.POINTER(vp)]),
+    "whir_device_free": (ctypes.c_int, [vp, vp]),
+    "whir_copy_to_device": (ctypes.c_int, [vp, vp, vp, ctypes.c_size_t]),
+    "whir_copy_to_host": (ctypes.c_int, [vp, vp, vp, ctypes.c_size_t]),
+    "whir_dft_batch": (ctypes.c_int, [vp, vp, ctypes.c_size_t, ctypes.c_size_t, ctypes.c_int, vp]),
+    "whir_merkle_commit": (ctypes.c_int, [vp, vp, ctypes.c_int, ctypes.c_size_t,
+                                          ctypes.POINTER(vp), u32p]),
+    "whir_merkle_levels": (ctypes.c_int, [vp, u32p]),
+    "whir_merkle_open": (ctypes.c_int, [vp, ctypes.POINTER(ctypes.c_size_t), ctypes.c_size_t,
+                                        u32p]),
+    "whir_merkle_free": (ctypes.c_int, [vp]),
+    "whir_eq_table": (ctypes.c_int, [vp, u32p, ctypes.c_int, u32p, vp]),
+    "whir_compress_hi": (ctypes.c_int, [vp, vp, ctypes.c_int, u32p, ctypes.c_int, u32p]),
+    "whir_compress_lo": (ctypes.c_int, [vp, vp, ctypes.c_int, u32p, ctypes.c_int, vp]),
+    "whir_eval_ext": (ctypes.c_int, [vp, vp, ctypes.c_int, u32p, u32p]),
+    "whir_sumcheck_coeffs": (ctypes.c_int, [vp, vp, vp, ctypes.c_int, u32p, u32p]),
+    "whir_sumcheck_fold": (ctypes.c_int, [vp, vp, vp, ctypes.c_int, u32p, vp, vp]),
+    "whir_combine_eqs": (ctypes.c_int, [vp, vp, ctypes.c_int, u32p, ctypes.c_int, u32p]),
+    "whir_combine_pows": (ctypes.c_int, [vp, vp, ctypes.c_int, u32p, ctypes.c_int, u32p,
+                                         ctypes.c_int]),
+    "whir_combine_pows_scaled": (ctypes.c_int, [vp, vp, ctypes.c_int, u32p, ctypes.c_int, u32p]),
+    "whir_transcript_new": (ctypes.c_int, [ctypes.POINTER(vp)]),
+    "whir_transcript_free": (ctypes.c_int, [vp]),
+    "whir_transcript_write": (ctypes.c_int, [vp, u32p]),
+    "whir_transcript_write_base": (ctypes.c_int, [vp, ctypes.c_uint32]),
+    "whir_transcript_draw": (ctypes.c_int, [vp, u32p]),
+    "whir_transcript_draw_base": (ctypes.c_int, [vp, u32p]),
+    "whir_transcript_draw_bits": (ctypes.c_int, [vp, ctypes.c_int,
+                                                 ctypes.POINTER(ctypes.c_size_t)]),
+    "whir_transcript_size": (ctypes.c_int, [vp, ctypes.POINTER(ctypes.c_size_t)]),
+    "whir_transcript_bytes": (ctypes.c_int, [vp, ctypes.c_char_p, ctypes.c_size_t]),
+    "whir_prover_new": (ctypes.c_int, [vp, ctypes.POINTER(Params), ctypes.POINTER(vp)]),
+    "whir_prover_free": (ctypes.c_int, [vp]),
+    "whir_commit": (ctypes.c_int, [vp, vp, vp, ctypes.c_int, i32p, ctypes.c_int]),
+    "whir_stack_eval": (ctypes.c_int, [vp, vp, ctypes.c_int, u32p, u32p]),
+    "whir_open": (ctypes.c_int, [vp, vp]),
+    "whir_prove": (ctypes.c_int, [vp, vp, vp, ctypes.c_int, i32p, ctypes.c_int, i32p,
+                                  ctypes.c_int, i32p]),
+    "whir_prof_enable": (ctypes.c_int, [vp, ctypes.c_int]),
+    "whir_prof_read": (ctypes.c_int, [vp, ctypes.c_int, ctypes.POINTER(ctypes.c_double),
+                                      ctypes.POINTER(ctypes.c_long),
+                                      ctypes.POINTER(ctypes.c_double)]),
+    "whir_poseidon2_permute": (ctypes.c_int, [ctypes.c_int, u32p]),
+}
+
+
+def lib_path():
+    return _build.LIB
+
+
+def lib():
+    """Load libwhir_gb300.so (building it if absent)."""
+    global _lib
+    if _lib is None:
+        if not os.path.exists(_build.LIB):
+            _build.build()
+        L = ctypes.CDLL(_build.LIB)
+        for name, (res, args) in _SIGS.items():
+            fn = getattr(L, name)
+            fn.restype = res
+            fn.argtypes = args
+        _lib = L
+    return _lib
+
+
+def _check(rc):
+    if rc != 0:
+        msg = lib().whir_last_error()
+        raise WhirError(f"whir error {rc}: {msg.decode() if msg else ''}")
+
+
+def _u32(a):
+    a = np.ascontiguousarray(a, dtype=np.uint32)
+    return a, a.ctypes.data_as(u32p)
+
+
+class DeviceArray:
+    """Device allocation of the context's GPU (freed on close / GC)."""
+
+    def __init__(self, ctx, nbytes):
+        self.ctx = ctx
+        self.nbytes = int(nbytes)
+        p = vp()
+        _check(lib().whir_device_alloc(ctx.h, max(16, self.nbytes), ctypes.byref(p)))
+        self.ptr = p.value
+
+    def close(self):
+        if self.ptr:
+            lib().whir_device_free(self.ctx.h, self.ptr)
+            self.ptr = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def upload(self, arr):
+        arr = np.ascontiguousarray(arr)
+        assert arr.nbytes <= self.nbytes
+        _check(lib().whir_copy_to_device(self.ctx.h, self.ptr, arr.ctypes.data, arr.nbytes))
+        return self
+
+    def download(self, n_words, dtype=np.uint32):
+        out = np.empty(n_words, dtype)
+        _check(lib().whir_copy_to_host(self.ctx.h, out.ctypes.data, self.ptr, out.nbytes))
+        return out
+
+
+class Context:
+    """One GPU and one CUDA stream (whir_ctx)."""
+
+    def __init__(self, device=0):
+        h = vp()
+        _check(lib().whir_ctx_create(device, ctypes.byref(h)))
+        self.h = h.value
+
+    def close(self):
+        if self.h:
+            lib().whir_ctx_destroy(self.h)
+            self.h = None
+
+    def stream(self):
+        s = vp()
+        _check(lib().whir_ctx_stream(self.h, ctypes.byref(s)))
+        return s.value
+
+    def alloc(self, nbytes):
+        return DeviceArray(self, nbytes)
+
+    def to_device(self, arr):
+        arr = np.ascontiguousarray(arr)
+        return DeviceArray(self, arr.nbytes).upload(arr)
+
+    def prof_enable(self, on=True):
+        _check(lib().whir_prof_enable(self.h, 1 if on else 0))
+
+    def prof_read(self, klass):
+        ms, n, b = ctypes.c_double(), ctypes.c_long(), ctypes.c_double()
+        _check(lib().whir_prof_read(self.h, klass, ctypes.byref(ms), ctypes.byref(n),
+                                    ctypes.byref(b)))
+        return ms.value, n.value, b.value
+
+
+# ---- kernel-level entry points (device arrays in, numpy or device out) ----
+def dft_batch(ctx, dev_in, h_in, width, log_h):
+    out = ctx.alloc(4 * width << log_h)
+    _check(lib().whir_dft_batch(ctx.h, dev_in.ptr, h_in, width, log_h, out.ptr))
+    return out
+
+
+class MerkleTree:
+    def __init__(self, ctx, dev_rows, log_h, row_len):
+        self.ctx, self.rows, self.log_h, self.row_len = ctx, dev_rows, log_h, row_len
+        h = vp()
+        root = np.zeros(8, np.uint32)
+        _check(lib().whir_merkle_commit(ctx.h, dev_rows.ptr, log_h, row_len, ctypes.byref(h),
+                                        root.ctypes.data_as(u32p)))
+        self.h, self.root = h.value, root
+
+    def levels(self):
+        out = np.empty(((2 << self.log_h) - 1) * 8, np.uint32)
+        _check(lib().whir_merkle_levels(self.h, out.ctypes.data_as(u32p)))
+        return out
+
+    def open(self, indexes):
+        idx = np.ascontiguousarray(indexes, dtype=np.uintp)
+        per = self.row_len + 8 * self.log_h
+        out = np.empty(per * len(idx), np.uint32)
+        _check(lib().whir_merkle_open(self.h, idx.ctypes.data_as(ctypes.POINTER(ctypes.c_size_t)),
+                                      len(idx), out.ctypes.data_as(u32p)))
+        return out.reshape(len(idx), per)
+
+    def close(self):
+        if self.h:
+            lib().whir_merkle_free(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+def eq_table(ctx, point, k, scale):
+    out = ctx.alloc(16 << k)
+    pt, pp = _u32(point)
+    sc, sp = _u32(scale)
+    _check(lib().whir_eq_table(ctx.h, pp, k, sp, out.ptr))
+    return out
+
+
+def compress_hi(ctx, dev_poly, k, point, kz):
+    out = np.empty(4 << (k - kz), np.uint32)
+    pt, pp = _u32(point)
+    _check(lib().whir_compress_hi(ctx.h, dev_poly.ptr, k, pp, kz, out.ctypes.data_as(u32p)))
+    return out
+
+
+def compress_lo(ctx, dev_poly, k, point, kz):
+    out = ctx.alloc(16 << (k - kz))
+    pt, pp = _u32(point)
+    _check(lib().whir_compress_lo(ctx.h, dev_poly.ptr, k, pp, kz, out.ptr))
+    return out
+
+
+def eval_ext(ctx, dev_poly, k, point):
+    out = np.empty(4, np.uint32)
+    pt, pp = _u32(point)
+    _check(lib().whir_eval_ext(ctx.h, dev_poly.ptr, k, pp, out.ctypes.data_as(u32p)))
+    return out
+
+
+def sumcheck_coeffs(ctx, dev_poly, dev_w, k):
+    c0, c2 = np.empty(4, np.uint32), np.empty(4, np.uint32)
+    _check(lib().whir_sumcheck_coeffs(ctx.h, dev_poly.ptr, dev_w.ptr, k,
+                                      c0.ctypes.data_as(u32p), c2.ctypes.data_as(u32p)))
+    return c0, c2
+
+
+def sumcheck_fold(ctx, dev_poly, dev_w, k, r):
+    po, wo = ctx.alloc(16 << (k - 1)), ctx.alloc(16 << (k - 1))
+    rr, rp = _u32(r)
+    _check(lib().whir_sumcheck_fold(ctx.h, dev_poly.ptr, dev_w.ptr, k, rp, po.ptr, wo.ptr))
+    return po, wo
+
+
+def combine_eqs(ctx, dev_w, k, points, n, alpha):
+    pt, pp = _u32(points)
+    al, ap = _u32(alpha)
+    _check(lib().whir_combine_eqs(ctx.h, dev_w.ptr, k, pp, n, ap))
+
+
+def combine_pows(ctx, dev_w, k, vars_, n, alpha, shift):
+    va, vpp = _u32(vars_)
+    al, ap = _u32(alpha)
+    _check(lib().whir_combine_pows(ctx.h, dev_w.ptr, k, vpp, n, ap, shift))
+
+
+def combine_pows_scaled(ctx, dev_w, k, vars_, n, scales):
+    va, vpp = _u32(vars_)
+    sc, sp = _u32(scales)
+    _check(lib().whir_combine_pows_scaled(ctx.h, dev_w.ptr, k, vpp, n, sp))
+
+
+def poseidon2_permute(width, state):
+    s, sp = _u32(np.array(state, dtype=np.uint32).copy())
+    _check(lib().whir_poseidon2_permute(width, sp))
+    return s
+
+
+# ---- transcript and protocol ----
+class PoseidonWriter:
+    """PoseidonWriter<Vec<u8>, KoalaBear, DuplexChallenger<_, Poseidon2<16>, 16, 8>>."""
+
+    def __init__(self):
+        h = vp()
+        _check(lib().whir_transcript_new(ctypes.byref(h)))
+        self.h = h.value
+
+    def write(self, e):
+        a, p = _u32(e)
+        _check(lib().whir_transcript_write(self.h, p))
+
+    def write_base(self, v):
+        _check(lib().whir_transcript_write_base(self.h, int(v)))
+
+    def draw(self):
+        out = np.empty(4, np.uint32)
+        _check(lib().whir_transcript_draw(self.h, out.ctypes.data_as(u32p)))
+        return out
+
+    def draw_base(self):
+        out = np.empty(1, np.uint32)
+        _check(lib().whir_transcript_draw_base(self.h, out.ctypes.data_as(u32p)))
+        return int(out[0])
+
+    def draw_bits(self, bits):
+        out = ctypes.c_size_t()
+        _check(lib().whir_transcript_draw_bits(self.h, bits, ctypes.byref(out)))
+        return out.value
+
+    def finalize(self):
+        n = ctypes.c_size_t()
+        _check(lib().whir_transcript_size(self.h, ctypes.byref(n)))
+        buf = ctypes.create_string_buffer(max(1, n.value))
+        _check(lib().whir_transcript_bytes(self.h, buf, n.value))
+        return buf.raw[: n.value]
+
+    def close(self):
+        if self.h:
+            lib().whir_transcript_free(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+class Whir:
+    """Whir::new(k, folding, rate, initial_reduction, soundness, security_level)."""
+
+    def __init__(self, ctx, k, folding, rate, initial_reduction, soundness, security_level):
+        self.ctx = ctx
+        if isinstance(soundness, str):
+            soundness = SOUNDNESS[soundness]
+        self.params = Params(k, folding, rate, initial_reduction, soundness, security_level)
+        h = vp()
+        _check(lib().whir_prover_new(ctx.h, ctypes.byref(self.params), ctypes.byref(h)))
+        self.h = h.value
+
+    @staticmethod
+    def _polys(polys):
+        if isinstance(polys, DeviceArray):
+            return polys.ptr, 1, None
+        flat = np.ascontiguousarray(np.concatenate([np.asarray(p, np.uint32) for p in polys])
+                                    if isinstance(polys, (list, tuple)) else polys, np.uint32)
+        return flat.ctypes.data, 0, flat
+
+    def commit(self, transcript, polys, poly_k):
+        ptr, dev, keep = self._polys(polys)
+        ks = (ctypes.c_int32 * len(poly_k))(*poly_k)
+        _check(lib().whir_commit(self.h, transcript.h, ptr, dev, ks, len(poly_k)))
+
+    def stack_eval(self, transcript, poly_id, point):
+        pt, pp = _u32(point)
+        out = np.empty(4, np.uint32)
+        _check(lib().whir_stack_eval(self.h, transcript.h, poly_id, pp, out.ctypes.data_as(u32p)))
+        return out
+
+    def open(self, transcript):
+        _check(lib().whir_open(self.h, transcript.h))
+
+    def prove(self, transcript, polys, poly_k, groups):
+        ptr, dev, keep = self._polys(polys)
+        ks = (ctypes.c_int32 * len(poly_k))(*poly_k)
+        gn = (ctypes.c_int32 * max(1, len(groups)))(*[len(g) for g in groups])
+        flat = [i for g in groups for i in g]
+        gi = (ctypes.c_int32 * max(1, len(flat)))(*flat)
+        _check(lib().whir_prove(self.h, transcript.h, ptr, dev, ks, len(poly_k), gn, len(groups),
+                                gi))
+
+    def close(self):
+        if self.h:
+            lib().whir_prover_free(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+def prove_harness(ctx, params, polys, poly_k, groups, whir=None):
+    """Reference harness (crates/whir/src/test.rs:218-235): returns (proof, checkpoint)."""
+    w = whir or Whir(ctx, *params)
+    t = PoseidonWriter()
+    w.prove(t, polys, poly_k, groups)
+    cp = t.draw_base()
+    return t.finalize(), cp

@@ -1,0 +1,546 @@
+// extern "C" boundary (include/whir_gb300.h): argument checks, exception to
+// status-code translation, and the kernel-level entry points.
+#include "../../include/whir_gb300.h"
+
+#include <string.h>
+
+#include <new>
+#include <string>
+#include <vector>
+
+#include "kernels.h"
+#include "poseidon2_host.h"
+#include "prover.h"
+#include "transcript.h"
+
+using whir::Context;
+using whir::DeviceBuffer;
+using whir::WhirError;
+using kb::E4;
+
+struct whir_ctx {
+  Context ctx;
+  DeviceBuffer scratch, eq, acc, small;
+  explicit whir_ctx(int dev) : ctx(dev) {}
+};
+struct whir_transcript {
+  whir::Transcript t;
+};
+struct whir_prover {
+  whir_ctx *ctx;
+  whir::Prover p;
+  whir_prover(whir_ctx *c, const whir::Params &prm) : ctx(c), p(&c->ctx, prm) {}
+};
+struct whir_tree {
+  whir_ctx *ctx;
+  DeviceBuffer nodes;
+  whir::DeviceTree t;
+};
+
+static thread_local std::string g_err;
+
+#define API_BEGIN try {
+#define API_END                                          \
+  return WHIR_OK;                                        \
+  }                                                      \
+  catch (const WhirError &e) {                           \
+    g_err = e.what();                                    \
+    return e.code == -2 ? WHIR_ERR_CUDA                  \
+           : e.code == -3 ? WHIR_ERR_NOMEM               \
+           : e.code == -4 ? WHIR_ERR_CAPACITY            \
+                          : WHIR_ERR_ARG;                \
+  }                                                      \
+  catch (const std::bad_alloc &) {                       \
+    g_err = "host allocation failed";                    \
+    return WHIR_ERR_NOMEM;                               \
+  }                                                      \
+  catch (const std::exception &e) {                      \
+    g_err = e.what();                                    \
+    return WHIR_ERR_INTERNAL;                            \
+  }
+
+static void need(bool ok, const char *what) {
+  if (!ok) throw WhirError(-1, what);
+}
+static E4 ext_in(const uint32_t *v) {
+  E4 e;
+  for (int i = 0; i < 4; i++) e.c[i] = v[i];
+  for (int i = 0; i < 4; i++) need(v[i] < kb::P, "non-canonical field element");
+  return e;
+}
+static void ext_out(const E4 &e, uint32_t *v) { memcpy(v, e.c, 16); }
+static whir::gpu::Point point_in(const uint32_t *pt, int k) {
+  need(k >= 0 && k <= whir::gpu::MAX_VARS, "point has too many variables");
+  need(pt != nullptr || k == 0, "null point");
+  whir::gpu::Point z;
+  z.k = k;
+  for (int i = 0; i < k; i++) z.z[i] = ext_in(pt + 4 * i);
+  return z;
+}
+static unsigned long long *acc_buf(whir_ctx *c, size_t words) {
+  c->acc.reserve(8 * words);
+  unsigned long long *a = c->acc.as<unsigned long long>();
+  whir::cuda_check(cudaMemsetAsync(a, 0, 8 * words, c->ctx.stream()), "memset");
+  return a;
+}
+static void read_acc(whir_ctx *c, unsigned long long *a, size_t words, uint32_t *out) {
+  std::vector<unsigned long long> h(words);
+  whir::cuda_check(cudaMemcpyAsync(h.data(), a, 8 * words, cudaMemcpyDeviceToHost, c->ctx.stream()),
+                   "d2h");
+  c->ctx.sync();
+  for (size_t i = 0; i < words; i++) out[i] = (uint32_t)(h[i] % kb::P);
+}
+
+extern "C" {
+
+const char *whir_last_error(void) { return g_err.c_str(); }
+
+int whir_ctx_create(int device, whir_ctx **out) {
+  API_BEGIN
+  need(out != nullptr, "null out");
+  *out = new whir_ctx(device);
+  API_END
+}
+int whir_ctx_destroy(whir_ctx *ctx) {
+  API_BEGIN
+  delete ctx;
+  API_END
+}
+int whir_ctx_stream(whir_ctx *ctx, void **stream) {
+  API_BEGIN
+  need(ctx && stream, "null argument");
+  *stream = (void *)ctx->ctx.stream();
+  API_END
+}
+int whir_device_alloc(whir_ctx *ctx, size_t bytes, void **out) {
+  API_BEGIN
+  need(ctx && out, "null argument");
+  cudaError_t e = cudaMalloc(out, bytes ? bytes : 16);
+  if (e != cudaSuccess) throw WhirError(-3, cudaGetErrorString(e));
+  API_END
+}
+int whir_device_free(whir_ctx *ctx, void *ptr) {
+  API_BEGIN
+  need(ctx != nullptr, "null context");
+  ctx->ctx.sync();
+  whir::cuda_check(cudaFree(ptr), "cudaFree");
+  API_END
+}
+int whir_copy_to_device(whir_ctx *ctx, void *dst, const void *src, size_t bytes) {
+  API_BEGIN
+  need(ctx && dst && src, "null argument");
+  whir::cuda_check(cudaMemcpyAsync(dst, src, bytes, cudaMemcpyHostToDevice, ctx->ctx.stream()),
+                   "h2d");
+  ctx->ctx.sync();
+  API_END
+}
+int whir_copy_to_host(whir_ctx *ctx, void *dst, const void *src, size_t bytes) {
+  API_BEGIN
+  need(ctx && dst && src, "null argument");
+  whir::cuda_check(cudaMemcpyAsync(dst, src, bytes, cudaMemcpyDeviceToHost, ctx->ctx.stream()),
+                   "d2h");
+  ctx->ctx.sync();
+  API_END
+}
+
+int whir_dft_batch(whir_ctx *ctx, const uint32_t *in, size_t h_in, size_t width, int log_h,
+                   uint32_t *out) {
+  API_BEGIN
+  need(ctx && in && out, "null argument");
+  need(log_h >= 0 && log_h <= 24, "log_h must be in [0, 24] (two-adicity of KoalaBear)");
+  need(width > 0 && h_in <= ((size_t)1 << log_h), "bad matrix shape");
+  if (log_h > 11) ctx->scratch.reserve(4 * (width << log_h));
+  whir::cuda_check(whir::gpu::dft_batch(in, h_in, width, log_h, out,
+                                        log_h > 11 ? ctx->scratch.as<uint32_t>() : nullptr,
+                                        ctx->ctx.stream()),
+                   "dft_batch");
+  ctx->ctx.sync();
+  API_END
+}
+
+int whir_merkle_commit(whir_ctx *ctx, const uint32_t *rows, int log_h, size_t row_len,
+                       whir_tree **out, uint32_t root[8]) {
+  API_BEGIN
+  need(ctx && rows && out && root, "null argument");
+  need(log_h >= 0 && log_h <= 30 && row_len > 0 && row_len < (1u << 20), "bad tree shape");
+  whir_tree *t = new whir_tree();
+  t->ctx = ctx;
+  try {
+    t->nodes.reserve(4 * whir::gpu::tree_words(log_h));
+    cudaStream_t st = ctx->ctx.stream();
+    size_t n = (size_t)1 << log_h;
+    whir::cuda_check(whir::gpu::hash_rows(rows, n, (int)row_len, t->nodes.as<uint32_t>(), st),
+                     "hash_rows");
+    whir::cuda_check(whir::gpu::build_tree(t->nodes.as<uint32_t>(), log_h, st), "build_tree");
+    uint32_t h[8];
+    whir::cuda_check(cudaMemcpyAsync(h, t->nodes.as<uint32_t>() + whir::gpu::tree_words(log_h) - 8,
+                                     32, cudaMemcpyDeviceToHost, st),
+                     "d2h");
+    ctx->ctx.sync();
+    t->t.rows = rows;
+    t->t.nodes = t->nodes.as<uint32_t>();
+    t->t.log_h = log_h;
+    t->t.row_len = (int)row_len;
+    memcpy(t->t.root, h, 32);
+    memcpy(root, h, 32);
+  } catch (...) {
+    delete t;
+    throw;
+  }
+  *out = t;
+  API_END
+}
+int whir_merkle_levels(whir_tree *tree, uint32_t *out) {
+  API_BEGIN
+  need(tree && out, "null argument");
+  size_t words = whir::gpu::tree_words(tree->t.log_h);
+  whir::cuda_check(cudaMemcpyAsync(out, tree->t.nodes, 4 * words, cudaMemcpyDeviceToHost,
+                                   tree->ctx->ctx.stream()),
+                   "d2h");
+  tree->ctx->ctx.sync();
+  API_END
+}
+int whir_merkle_open(whir_tree *tree, const size_t *idx, size_t n, uint32_t *out) {
+  API_BEGIN
+  need(tree && (idx || !n) && (out || !n), "null argument");
+  if (!n) return WHIR_OK;
+  whir_ctx *c = tree->ctx;
+  size_t h = (size_t)1 << tree->t.log_h;
+  std::vector<uint32_t> i32(n);
+  for (size_t i = 0; i < n; i++) {
+    need(idx[i] < h, "query index out of range");
+    i32[i] = (uint32_t)idx[i];
+  }
+  size_t per = (size_t)tree->t.row_len + 8 * (size_t)tree->t.log_h;
+  c->small.reserve(4 * n + 4 * per * n);
+  uint32_t *d = c->small.as<uint32_t>();
+  cudaStream_t st = c->ctx.stream();
+  whir::cuda_check(cudaMemcpyAsync(d, i32.data(), 4 * n, cudaMemcpyHostToDevice, st), "h2d");
+  whir::cuda_check(whir::gpu::gather_openings(tree->t.rows, tree->t.row_len, tree->t.nodes,
+                                              tree->t.log_h, d, (int)n, d + n, st),
+                   "gather");
+  whir::cuda_check(cudaMemcpyAsync(out, d + n, 4 * per * n, cudaMemcpyDeviceToHost, st), "d2h");
+  c->ctx.sync();
+  API_END
+}
+int whir_merkle_free(whir_tree *tree) {
+  API_BEGIN
+  if (tree) tree->ctx->ctx.sync();
+  delete tree;
+  API_END
+}
+
+int whir_eq_table(whir_ctx *ctx, const uint32_t *point, int k, const uint32_t scale[4],
+                  uint32_t *out) {
+  API_BEGIN
+  need(ctx && out && scale, "null argument");
+  need(k <= 24, "k too large");
+  whir::gpu::Point z = point_in(point, k);
+  ctx->eq.reserve(sizeof(E4) * (((size_t)1 << (k / 2)) + ((size_t)1 << (k - k / 2))));
+  whir::cuda_check(whir::gpu::eq_full(z, ext_in(scale), reinterpret_cast<E4 *>(out),
+                                      ctx->eq.as<E4>(), ctx->ctx.stream()),
+                   "eq_full");
+  ctx->ctx.sync();
+  API_END
+}
+
+int whir_compress_hi(whir_ctx *ctx, const uint32_t *poly, int k, const uint32_t *point, int kz,
+                     uint32_t *out) {
+  API_BEGIN
+  need(ctx && poly && out, "null argument");
+  need(kz >= 0 && kz <= k && k - kz <= 8, "compress_hi keeps at most 8 variables");
+  whir::gpu::Point z = point_in(point, kz);
+  int ks = k - kz;
+  int s_lo = kz < 10 ? kz : 10;
+  ctx->eq.reserve(sizeof(E4) * (((size_t)1 << s_lo) + ((size_t)1 << (kz - s_lo))));
+  E4 *lo = ctx->eq.as<E4>(), *hi = lo + ((size_t)1 << s_lo);
+  cudaStream_t st = ctx->ctx.stream();
+  whir::cuda_check(whir::gpu::eq_split(z, s_lo, kb::e_one(), lo, hi, st), "eq_split");
+  size_t words = (size_t)4 << ks;
+  unsigned long long *a = acc_buf(ctx, words);
+  whir::cuda_check(whir::gpu::compress_hi(poly, k, ks, lo, s_lo, hi, a, st), "compress_hi");
+  read_acc(ctx, a, words, out);
+  API_END
+}
+
+int whir_compress_lo(whir_ctx *ctx, const uint32_t *poly, int k, const uint32_t *point, int kz,
+                     uint32_t *out) {
+  API_BEGIN
+  need(ctx && poly && out, "null argument");
+  need(kz >= 0 && kz <= k && kz <= 8, "compress_lo fixes at most 8 variables");
+  whir::gpu::Point z = point_in(point, kz);
+  whir::cuda_check(whir::gpu::compress_lo(poly, k, z, reinterpret_cast<E4 *>(out),
+                                          ctx->ctx.stream()),
+                   "compress_lo");
+  ctx->ctx.sync();
+  API_END
+}
+
+int whir_eval_ext(whir_ctx *ctx, const uint32_t *poly, int k, const uint32_t *point,
+                  uint32_t out[4]) {
+  API_BEGIN
+  need(ctx && poly && out, "null argument");
+  need(k >= 0 && k <= 30, "bad k");
+  whir::gpu::Point z = point_in(point, k);
+  int s_lo = k < 10 ? k : 10;
+  ctx->eq.reserve(sizeof(E4) * (((size_t)1 << s_lo) + ((size_t)1 << (k - s_lo))));
+  E4 *lo = ctx->eq.as<E4>(), *hi = lo + ((size_t)1 << s_lo);
+  cudaStream_t st = ctx->ctx.stream();
+  whir::cuda_check(whir::gpu::eq_split(z, s_lo, kb::e_one(), lo, hi, st), "eq_split");
+  unsigned long long *a = acc_buf(ctx, 4);
+  whir::cuda_check(whir::gpu::eval_ext(reinterpret_cast<const E4 *>(poly), k, lo, s_lo, hi, a, st),
+                   "eval_ext");
+  read_acc(ctx, a, 4, out);
+  API_END
+}
+
+int whir_sumcheck_coeffs(whir_ctx *ctx, const uint32_t *poly, const uint32_t *weights, int k,
+                         uint32_t c0[4], uint32_t c2[4]) {
+  API_BEGIN
+  need(ctx && poly && weights && c0 && c2, "null argument");
+  need(k >= 1 && k <= 30, "coeffs needs k >= 1");
+  unsigned long long *a = acc_buf(ctx, 8);
+  whir::cuda_check(whir::gpu::sumcheck_round(reinterpret_cast<const E4 *>(poly),
+                                             reinterpret_cast<const E4 *>(weights),
+                                             (size_t)1 << k, false, kb::e_zero(), nullptr,
+                                             nullptr, true, a, ctx->ctx.stream()),
+                   "round");
+  uint32_t h[8];
+  read_acc(ctx, a, 8, h);
+  memcpy(c0, h, 16);
+  memcpy(c2, h + 4, 16);
+  API_END
+}
+
+int whir_sumcheck_fold(whir_ctx *ctx, const uint32_t *poly, const uint32_t *weights, int k,
+                       const uint32_t r[4], uint32_t *poly_out, uint32_t *weights_out) {
+  API_BEGIN
+  need(ctx && poly && weights && r && poly_out && weights_out, "null argument");
+  need(k >= 1 && k <= 30, "fold needs k >= 1");
+  whir::cuda_check(whir::gpu::sumcheck_round(reinterpret_cast<const E4 *>(poly),
+                                             reinterpret_cast<const E4 *>(weights),
+                                             (size_t)1 << k, true, ext_in(r),
+                                             reinterpret_cast<E4 *>(poly_out),
+                                             reinterpret_cast<E4 *>(weights_out), false, nullptr,
+                                             ctx->ctx.stream()),
+                   "fold");
+  ctx->ctx.sync();
+  API_END
+}
+
+int whir_combine_eqs(whir_ctx *ctx, uint32_t *weights, int k, const uint32_t *points, int n,
+                     const uint32_t alpha[4]) {
+  API_BEGIN
+  need(ctx && weights && alpha && (points || !n) && n >= 0, "bad argument");
+  need(k >= 0 && k <= 24, "bad k");
+  if (n == 0) return WHIR_OK;
+  E4 a = ext_in(alpha), s = kb::e_one();
+  int sl = k / 2;
+  size_t per = ((size_t)1 << sl) + ((size_t)1 << (k - sl));
+  ctx->eq.reserve(sizeof(E4) * per * n);
+  cudaStream_t st = ctx->ctx.stream();
+  for (int t = 0; t < n; t++) {
+    whir::gpu::Point z = point_in(points + (size_t)4 * k * t, k);
+    E4 *tab = ctx->eq.as<E4>() + per * t;
+    whir::cuda_check(whir::gpu::eq_split(z, sl, s, tab, tab + ((size_t)1 << sl), st), "eq_split");
+    s = kb::e_mul(s, a);
+  }
+  whir::cuda_check(whir::gpu::add_eq(reinterpret_cast<E4 *>(weights), k, ctx->eq.as<E4>(), n, st),
+                   "add_eq");
+  ctx->ctx.sync();
+  API_END
+}
+
+static void combine_pows_impl(whir_ctx *ctx, uint32_t *weights, int k, const uint32_t *vars, int n,
+                              const std::vector<E4> &scales) {
+  for (int i = 0; i < n; i++) need(vars[i] < kb::P, "non-canonical field element");
+  size_t bytes = 16 * (size_t)n + 4 * (size_t)n;
+  ctx->small.reserve(bytes);
+  std::vector<uint8_t> h(bytes);
+  memcpy(h.data(), scales.data(), 16 * (size_t)n);
+  memcpy(h.data() + 16 * (size_t)n, vars, 4 * (size_t)n);
+  cudaStream_t st = ctx->ctx.stream();
+  whir::cuda_check(cudaMemcpyAsync(ctx->small.as<uint8_t>(), h.data(), bytes,
+                                   cudaMemcpyHostToDevice, st),
+                   "h2d");
+  whir::cuda_check(whir::gpu::add_pows(reinterpret_cast<E4 *>(weights), k,
+                                       reinterpret_cast<const uint32_t *>(ctx->small.as<uint8_t>() +
+                                                                          16 * (size_t)n),
+                                       ctx->small.as<E4>(), n, st),
+                   "add_pows");
+  ctx->ctx.sync();
+}
+
+int whir_combine_pows(whir_ctx *ctx, uint32_t *weights, int k, const uint32_t *vars, int n,
+                      const uint32_t alpha[4], int shift) {
+  API_BEGIN
+  need(ctx && weights && alpha && (vars || !n) && n >= 0 && shift >= 0, "bad argument");
+  need(k >= 0 && k <= 30, "bad k");
+  if (n == 0) return WHIR_OK;
+  E4 a = ext_in(alpha);
+  std::vector<E4> sc(n);
+  E4 s = kb::e_pow(a, (uint64_t)shift);
+  for (int i = 0; i < n; i++) {
+    sc[i] = s;
+    s = kb::e_mul(s, a);
+  }
+  combine_pows_impl(ctx, weights, k, vars, n, sc);
+  API_END
+}
+
+int whir_combine_pows_scaled(whir_ctx *ctx, uint32_t *weights, int k, const uint32_t *vars,
+                             int n, const uint32_t *scales) {
+  API_BEGIN
+  need(ctx && weights && (vars || !n) && (scales || !n) && n >= 0, "bad argument");
+  need(k >= 0 && k <= 30, "bad k");
+  if (n == 0) return WHIR_OK;
+  std::vector<E4> sc(n);
+  for (int i = 0; i < n; i++) sc[i] = ext_in(scales + 4 * i);
+  combine_pows_impl(ctx, weights, k, vars, n, sc);
+  API_END
+}
+
+int whir_poseidon2_permute(int width, uint32_t *state) {
+  API_BEGIN
+  need(state != nullptr, "null state");
+  need(width == 16 || width == 24, "width must be 16 or 24");
+  for (int i = 0; i < width; i++) need(state[i] < kb::P, "non-canonical field element");
+  whir::poseidon2_permute_host(whir::poseidon2_constants(width), state);
+  API_END
+}
+
+int whir_transcript_new(whir_transcript **out) {
+  API_BEGIN
+  need(out != nullptr, "null out");
+  *out = new whir_transcript();
+  API_END
+}
+int whir_transcript_free(whir_transcript *t) {
+  API_BEGIN
+  delete t;
+  API_END
+}
+int whir_transcript_write(whir_transcript *t, const uint32_t e[4]) {
+  API_BEGIN
+  need(t && e, "null argument");
+  t->t.write_ext(ext_in(e));
+  API_END
+}
+int whir_transcript_write_base(whir_transcript *t, uint32_t v) {
+  API_BEGIN
+  need(t != nullptr, "null transcript");
+  need(v < kb::P, "non-canonical field element");
+  t->t.write_fe(v);
+  API_END
+}
+int whir_transcript_draw(whir_transcript *t, uint32_t out[4]) {
+  API_BEGIN
+  need(t && out, "null argument");
+  ext_out(t->t.draw_ext(), out);
+  API_END
+}
+int whir_transcript_draw_base(whir_transcript *t, uint32_t *out) {
+  API_BEGIN
+  need(t && out, "null argument");
+  *out = t->t.draw_fe();
+  API_END
+}
+int whir_transcript_draw_bits(whir_transcript *t, int bits, size_t *out) {
+  API_BEGIN
+  need(t && out, "null argument");
+  need(bits >= 0 && bits < 31, "bits must satisfy 2^bits < p");
+  *out = t->t.draw_bits(bits);
+  API_END
+}
+int whir_transcript_size(whir_transcript *t, size_t *len) {
+  API_BEGIN
+  need(t && len, "null argument");
+  *len = t->t.bytes().size();
+  API_END
+}
+int whir_transcript_bytes(whir_transcript *t, uint8_t *out, size_t cap) {
+  API_BEGIN
+  need(t && (out || !cap), "null argument");
+  const auto &b = t->t.bytes();
+  if (b.size() > cap) throw WhirError(-4, "proof buffer too small");
+  memcpy(out, b.data(), b.size());
+  API_END
+}
+
+int whir_prover_new(whir_ctx *ctx, const whir_params *params, whir_prover **out) {
+  API_BEGIN
+  need(ctx && params && out, "null argument");
+  whir::Params p{params->k,         params->folding,   params->rate,
+                 params->initial_reduction, params->soundness, params->security_level};
+  *out = new whir_prover(ctx, p);
+  API_END
+}
+int whir_prover_free(whir_prover *p) {
+  API_BEGIN
+  if (p) p->ctx->ctx.sync();
+  delete p;
+  API_END
+}
+static std::vector<int> ks_in(const int32_t *poly_k, int n_polys) {
+  need(poly_k && n_polys > 0 && n_polys < (1 << 20), "bad polynomial list");
+  std::vector<int> v(poly_k, poly_k + n_polys);
+  for (int k : v) need(k >= 0 && k <= 30, "bad polynomial size");
+  return v;
+}
+int whir_commit(whir_prover *p, whir_transcript *t, const uint32_t *polys, int on_device,
+                const int32_t *poly_k, int n_polys) {
+  API_BEGIN
+  need(p && t && polys, "null argument");
+  std::vector<int> ks = ks_in(poly_k, n_polys);
+  p->p.commit(t->t, polys, on_device != 0, ks);
+  API_END
+}
+int whir_stack_eval(whir_prover *p, whir_transcript *t, int id, const uint32_t *point,
+                    uint32_t eval[4]) {
+  API_BEGIN
+  need(p && t && point && eval, "null argument");
+  need(id >= 0, "bad id");
+  ext_out(p->p.eval(t->t, id, reinterpret_cast<const E4 *>(point)), eval);
+  API_END
+}
+int whir_open(whir_prover *p, whir_transcript *t) {
+  API_BEGIN
+  need(p && t, "null argument");
+  p->p.open(t->t);
+  API_END
+}
+int whir_prove(whir_prover *p, whir_transcript *t, const uint32_t *polys, int on_device,
+               const int32_t *poly_k, int n_polys, const int32_t *group_n, int n_groups,
+               const int32_t *group_ids) {
+  API_BEGIN
+  need(p && t && polys, "null argument");
+  std::vector<int> ks = ks_in(poly_k, n_polys);
+  need(n_groups >= 0 && (group_n || !n_groups), "bad claim groups");
+  std::vector<std::vector<int>> groups;
+  size_t off = 0;
+  for (int g = 0; g < n_groups; g++) {
+    need(group_n[g] > 0, "empty claim group");
+    std::vector<int> ids(group_ids + off, group_ids + off + group_n[g]);
+    for (int id : ids) need(id >= 0 && id < n_polys, "claim id out of range");
+    off += group_n[g];
+    groups.push_back(ids);
+  }
+  p->p.prove(t->t, polys, on_device != 0, ks, groups);
+  API_END
+}
+
+int whir_prof_enable(whir_ctx *ctx, int on) {
+  API_BEGIN
+  need(ctx != nullptr, "null context");
+  ctx->ctx.prof_enable(on != 0);
+  API_END
+}
+int whir_prof_read(whir_ctx *ctx, int klass, double *ms, long *launches, double *bytes) {
+  API_BEGIN
+  need(ctx && ms && launches && bytes, "null argument");
+  need(klass >= 0 && klass < Context::K_NCLASS, "bad kernel class");
+  ctx->ctx.prof_read(klass, ms, launches, bytes);
+  API_END
+}
+
+}  // extern "C"

@@ -1,0 +1,81 @@
+// Launchers of the sm_103a kernels.  Every pointer is a device pointer unless
+// its name ends in _h; every launch goes to the given stream and returns
+// without synchronising.  Field words are Montgomery form (see kb.cuh).
+#pragma once
+#include <cuda_runtime.h>
+#include <stddef.h>
+#include <stdint.h>
+
+#include "kb.cuh"
+
+namespace whir {
+namespace gpu {
+
+// ---- one-time device set-up (constants, twiddle tables) ----
+cudaError_t init_device_tables();
+
+// ---- RS encoding: p3 TwoAdicSubgroupDft::dft_batch (crates/whir/src/whir.rs:34,59) ----
+// out[i][c] = sum_{r < h_in} in[r][c] * w^(r i), w = two_adic_generator(log_h),
+// rows of `width` words, natural order; rows >= h_in are zero.  `scratch`
+// holds 2^log_h * width words when log_h > 11 (two passes), else unused.
+cudaError_t dft_batch(const uint32_t *in, size_t h_in, size_t width, int log_h, uint32_t *out,
+                      uint32_t *scratch, cudaStream_t st);
+
+// ---- Merkle (crates/merkle/src/poseidon_packed.rs) ----
+// leaf digests: PaddingFreeSponge<P24, 24, 16, 8> over each row of row_len words
+cudaError_t hash_rows(const uint32_t *rows, size_t n_rows, int row_len, uint32_t *digests,
+                      cudaStream_t st);
+// all levels above the leaves: level l+1 node i = C(level l node i, node i + n/2)
+// nodes: level 0 (2^log_h digests) first, then each level in turn
+cudaError_t build_tree(uint32_t *nodes, int log_h, cudaStream_t st);
+// per query: the leaf row then log_h sibling digests bottom-up
+cudaError_t gather_openings(const uint32_t *rows, int row_len, const uint32_t *nodes, int log_h,
+                            const uint32_t *idx, int n, uint32_t *out, cudaStream_t st);
+KB_HD size_t tree_words(int log_h) { return (((size_t)2 << log_h) - 1) * 8; }
+KB_HD size_t level_offset_words(int log_h, int level) {
+  return (((size_t)2 << log_h) - ((size_t)2 << (log_h - level))) * 8;
+}
+
+// ---- eq tables and sumcheck passes (crates/poly, crates/whir/src/sumcheck) ----
+constexpr int MAX_VARS = 32;
+struct Point {
+  int k;
+  kb::E4 z[MAX_VARS];
+};
+// eq(z) * scale as two split tables: lo over z[0..s), hi over z[s..k) (scale in hi)
+// lo/hi hold 2^s and 2^(k-s) E4.
+cudaError_t eq_split(const Point &z, int s, kb::E4 scale, kb::E4 *lo, kb::E4 *hi,
+                     cudaStream_t st);
+// full table eq(z) * scale of 2^k entries (k <= 24)
+cudaError_t eq_full(const Point &z, kb::E4 scale, kb::E4 *out, kb::E4 *tmp, cudaStream_t st);
+
+// SplitEq::compress_hi (crates/poly/src/eq.rs:290-398) over a base poly:
+// acc[j] += sum_h eq(zrest)[h] * P[h * 2^ks + j]; acc is u64[2^ks][4] of
+// unreduced canonical sums (reduce mod p on read).  eq tables from eq_split.
+cudaError_t compress_hi(const uint32_t *poly, int k, int ks, const kb::E4 *eq_lo, int s_lo,
+                        const kb::E4 *eq_hi, unsigned long long *acc, cudaStream_t st);
+// SplitEq::compress_lo_into (eq.rs:491-539): out[i] = sum_j eq(rs)[j] * P[i*2^ks + j]
+cudaError_t compress_lo(const uint32_t *poly, int k, const Point &rs, kb::E4 *out,
+                        cudaStream_t st);
+// w[i] += sum_t lo_t[i & (2^s-1)] * hi_t[i >> s] for n_tables split eq tables
+// stored back to back (lo0, hi0, lo1, hi1, ...), s = k / 2, each lo 2^s and
+// hi 2^(k-s) entries.
+cudaError_t add_eq(kb::E4 *w, int k, const kb::E4 *tables, int n_tables, cudaStream_t st);
+// w[i] += sum_t scale_t * var_t^i  (pow::combine_pows(_scaled), combine.rs:408-468)
+cudaError_t add_pows(kb::E4 *w, int k, const uint32_t *vars, const kb::E4 *scales, int n,
+                     cudaStream_t st);
+// one sumcheck round (expr.rs:14-27, poly.rs:131-142): optionally fold both
+// arrays by r into (p_out, w_out), then add (c0, c2) of the result into acc
+// (u64[8], unreduced canonical) when coeffs != 0.
+cudaError_t sumcheck_round(const kb::E4 *p_in, const kb::E4 *w_in, size_t n_in, bool fold,
+                           kb::E4 r, kb::E4 *p_out, kb::E4 *w_out, bool coeffs,
+                           unsigned long long *acc, cudaStream_t st);
+// <eq(z), poly> for an extension poly (SplitEq::eval_ext, eq.rs:179-250) -> acc u64[4]
+cudaError_t eval_ext(const kb::E4 *poly, int k, const kb::E4 *eq_lo, int s_lo,
+                     const kb::E4 *eq_hi, unsigned long long *acc, cudaStream_t st);
+// out[q] = <eq(rs), row(idx[q])> over base rows (fold_with_code evals, prover.rs:497-506)
+cudaError_t row_evals(const uint32_t *rows, int row_len, const uint32_t *idx, int n,
+                      const Point &rs, kb::E4 *out, cudaStream_t st);
+
+}  // namespace gpu
+}  // namespace whir

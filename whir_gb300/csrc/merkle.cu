@@ -1,0 +1,147 @@
+// Merkle commitment kernels: leaf hashing (width-24 sponge), tree ascent
+// (width-16 truncated-permutation compression, halves pairing) and the
+// opening gather.  Tree shape and hashing follow
+// crates/merkle/src/poseidon_packed.rs:98-143,269-304,344-384 and
+// crates/merkle/src/poseidon.rs:33-74.
+#include "kernels.h"
+#include "p2_device.cuh"
+#include "poseidon2_host.h"
+
+namespace whir {
+namespace gpu {
+
+static cudaError_t upload_p2(int width) {
+  const Poseidon2Constants &c = poseidon2_constants(width);
+  uint32_t buf[8 * 24 + 23 + 24];
+  int n = 0;
+  for (int r = 0; r < 8; r++)
+    for (int i = 0; i < width; i++) buf[n++] = c.ext_rc[r][i];
+  for (int r = 0; r < c.rounds_p; r++) buf[n++] = c.int_rc[r];
+  for (int i = 0; i < width; i++) buf[n++] = c.diag[i];
+  if (width == 16) return cudaMemcpyToSymbol(c_p2_16, buf, n * 4);
+  return cudaMemcpyToSymbol(c_p2_24, buf, n * 4);
+}
+
+cudaError_t init_poseidon2_tables() {
+  cudaError_t e = upload_p2(16);
+  if (e != cudaSuccess) return e;
+  return upload_p2(24);
+}
+
+// One row per thread; rows of 16 words are one permutation, rows of 64 words
+// four (PaddingFreeSponge: overwrite the 16 rate lanes, permute).
+template <int ROW>
+__global__ void __launch_bounds__(128) hash_rows_fixed(const uint32_t *__restrict__ rows,
+                                                       size_t n_rows,
+                                                       uint32_t *__restrict__ digests) {
+  size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n_rows) return;
+  const uint4 *src = reinterpret_cast<const uint4 *>(rows + i * ROW);
+  uint32_t s[24];
+#pragma unroll
+  for (int j = 16; j < 24; j++) s[j] = 0;
+#pragma unroll 1
+  for (int chunk = 0; chunk < ROW / 16; chunk++) {
+#pragma unroll
+    for (int q = 0; q < 4; q++) {
+      uint4 v = __ldg(src + chunk * 4 + q);
+      s[4 * q] = v.x;
+      s[4 * q + 1] = v.y;
+      s[4 * q + 2] = v.z;
+      s[4 * q + 3] = v.w;
+    }
+    p2_permute<24>(s);
+  }
+  uint4 *dst = reinterpret_cast<uint4 *>(digests + i * 8);
+  dst[0] = make_uint4(s[0], s[1], s[2], s[3]);
+  dst[1] = make_uint4(s[4], s[5], s[6], s[7]);
+}
+
+// Any row length (small foldings): the trailing partial chunk overwrites only
+// its lanes and is permuted; an empty trailing chunk is not.
+__global__ void hash_rows_generic(const uint32_t *__restrict__ rows, size_t n_rows, int row_len,
+                                  uint32_t *__restrict__ digests) {
+  size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n_rows) return;
+  const uint32_t *src = rows + i * row_len;
+  uint32_t s[24];
+#pragma unroll
+  for (int j = 0; j < 24; j++) s[j] = 0;
+  int pos = 0;
+  while (pos < row_len) {
+    int take = row_len - pos < 16 ? row_len - pos : 16;
+    for (int j = 0; j < take; j++) s[j] = src[pos + j];
+    pos += take;
+    p2_permute<24>(s);
+  }
+  for (int j = 0; j < 8; j++) digests[i * 8 + j] = s[j];
+}
+
+cudaError_t hash_rows(const uint32_t *rows, size_t n_rows, int row_len, uint32_t *digests,
+                      cudaStream_t st) {
+  if (n_rows == 0) return cudaSuccess;
+  const int T = 128;
+  unsigned grid = (unsigned)((n_rows + T - 1) / T);
+  // the fixed-width kernels use 16-byte vector loads and stores
+  bool aligned = (((uintptr_t)rows | (uintptr_t)digests) & 15) == 0;
+  if (aligned && row_len == 16) hash_rows_fixed<16><<<grid, T, 0, st>>>(rows, n_rows, digests);
+  else if (aligned && row_len == 64) hash_rows_fixed<64><<<grid, T, 0, st>>>(rows, n_rows, digests);
+  else hash_rows_generic<<<grid, T, 0, st>>>(rows, n_rows, row_len, digests);
+  return cudaGetLastError();
+}
+
+__global__ void __launch_bounds__(128) compress_level(const uint32_t *__restrict__ src,
+                                                      uint32_t *__restrict__ dst, size_t half) {
+  size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= half) return;
+  const uint4 *a = reinterpret_cast<const uint4 *>(src + i * 8);
+  const uint4 *b = reinterpret_cast<const uint4 *>(src + (i + half) * 8);
+  uint4 a0 = __ldg(a), a1 = __ldg(a + 1), b0 = __ldg(b), b1 = __ldg(b + 1);
+  uint32_t s[16] = {a0.x, a0.y, a0.z, a0.w, a1.x, a1.y, a1.z, a1.w,
+                    b0.x, b0.y, b0.z, b0.w, b1.x, b1.y, b1.z, b1.w};
+  p2_permute<16>(s);
+  uint4 *d = reinterpret_cast<uint4 *>(dst + i * 8);
+  d[0] = make_uint4(s[0], s[1], s[2], s[3]);
+  d[1] = make_uint4(s[4], s[5], s[6], s[7]);
+}
+
+cudaError_t build_tree(uint32_t *nodes, int log_h, cudaStream_t st) {
+  const int T = 128;
+  for (int l = 0; l < log_h; l++) {
+    size_t half = ((size_t)1 << (log_h - l)) / 2;
+    uint32_t *src = nodes + level_offset_words(log_h, l);
+    uint32_t *dst = nodes + level_offset_words(log_h, l + 1);
+    compress_level<<<(unsigned)((half + T - 1) / T), T, 0, st>>>(src, dst, half);
+  }
+  return cudaGetLastError();
+}
+
+__global__ void gather_openings_kernel(const uint32_t *__restrict__ rows, int row_len,
+                                       const uint32_t *__restrict__ nodes, int log_h,
+                                       const uint32_t *__restrict__ idx, int n,
+                                       uint32_t *__restrict__ out) {
+  int q = blockIdx.x;
+  if (q >= n) return;
+  size_t index = idx[q];
+  size_t per = (size_t)row_len + 8 * (size_t)log_h;
+  uint32_t *o = out + q * per;
+  for (int j = threadIdx.x; j < row_len; j += blockDim.x) o[j] = rows[index * row_len + j];
+  // sibling at level l is index_l ^ mid_l with mid_l = 2^(log_h - l - 1)
+  for (int t = threadIdx.x; t < 8 * log_h; t += blockDim.x) {
+    int l = t / 8, w = t % 8;
+    size_t mask = ((size_t)1 << (log_h - l)) - 1;  // index at level l is index & mask
+    size_t mid = (size_t)1 << (log_h - l - 1);
+    size_t sib = (index & mask) ^ mid;
+    o[row_len + t] = nodes[level_offset_words(log_h, l) + sib * 8 + w];
+  }
+}
+
+cudaError_t gather_openings(const uint32_t *rows, int row_len, const uint32_t *nodes, int log_h,
+                            const uint32_t *idx, int n, uint32_t *out, cudaStream_t st) {
+  if (n == 0) return cudaSuccess;
+  gather_openings_kernel<<<n, 128, 0, st>>>(rows, row_len, nodes, log_h, idx, n, out);
+  return cudaGetLastError();
+}
+
+}  // namespace gpu
+}  // namespace whir

@@ -1,0 +1,1015 @@
+// GPU WHIR prover host orchestration (see prover.h).
+#include "prover.h"
+
+#include <math.h>
+#include <string.h>
+
+#include <algorithm>
+#include <functional>
+#include <map>
+#include <unordered_map>
+
+namespace whir {
+
+using kb::E4;
+using namespace kb;
+
+// ---------------- params (crates/whir/src/params.rs) ----------------
+static const double LOG2_10 = 3.321928094887362347870319429489390175864831393;
+static double log_eta(int s, int lir) {
+  if (s == 0) return 0.;
+  if (s == 1) return -(0.5 * lir + LOG2_10 + 1.);
+  return -(lir + LOG2_10 + 1.);
+}
+static double list_size_bits(int s, int log_degree, int lir) {
+  double le = log_eta(s, lir);
+  if (s == 0) return 0.;
+  if (s == 1) return lir / 2. - (1. + le);
+  return (double)(log_degree + lir) - le;
+}
+static double log_1_delta(int s, int lir) {
+  double eta = ::pow(2., log_eta(s, lir));
+  double rate = 1. / (double)(1u << lir);
+  double delta = s == 0 ? 0.5 * (1. - rate) : s == 1 ? 1. - sqrt(rate) - eta : 1. - rate - eta;
+  return log2(1. - delta);
+}
+int n_stir_queries(int s, int security, int lir) {
+  return (int)ceil(-(double)security / log_1_delta(s, lir));
+}
+int n_ood_queries(int s, int security, int log_degree, int lir, int field_bits) {
+  if (s == 0) return 0;
+  for (int n = 1; n < 64; n++) {
+    double err = 2. * list_size_bits(s, log_degree, lir) + (double)(log_degree * n);
+    if ((double)(n * field_bits) + 1. - err >= (double)security) return n;
+  }
+  throw WhirError(-1, "could not find an appropriate number of OOD samples");
+}
+void number_of_rounds(int folding, int k, int *n_rounds, int *final_rounds) {
+  if (k <= 6) {
+    *n_rounds = 0;
+    *final_rounds = k - folding;
+    return;
+  }
+  int nr = (k - 6 + folding - 1) / folding;
+  *final_rounds = k - nr * folding;
+  *n_rounds = nr - 1;
+}
+
+uint32_t two_adic_generator(int bits) {
+  uint32_t g = from_canonical(0x6ac49f88u);  // 3^127, order 2^24
+  for (int i = bits; i < 24; i++) g = mul(g, g);
+  return g;
+}
+
+void cuda_check(cudaError_t e, const char *what) {
+  if (e != cudaSuccess)
+    throw WhirError(-2, std::string(what) + ": " + cudaGetErrorString(e));
+}
+
+// ---------------- device buffers, context ----------------
+DeviceBuffer::~DeviceBuffer() {
+  if (ptr_) cudaFree(ptr_);
+}
+void DeviceBuffer::reserve(size_t bytes) {
+  if (bytes <= bytes_) return;
+  if (ptr_) cudaFree(ptr_);
+  ptr_ = nullptr;
+  bytes_ = 0;
+  cudaError_t e = cudaMalloc(&ptr_, bytes ? bytes : 16);
+  if (e != cudaSuccess) {
+    ptr_ = nullptr;
+    throw WhirError(-3, std::string("device allocation failed: ") + cudaGetErrorString(e));
+  }
+  bytes_ = bytes;
+}
+
+Context::Context(int device) : device_(device) {
+  cuda_check(cudaSetDevice(device), "cudaSetDevice");
+  cuda_check(cudaStreamCreateWithFlags(&stream_, cudaStreamNonBlocking), "cudaStreamCreate");
+  cuda_check(gpu::init_device_tables(), "device tables");
+}
+Context::~Context() {
+  cudaSetDevice(device_);
+  for (auto &e : evs_) {
+    cudaEventDestroy(e.a);
+    cudaEventDestroy(e.b);
+  }
+  for (auto e : free_events_) cudaEventDestroy(e);
+  if (pinned_) cudaFreeHost(pinned_);
+  if (stream_) cudaStreamDestroy(stream_);
+}
+void *Context::pinned(size_t bytes) {
+  if (bytes > pinned_bytes_) {
+    cuda_check(cudaStreamSynchronize(stream_), "sync");
+    if (pinned_) cudaFreeHost(pinned_);
+    pinned_ = nullptr;
+    size_t n = std::max(bytes, (size_t)1 << 20);
+    cuda_check(cudaMallocHost(&pinned_, n), "cudaMallocHost");
+    pinned_bytes_ = n;
+  }
+  return pinned_;
+}
+void Context::sync() { cuda_check(cudaStreamSynchronize(stream_), "stream sync"); }
+
+cudaEvent_t Context::take_event() {
+  if (!free_events_.empty()) {
+    cudaEvent_t e = free_events_.back();
+    free_events_.pop_back();
+    return e;
+  }
+  cudaEvent_t e;
+  cuda_check(cudaEventCreate(&e), "cudaEventCreate");
+  return e;
+}
+void Context::prof_enable(bool on) { prof_ = on; }
+void Context::prof_begin(int klass) {
+  if (!prof_) return;
+  open_klass_ = klass;
+  open_ev_ = take_event();
+  cudaEventRecord(open_ev_, stream_);
+}
+void Context::prof_end(int klass, double bytes) {
+  if (!prof_ || open_klass_ != klass) return;
+  cudaEvent_t b = take_event();
+  cudaEventRecord(b, stream_);
+  evs_.push_back(Ev{open_ev_, b, klass, bytes});
+  open_klass_ = -1;
+}
+void Context::prof_read(int klass, double *ms, long *launches, double *bytes) {
+  if (!evs_.empty()) {
+    sync();
+    for (auto &e : evs_) {
+      float t = 0;
+      cudaEventElapsedTime(&t, e.a, e.b);
+      acc_ms_[e.klass] += t;
+      acc_n_[e.klass] += 1;
+      acc_bytes_[e.klass] += e.bytes;
+      free_events_.push_back(e.a);
+      free_events_.push_back(e.b);
+    }
+    evs_.clear();
+  }
+  *ms = acc_ms_[klass];
+  *launches = acc_n_[klass];
+  *bytes = acc_bytes_[klass];
+  acc_ms_[klass] = 0;
+  acc_n_[klass] = 0;
+  acc_bytes_[klass] = 0;
+}
+
+// ---------------- host helpers ----------------
+static E4 e_inv2() { return e_from(inv(from_canonical(2))); }
+static void lagrange012(const E4 &r, E4 w[3]) {
+  E4 it = e_inv2(), one = e_one(), two = e_dbl(e_one());
+  w[0] = e_mul(e_mul(e_sub(r, one), e_sub(r, two)), it);
+  w[1] = e_mul(r, e_sub(two, r));
+  w[2] = e_mul(e_mul(r, e_sub(r, one)), it);
+}
+static E4 extrapolate012(const E4 &e0, const E4 &e1, const E4 &e2, const E4 &r) {
+  E4 w[3];
+  lagrange012(r, w);
+  return e_add(e_add(e_mul(e0, w[0]), e_mul(e1, w[1])), e_mul(e2, w[2]));
+}
+static void eq_host(const E4 *z, int k, const E4 &scale, E4 *out) {
+  out[0] = scale;
+  for (int i = 0; i < k; i++) {
+    size_t h = (size_t)1 << i;
+    for (size_t j = 0; j < h; j++) {
+      E4 hi = e_mul(out[j], z[i]);
+      out[j + h] = hi;
+      out[j] = e_sub(out[j], hi);
+    }
+  }
+}
+static E4 eval_eq_xy(const E4 *x, const E4 *y, int n) {
+  E4 acc = e_one();
+  for (int i = 0; i < n; i++) {
+    E4 t = e_sub(e_sub(e_dbl(e_mul(y[i], x[i])), x[i]), y[i]);
+    acc = e_mul(acc, e_add(t, e_one()));
+  }
+  return acc;
+}
+static E4 horner(const E4 *c, size_t n, const E4 &x) {
+  E4 acc = e_zero();
+  for (size_t i = n; i-- > 0;) acc = e_add(e_mul(acc, x), c[i]);
+  return acc;
+}
+static void expand(E4 *out, int k, E4 v) {
+  for (int i = 0; i < k; i++) {
+    out[i] = v;
+    v = e_sq(v);
+  }
+}
+static E4 eval_ext_small(const E4 *poly, int k, const E4 *z) {
+  std::vector<E4> eq((size_t)1 << k);
+  eq_host(z, k, e_one(), eq.data());
+  E4 acc = e_zero();
+  for (size_t i = 0; i < eq.size(); i++) acc = e_add(acc, e_mul(eq[i], poly[i]));
+  return acc;
+}
+static size_t ipow3(int r) {
+  size_t v = 1;
+  while (r--) v *= 3;
+  return v;
+}
+static E4 reduce_acc(const unsigned long long *a) {
+  E4 r;
+  for (int c = 0; c < 4; c++) r.c[c] = (uint32_t)(a[c] % P);
+  return r;
+}
+
+// ---------------- encode + commit ----------------
+void encode_commit(Context &ctx, const uint32_t *src, int k, int rate, int folding, int dim,
+                   uint32_t *codeword, uint32_t *scratch, uint32_t *nodes, DeviceTree *out) {
+  cudaStream_t st = ctx.stream();
+  int log_h = k + rate - folding;
+  size_t width = (size_t)dim << folding, h_in = (size_t)1 << (k - folding);
+  size_t rows = (size_t)1 << log_h;
+  ctx.prof_begin(Context::K_DFT);
+  cuda_check(gpu::dft_batch(src, h_in, width, log_h, codeword, scratch, st), "dft_batch");
+  ctx.prof_end(Context::K_DFT, 4.0 * (double)(h_in * width + rows * width));
+  ctx.prof_begin(Context::K_LEAF);
+  cuda_check(gpu::hash_rows(codeword, rows, (int)width, nodes, st), "hash_rows");
+  ctx.prof_end(Context::K_LEAF, 4.0 * (double)(rows * width + rows * 8));
+  ctx.prof_begin(Context::K_TREE);
+  cuda_check(gpu::build_tree(nodes, log_h, st), "build_tree");
+  ctx.prof_end(Context::K_TREE, 32.0 * (double)(2 * rows - 2 + rows - 1));
+  uint32_t *h = (uint32_t *)ctx.pinned(64);
+  cuda_check(cudaMemcpyAsync(h, nodes + gpu::tree_words(log_h) - 8, 32, cudaMemcpyDeviceToHost, st),
+             "root copy");
+  ctx.sync();
+  out->rows = codeword;
+  out->nodes = nodes;
+  out->log_h = log_h;
+  out->row_len = (int)width;
+  memcpy(out->root, h, 32);
+}
+
+// ---------------- prover state ----------------
+namespace {
+
+struct SvoClaim {
+  int poly;
+  int k;
+  std::vector<E4> point;
+  std::vector<E4> compressed;  // 2^ks
+  std::vector<E4> partial;     // l = 1..ks, 2^l each, concatenated
+  E4 eval;
+};
+inline size_t partial_off(int l) { return ((size_t)1 << l) - 2; }
+
+struct VirtClaim {
+  std::vector<E4> point;
+  E4 eval;
+  std::vector<E4> acc;
+};
+
+struct LayEntry {
+  int nbits;
+  uint8_t bits[32];
+  int poly;
+  size_t index;
+};
+
+}  // namespace
+
+struct Prover::Impl {
+  Context *ctx;
+  Params p;
+  int ks;
+  // layout
+  int n_polys = 0;
+  std::vector<int> pk;
+  std::vector<LayEntry> lay;
+  std::vector<size_t> poly_off;  // word offset of each poly inside the stacked poly
+  // device memory
+  DeviceBuffer stacked, cw0, tree0, scratch, cw[2], trees[2], sp[2], sw[2], eqbuf, acc, small,
+      gather;
+  DeviceTree t0, tr[2];
+  int cur_tree = -1;  // index into tr of the latest round commitment
+  // claims
+  std::vector<SvoClaim> claims;
+  std::vector<VirtClaim> virt;
+  // sumcheck state
+  E4 sum, alpha;
+  std::vector<E4> rs;
+  int kc = 0;           // variables of the expression
+  int ping = 0;         // sp[ping]/sw[ping] hold the arrays
+  bool pending = false; // fold by pending_r not applied yet
+  E4 pending_r;
+
+  cudaStream_t st() const { return ctx->stream(); }
+
+  size_t acc_size() const {
+    size_t s = 0;
+    for (int r = 0; r < ks; r++) s += 2 * ipow3(r);
+    return s;
+  }
+
+  // ---- layout (ProverStack::layout, prover.rs:92-124) ----
+  void make_layout() {
+    std::vector<int> order(n_polys);
+    for (int i = 0; i < n_polys; i++) order[i] = i;
+    std::stable_sort(order.begin(), order.end(), [&](int a, int b) { return pk[a] < pk[b]; });
+    size_t total = 0;
+    for (int i = 0; i < n_polys; i++) total += (size_t)1 << pk[i];
+    int k = 0;
+    while (((size_t)1 << k) < total) k++;
+    if (k != p.k) throw WhirError(-1, "stacked layout size does not match params.k");
+    if (k < ks) throw WhirError(-1, "k smaller than folding");
+    lay.assign(n_polys, LayEntry{});
+    size_t off = 0;
+    for (int t = 0; t < n_polys; t++) {
+      int id = order[n_polys - 1 - t];
+      LayEntry &e = lay[t];
+      e.poly = id;
+      e.nbits = k - pk[id];
+      e.index = off >> pk[id];
+      for (int b = 0; b < e.nbits; b++) e.bits[b] = (e.index >> b) & 1;
+      off += (size_t)1 << pk[id];
+    }
+    // BTreeMap<Selector, _> order: Vec<bool> compared lexicographically
+    std::sort(lay.begin(), lay.end(), [](const LayEntry &a, const LayEntry &b) {
+      int n = std::min(a.nbits, b.nbits);
+      for (int i = 0; i < n; i++)
+        if (a.bits[i] != b.bits[i]) return a.bits[i] < b.bits[i];
+      return a.nbits < b.nbits;
+    });
+    poly_off.assign(n_polys, 0);
+    for (auto &e : lay) poly_off[e.poly] = e.index << pk[e.poly];
+  }
+
+  // ---- workspace ----
+  void reserve() {
+    int k = p.k, f = p.folding;
+    size_t cw0_words = ((size_t)1 << (k + p.rate - f)) << f;
+    stacked.reserve(4 * ((size_t)1 << k));
+    cw0.reserve(4 * cw0_words);
+    tree0.reserve(4 * gpu::tree_words(k + p.rate - f));
+    size_t scratch_words = cw0_words;
+    int n_rounds, fin;
+    number_of_rounds(f, k, &n_rounds, &fin);
+    size_t max_cw = 16, max_tree = 8;
+    for (int r = 0; r < n_rounds; r++) {
+      int kfd, this_rate, prev_rate;
+      round_params(r, &kfd, &this_rate, &prev_rate);
+      int kp = k - f * (r + 1);
+      int log_h = kp + this_rate - f;
+      size_t words = ((size_t)4 << f) << log_h;
+      max_cw = std::max(max_cw, words);
+      max_tree = std::max(max_tree, gpu::tree_words(log_h));
+    }
+    scratch_words = std::max(scratch_words, max_cw);
+    scratch.reserve(4 * scratch_words);
+    for (int i = 0; i < 2; i++) {
+      cw[i].reserve(4 * max_cw);
+      trees[i].reserve(4 * max_tree);
+      size_t n = (size_t)1 << (k - f);
+      sp[i].reserve(sizeof(E4) * n);
+      sw[i].reserve(sizeof(E4) * n);
+    }
+    eqbuf.reserve(sizeof(E4) * (size_t)64 * 8192);
+    acc.reserve(8 * 4096);
+    small.reserve(1 << 20);
+    gather.reserve((size_t)4 * 4096 * (((size_t)4 << f) + 8 * 32));
+  }
+
+  void round_params(int round, int *kfd, int *this_rate, int *prev_rate) const {
+    int prev_red = round == 0 ? 0 : p.initial_reduction + round - 1;
+    int this_red = p.initial_reduction + round;
+    int k_domain = p.rate + p.k - prev_red;
+    *kfd = k_domain - p.folding;
+    *prev_rate = p.rate + round * p.folding - prev_red;
+    *this_rate = p.rate + (round + 1) * p.folding - this_red;
+  }
+
+  // ---- SVO claim (SvoPoint::new + eval, svo.rs:64-91) ----
+  void svo_claim(SvoClaim &c, const uint32_t *poly_dev, int kp, const E4 *point) {
+    c.k = kp;
+    c.point.assign(point, point + kp);
+    int nz = kp - ks;
+    gpu::Point z;
+    z.k = nz;
+    for (int i = 0; i < nz; i++) z.z[i] = point[ks + i];
+    int s_lo = std::min(10, nz);
+    E4 *lo = eqbuf.as<E4>(), *hi = lo + ((size_t)1 << s_lo);
+    cuda_check(gpu::eq_split(z, s_lo, e_one(), lo, hi, st()), "eq_split");
+    size_t na = (size_t)4 << ks;
+    unsigned long long *a = acc.as<unsigned long long>();
+    cuda_check(cudaMemsetAsync(a, 0, 8 * na, st()), "memset");
+    ctx->prof_begin(Context::K_SUMCHECK);
+    cuda_check(gpu::compress_hi(poly_dev, kp, ks, lo, s_lo, hi, a, st()), "compress_hi");
+    ctx->prof_end(Context::K_SUMCHECK, 4.0 * (double)((size_t)1 << kp));
+    unsigned long long *h = (unsigned long long *)ctx->pinned(8 * na);
+    cuda_check(cudaMemcpyAsync(h, a, 8 * na, cudaMemcpyDeviceToHost, st()), "d2h");
+    ctx->sync();
+    size_t n = (size_t)1 << ks;
+    c.compressed.resize(n);
+    for (size_t j = 0; j < n; j++) c.compressed[j] = reduce_acc(h + 4 * j);
+    std::vector<E4> eq(n);
+    eq_host(point, ks, e_one(), eq.data());
+    c.eval = e_zero();
+    for (size_t j = 0; j < n; j++) c.eval = e_add(c.eval, e_mul(eq[j], c.compressed[j]));
+    c.partial.assign(partial_off(ks + 1), e_zero());
+    for (int l = 1; l <= ks; l++) {  // svo_partial_evals (svo.rs:18-38)
+      size_t na2 = (size_t)1 << l, nr = (size_t)1 << (ks - l);
+      std::vector<E4> er(nr);
+      eq_host(point + l, ks - l, e_one(), er.data());
+      E4 *out = c.partial.data() + partial_off(l);
+      for (size_t x = 0; x < na2; x++) {
+        E4 s = e_zero();
+        for (size_t r = 0; r < nr; r++) s = e_add(s, e_mul(c.compressed[x + na2 * r], er[r]));
+        out[x] = s;
+      }
+    }
+  }
+
+  // Svo::calculate_accumulators for one claim weighted by `w` (svo.rs:225-278);
+  // accumulators are linear in the weighted partial evals, so summing per
+  // claim equals the reference's per-point grouping.
+  void accumulate(std::vector<E4> &accv, const SvoClaim &c, const E4 &w) const {
+    size_t off = 0;
+    std::vector<E4> eq, u;
+    for (int r = 0; r < ks; r++) {
+      int l = r + 1;
+      size_t n = ipow3(r), na = (size_t)1 << l;
+      const E4 *pe = c.partial.data() + partial_off(l);
+      eq.resize(na);
+      u.resize(l);
+      std::vector<E4> wpe(na);
+      for (size_t a = 0; a < na; a++) wpe[a] = e_mul(w, pe[a]);
+      for (int which = 0; which < 2; which++)
+        for (size_t t = 0; t < n; t++) {
+          size_t tt = t;
+          for (int i = 0; i < r; i++) {
+            u[i] = e_from(from_canonical((uint32_t)(tt % 3)));
+            tt /= 3;
+          }
+          u[r] = which ? e_dbl(e_one()) : e_zero();
+          eq_host(u.data(), l, e_one(), eq.data());
+          E4 dot = e_zero();
+          for (size_t a = 0; a < na; a++) dot = e_add(dot, e_mul(wpe[a], eq[a]));
+          E4 v = e_mul(eval_eq_xy(u.data(), c.point.data(), l), dot);
+          accv[off + which * n + t] = e_add(accv[off + which * n + t], v);
+        }
+      off += 2 * n;
+    }
+  }
+
+  const uint32_t *poly_dev(int id) const { return stacked.as<uint32_t>() + poly_off[id]; }
+
+  // claims in layout order: (claim index, layout entry)
+  std::vector<std::pair<int, int>> claims_layout_order() const {
+    std::vector<std::pair<int, int>> v;
+    for (int e = 0; e < n_polys; e++)
+      for (int c = 0; c < (int)claims.size(); c++)
+        if (claims[c].poly == lay[e].poly) v.push_back({c, e});
+    return v;
+  }
+
+  // ---- write_virtual_eval (prover.rs:232-277) ----
+  void write_virtual_eval(Transcript &ts) {
+    VirtClaim v;
+    v.point.resize(p.k);
+    expand(v.point.data(), p.k, ts.draw_ext());
+    v.eval = e_zero();
+    v.acc.assign(acc_size(), e_zero());
+    for (int e = 0; e < n_polys; e++) {
+      int id = lay[e].poly, kp = pk[id];
+      E4 sel[32];
+      for (int b = 0; b < lay[e].nbits; b++) sel[b] = lay[e].bits[b] ? e_one() : e_zero();
+      E4 weight = eval_eq_xy(sel, v.point.data() + kp, lay[e].nbits);
+      SvoClaim c;
+      svo_claim(c, poly_dev(id), kp, v.point.data());
+      v.eval = e_add(v.eval, e_mul(weight, c.eval));
+      accumulate(v.acc, c, weight);
+    }
+    ts.write_ext(v.eval);
+    virt.push_back(std::move(v));
+  }
+
+  // ---- sumcheck arrays on the device ----
+  E4 *P() { return sp[ping].as<E4>(); }
+  E4 *W() { return sw[ping].as<E4>(); }
+
+  void read_c0c2(E4 *c0, E4 *c2) {
+    unsigned long long *h = (unsigned long long *)ctx->pinned(64);
+    cuda_check(cudaMemcpyAsync(h, acc.as<unsigned long long>(), 64, cudaMemcpyDeviceToHost, st()),
+               "d2h");
+    ctx->sync();
+    *c0 = reduce_acc(h);
+    *c2 = reduce_acc(h + 4);
+  }
+  // (c0, c2) of the current arrays, applying a pending fold in the same pass
+  void coeffs(E4 *c0, E4 *c2) {
+    unsigned long long *a = acc.as<unsigned long long>();
+    cuda_check(cudaMemsetAsync(a, 0, 64, st()), "memset");
+    size_t n = (size_t)1 << kc;
+    ctx->prof_begin(Context::K_SUMCHECK);
+    if (pending) {
+      cuda_check(gpu::sumcheck_round(P(), W(), 2 * n, true, pending_r, sp[1 - ping].as<E4>(),
+                                     sw[1 - ping].as<E4>(), true, a, st()),
+                 "round");
+      ping = 1 - ping;
+      pending = false;
+      ctx->prof_end(Context::K_SUMCHECK, 3.0 * 2 * 16 * (double)n);
+    } else {
+      cuda_check(gpu::sumcheck_round(P(), W(), n, false, e_zero(), nullptr, nullptr, true, a, st()),
+                 "round");
+      ctx->prof_end(Context::K_SUMCHECK, 2 * 16 * (double)n);
+    }
+    read_c0c2(c0, c2);
+  }
+  void flush() {
+    if (!pending) return;
+    size_t n = (size_t)1 << kc;
+    cuda_check(gpu::sumcheck_round(P(), W(), 2 * n, true, pending_r, sp[1 - ping].as<E4>(),
+                                   sw[1 - ping].as<E4>(), false, nullptr, st()),
+               "fold");
+    ping = 1 - ping;
+    pending = false;
+  }
+  void defer_fold(const E4 &r) {  // Expression::fix_var (expr.rs:101-104)
+    pending = true;
+    pending_r = r;
+    kc -= 1;
+  }
+  // Expression::round (expr.rs:52-70)
+  E4 round(Transcript &ts) {
+    E4 c0, c2;
+    coeffs(&c0, &c2);
+    ts.write_ext(c0);
+    ts.write_ext(c2);
+    E4 r = ts.draw_ext();
+    defer_fold(r);
+    sum = extrapolate012(c0, e_sub(sum, c0), c2, r);
+    return r;
+  }
+
+  // w[off .. off + 2^kt) += eq(point) * scale for several points sharing the range
+  void add_eqs(E4 *w, int kt, const std::vector<std::vector<E4>> &pts, const std::vector<E4> &scales) {
+    if (pts.empty()) return;
+    int s = kt / 2;
+    size_t per = ((size_t)1 << s) + ((size_t)1 << (kt - s));
+    if (per * pts.size() * sizeof(E4) > eqbuf.bytes())
+      eqbuf.reserve(per * pts.size() * sizeof(E4));
+    E4 *tab = eqbuf.as<E4>();
+    for (size_t t = 0; t < pts.size(); t++) {
+      gpu::Point z;
+      z.k = kt;
+      for (int i = 0; i < kt; i++) z.z[i] = pts[t][i];
+      cuda_check(gpu::eq_split(z, s, scales[t], tab + t * per, tab + t * per + ((size_t)1 << s), st()),
+                 "eq_split");
+    }
+    cuda_check(gpu::add_eq(w, kt, tab, (int)pts.size(), st()), "add_eq");
+  }
+
+  void add_pows(const std::vector<uint32_t> &vars, const std::vector<E4> &scales) {
+    if (vars.empty()) return;
+    size_t bytes = vars.size() * 4 + scales.size() * 16;
+    uint8_t *h = (uint8_t *)ctx->pinned(bytes + 64);
+    memcpy(h, scales.data(), scales.size() * 16);
+    memcpy(h + scales.size() * 16, vars.data(), vars.size() * 4);
+    if (bytes > small.bytes()) small.reserve(bytes);
+    cuda_check(cudaMemcpyAsync(small.as<uint8_t>(), h, bytes, cudaMemcpyHostToDevice, st()), "h2d");
+    cuda_check(gpu::add_pows(W(), kc, (const uint32_t *)(small.as<uint8_t>() + scales.size() * 16),
+                             small.as<E4>(), (int)vars.size(), st()),
+               "add_pows");
+    ctx->sync();  // the staging area is reused right after
+  }
+
+  // ---- new_prover (prover.rs:280-354) incl. expression (185-229) ----
+  void new_prover(Transcript &ts) {
+    alpha = ts.draw_ext();
+    auto order = claims_layout_order();
+    int n = (int)claims.size();
+    std::vector<E4> alphas(n), evals;
+    E4 a = e_one();
+    for (auto &oe : order) {
+      alphas[oe.first] = a;
+      evals.push_back(claims[oe.first].eval);
+      a = e_mul(a, alpha);
+    }
+    for (auto &v : virt) evals.push_back(v.eval);
+    sum = horner(evals.data(), evals.size(), alpha);
+    std::vector<E4> accv(acc_size(), e_zero());
+    for (int c = 0; c < n; c++) accumulate(accv, claims[c], alphas[c]);
+    E4 av = e_pow(alpha, (uint64_t)n);
+    for (auto &v : virt) {
+      for (size_t i = 0; i < accv.size(); i++) accv[i] = e_add(accv[i], e_mul(av, v.acc[i]));
+      av = e_mul(av, alpha);
+    }
+    rs.clear();
+    size_t off = 0;
+    for (int r = 0; r < ks; r++) {
+      size_t nw = ipow3(r);
+      std::vector<E4> wts(1, e_one());
+      for (int i = 0; i < r; i++) {  // lagrange_weights_012_multi (svo.rs:7-16)
+        E4 l3[3];
+        lagrange012(rs[i], l3);
+        std::vector<E4> nx(wts.size() * 3);
+        for (int d = 0; d < 3; d++)
+          for (size_t t = 0; t < wts.size(); t++) nx[d * wts.size() + t] = e_mul(wts[t], l3[d]);
+        wts.swap(nx);
+      }
+      E4 c0 = e_zero(), c2 = e_zero();
+      for (size_t t = 0; t < nw; t++) {
+        c0 = e_add(c0, e_mul(accv[off + t], wts[t]));
+        c2 = e_add(c2, e_mul(accv[off + nw + t], wts[t]));
+      }
+      off += 2 * nw;
+      ts.write_ext(c0);
+      ts.write_ext(c2);
+      E4 r_ = ts.draw_ext();
+      sum = extrapolate012(c0, e_sub(sum, c0), c2, r_);
+      rs.push_back(r_);
+    }
+    // expression: compress_stacked (compress_lo_into per poly) + combine_eqs
+    kc = p.k - ks;
+    ping = 0;
+    pending = false;
+    size_t N = (size_t)1 << kc;
+    gpu::Point rsp;
+    rsp.k = ks;
+    for (int i = 0; i < ks; i++) rsp.z[i] = rs[i];
+    if (n_polys > 1) cuda_check(cudaMemsetAsync(P(), 0, N * sizeof(E4), st()), "memset");
+    for (int e = 0; e < n_polys; e++) {
+      int id = lay[e].poly;
+      size_t o = lay[e].index << (pk[id] - ks);
+      cuda_check(gpu::compress_lo(poly_dev(id), pk[id], rsp, P() + o, st()), "compress_lo");
+    }
+    cuda_check(cudaMemsetAsync(W(), 0, N * sizeof(E4), st()), "memset");
+    // group the eq additions by target range
+    std::map<std::pair<size_t, int>, std::pair<std::vector<std::vector<E4>>, std::vector<E4>>> groups;
+    a = e_one();
+    for (auto &oe : order) {
+      const SvoClaim &c = claims[oe.first];
+      int ksplit = c.k - ks;
+      size_t o = lay[oe.second].index << ksplit;
+      E4 scale = e_mul(a, eval_eq_xy(c.point.data(), rs.data(), ks));
+      auto &g = groups[{o, ksplit}];
+      g.first.emplace_back(c.point.begin() + ks, c.point.end());
+      g.second.push_back(scale);
+      a = e_mul(a, alpha);
+    }
+    for (auto &v : virt) {
+      E4 scale = e_mul(a, eval_eq_xy(v.point.data(), rs.data(), ks));
+      auto &g = groups[{0, kc}];
+      g.first.emplace_back(v.point.begin() + ks, v.point.end());
+      g.second.push_back(scale);
+      a = e_mul(a, alpha);
+    }
+    for (auto &kv : groups) add_eqs(W() + kv.first.first, kv.first.second, kv.second.first, kv.second.second);
+  }
+
+  // ---- queries (MerkleTree::query, poseidon_packed.rs:145-233) ----
+  // writes leaf + sibling hints for each index; returns the gathered leaves
+  std::vector<uint32_t> query(Transcript &ts, const DeviceTree &t, const std::vector<size_t> &idx) {
+    int n = (int)idx.size();
+    std::vector<uint32_t> rows;
+    if (n == 0) return rows;
+    size_t per = (size_t)t.row_len + 8 * (size_t)t.log_h;
+    uint32_t *hidx = (uint32_t *)ctx->pinned(4 * n + 4 * per * n);
+    for (int i = 0; i < n; i++) hidx[i] = (uint32_t)idx[i];
+    size_t need = 4 * (size_t)n + 4 * per * n;
+    if (need > gather.bytes()) gather.reserve(need);
+    uint32_t *didx = gather.as<uint32_t>(), *dout = didx + n;
+    cuda_check(cudaMemcpyAsync(didx, hidx, 4 * n, cudaMemcpyHostToDevice, st()), "h2d");
+    cuda_check(gpu::gather_openings(t.rows, t.row_len, t.nodes, t.log_h, didx, n, dout, st()),
+               "gather");
+    uint32_t *hout = hidx + n;
+    cuda_check(cudaMemcpyAsync(hout, dout, 4 * per * n, cudaMemcpyDeviceToHost, st()), "d2h");
+    ctx->sync();
+    rows.resize((size_t)t.row_len * n);
+    for (int i = 0; i < n; i++) {
+      const uint32_t *q = hout + per * i;
+      ts.hint_words(q, per);
+      memcpy(rows.data() + (size_t)t.row_len * i, q, 4 * (size_t)t.row_len);
+    }
+    return rows;
+  }
+
+  std::vector<size_t> stir_indexes(Transcript &ts, int bits, int n) {  // whir.rs:64-77
+    std::vector<size_t> v(n);
+    for (int i = 0; i < n; i++) v[i] = ts.draw_bits(bits);
+    std::sort(v.begin(), v.end());
+    v.erase(std::unique(v.begin(), v.end()), v.end());
+    return v;
+  }
+
+  // ---- fold (prover.rs:378-397) ----
+  std::vector<E4> fold(Transcript &ts, const std::vector<std::vector<E4>> &eq_pts,
+                       const std::vector<E4> &eq_evals, const std::vector<uint32_t> &vars,
+                       const std::vector<E4> &pow_evals) {
+    alpha = ts.draw_ext();
+    std::vector<E4> ev(eq_evals);
+    ev.insert(ev.end(), pow_evals.begin(), pow_evals.end());
+    sum = e_add(sum, horner(ev.data(), ev.size(), alpha));
+    flush();
+    std::vector<E4> sc;
+    E4 a = e_one();
+    for (size_t i = 0; i < eq_pts.size(); i++) {
+      sc.push_back(a);
+      a = e_mul(a, alpha);
+    }
+    add_eqs(W(), kc, eq_pts, sc);
+    std::vector<E4> ps;
+    for (size_t i = 0; i < vars.size(); i++) {
+      ps.push_back(a);
+      a = e_mul(a, alpha);
+    }
+    add_pows(vars, ps);
+    std::vector<E4> out;
+    for (int i = 0; i < p.folding; i++) {
+      E4 r = round(ts);
+      out.push_back(r);
+      rs.push_back(r);
+    }
+    return out;
+  }
+
+  // ---- fold_with_code (prover.rs:400-561) ----
+  std::vector<E4> fold_with_code(Transcript &ts, const std::vector<std::vector<E4>> &eq_pts,
+                                 const std::vector<E4> &eq_evals, const std::vector<size_t> &idx) {
+    int d = p.folding;
+    alpha = ts.draw_ext();
+    int k_data = t0.log_h;
+    sum = e_add(sum, horner(eq_evals.data(), eq_evals.size(), alpha));
+    flush();
+    std::vector<E4> sc;
+    E4 a = e_one();
+    for (size_t i = 0; i < eq_pts.size(); i++) {
+      sc.push_back(a);
+      a = e_mul(a, alpha);
+    }
+    add_eqs(W(), kc, eq_pts, sc);
+    int n = (int)idx.size();
+    std::vector<E4> scales(n);
+    for (int i = 0; i < n; i++) {
+      scales[i] = a;
+      a = e_mul(a, alpha);
+    }
+    // recursive indexes (prover.rs:483-495) and their row evals at eq(rs)
+    std::vector<size_t> ri;
+    for (int round = 0; round < d; round++) {
+      size_t stride = (size_t)1 << (k_data - round - 1), count = (size_t)1 << (round + 1);
+      for (int i = 0; i < n; i++) {
+        size_t base = idx[i] & (stride - 1);
+        for (size_t t = 0; t < count; t++) ri.push_back(base + t * stride);
+      }
+    }
+    std::sort(ri.begin(), ri.end());
+    ri.erase(std::unique(ri.begin(), ri.end()), ri.end());
+    std::unordered_map<size_t, E4> evals;
+    if (!ri.empty()) {
+      size_t m = ri.size();
+      uint32_t *h = (uint32_t *)ctx->pinned(4 * m + 16 * m);
+      for (size_t i = 0; i < m; i++) h[i] = (uint32_t)ri[i];
+      size_t need = 4 * m + 16 * m;
+      if (need > gather.bytes()) gather.reserve(need);
+      uint32_t *didx = gather.as<uint32_t>();
+      E4 *dout = reinterpret_cast<E4 *>(didx + ((m + 3) & ~(size_t)3));
+      cuda_check(cudaMemcpyAsync(didx, h, 4 * m, cudaMemcpyHostToDevice, st()), "h2d");
+      gpu::Point rsp;
+      rsp.k = (int)rs.size();
+      for (size_t i = 0; i < rs.size(); i++) rsp.z[i] = rs[i];
+      cuda_check(gpu::row_evals(t0.rows, t0.row_len, didx, (int)m, rsp, dout, st()), "row_evals");
+      E4 *hout = reinterpret_cast<E4 *>(h + ((m + 3) & ~(size_t)3));
+      cuda_check(cudaMemcpyAsync(hout, dout, 16 * m, cudaMemcpyDeviceToHost, st()), "d2h");
+      ctx->sync();
+      evals.reserve(m * 2);
+      for (size_t i = 0; i < m; i++) evals[ri[i]] = hout[i];
+    }
+    for (int i = 0; i < n; i++) sum = e_add(sum, e_mul(scales[i], evals.at(idx[i])));
+    uint32_t omega = two_adic_generator(k_data);
+    size_t mid0 = ((size_t)1 << k_data) / 2;
+    std::vector<uint32_t> ws(n), tw(n);
+    for (int i = 0; i < n; i++) {
+      ws[i] = kb::pow(omega, idx[i]);
+      tw[i] = inv(kb::pow(omega, idx[i] & (mid0 - 1)));
+    }
+    uint32_t two_inv = inv(from_canonical(2));
+    std::vector<E4> rc;  // rs of this call
+    // g (prover.rs:437-461), memoised per (round, index)
+    std::unordered_map<uint64_t, E4> memo;
+    std::vector<uint32_t> omega_inv(d + 1);
+    for (int r = 1; r <= d; r++) omega_inv[r] = inv(two_adic_generator(k_data - (r - 1)));
+    std::function<E4(int, size_t)> g = [&](int round, size_t index) -> E4 {
+      if (round == 0) return evals.at(index);
+      uint64_t key = ((uint64_t)round << 48) | index;
+      auto it = memo.find(key);
+      if (it != memo.end()) return it->second;
+      size_t l = (size_t)1 << (k_data - (round - 1)), mid = l / 2;
+      size_t i_lo = index & (mid - 1), i_hi = i_lo + mid;
+      E4 glo = g(round - 1, i_lo), ghi = g(round - 1, i_hi);
+      E4 even = e_scale(e_add(glo, ghi), two_inv);
+      E4 odd = e_scale(e_scale(e_sub(glo, ghi), two_inv), kb::pow(omega_inv[round], i_lo));
+      E4 v = e_add(even, e_mul(rc[round - 1], e_sub(odd, even)));
+      memo[key] = v;
+      return v;
+    };
+    for (int round = 0; round < d; round++) {
+      E4 c0, c2;
+      coeffs(&c0, &c2);
+      size_t l = (size_t)1 << (k_data - round), mid = l / 2;
+      for (int i = 0; i < n; i++) {
+        size_t i_lo = idx[i] & (mid - 1), i_hi = i_lo + mid;
+        E4 glo = g(round, i_lo), ghi = g(round, i_hi);
+        E4 even = e_scale(e_add(glo, ghi), two_inv);
+        E4 odd = e_scale(e_scale(e_sub(glo, ghi), two_inv), tw[i]);
+        c0 = e_add(c0, e_mul(scales[i], even));
+        uint32_t wt = sub(dbl(ws[i]), ONE);
+        c2 = e_add(c2, e_scale(e_mul(scales[i], e_sub(e_dbl(odd), even)), wt));
+      }
+      ts.write_ext(c0);
+      ts.write_ext(c2);
+      E4 r = ts.draw_ext();
+      sum = extrapolate012(c0, e_sub(sum, c0), c2, r);
+      rc.push_back(r);
+      defer_fold(r);
+      for (int i = 0; i < n; i++) {
+        E4 f = e_add(e_one(), e_mul(r, e_add(e_neg(e_one()), e_from(ws[i]))));
+        scales[i] = e_mul(scales[i], f);
+        ws[i] = mul(ws[i], ws[i]);
+        tw[i] = mul(tw[i], tw[i]);
+        if ((idx[i] >> (k_data - round - 2)) & 1) tw[i] = neg(tw[i]);
+      }
+    }
+    flush();
+    add_pows(ws, scales);  // combine_pows_scaled (combine.rs:441-468)
+    for (auto &r : rc) rs.push_back(r);
+    return rc;
+  }
+
+  // ---- Whir::open (whir.rs:168-359) ----
+  void open(Transcript &ts) {
+    int n_ood = n_ood_queries(p.soundness, p.security_level, p.k, p.rate, EXT_BITS);
+    for (int i = 0; i < n_ood; i++) write_virtual_eval(ts);
+    new_prover(ts);
+    int n_rounds, final_rounds;
+    number_of_rounds(p.folding, p.k, &n_rounds, &final_rounds);
+    cur_tree = -1;
+    std::vector<E4> round_point;
+    for (int round = 0; round < n_rounds; round++) {
+      int kfd, this_rate, prev_rate;
+      round_params(round, &kfd, &this_rate, &prev_rate);
+      flush();
+      int slot = cur_tree < 0 ? 0 : 1 - cur_tree;
+      encode_commit(*ctx, reinterpret_cast<const uint32_t *>(P()), kc, this_rate, p.folding, 4,
+                    cw[slot].as<uint32_t>(), scratch.as<uint32_t>(), trees[slot].as<uint32_t>(),
+                    &tr[slot]);
+      ts.write_digest(tr[slot].root);
+      int n_o = n_ood_queries(p.soundness, p.security_level, kc, this_rate, EXT_BITS);
+      std::vector<std::vector<E4>> pts;
+      std::vector<E4> evs;
+      for (int i = 0; i < n_o; i++) {
+        std::vector<E4> pt(kc);
+        expand(pt.data(), kc, ts.draw_ext());
+        E4 e = eval_poly(pt);
+        ts.write_ext(e);
+        pts.push_back(std::move(pt));
+        evs.push_back(e);
+      }
+      int n_s = n_stir_queries(p.soundness, p.security_level, prev_rate);
+      std::vector<size_t> idx = stir_indexes(ts, kfd, n_s);
+      std::vector<E4> rnew;
+      if (round == 0) {
+        query(ts, t0, idx);
+        rnew = fold_with_code(ts, pts, evs, idx);
+      } else {
+        const DeviceTree &prev = tr[cur_tree];
+        std::vector<uint32_t> rows = query(ts, prev, idx);
+        uint32_t omega = two_adic_generator(kfd);
+        std::vector<uint32_t> vars(idx.size());
+        std::vector<E4> pev(idx.size());
+        for (size_t i = 0; i < idx.size(); i++) {
+          vars[i] = kb::pow(omega, idx[i]);
+          pev[i] = eval_ext_small(reinterpret_cast<const E4 *>(rows.data() + prev.row_len * i),
+                                  p.folding, round_point.data());
+        }
+        rnew = fold(ts, pts, evs, vars, pev);
+      }
+      round_point = rnew;
+      cur_tree = slot;
+    }
+    flush();
+    size_t nf = (size_t)1 << kc;
+    E4 *hf = (E4 *)ctx->pinned(16 * nf);
+    cuda_check(cudaMemcpyAsync(hf, P(), 16 * nf, cudaMemcpyDeviceToHost, st()), "d2h");
+    ctx->sync();
+    std::vector<E4> fp(hf, hf + nf);
+    for (auto &e : fp) ts.write_ext(e);
+    int kfd, this_rate, prev_rate;
+    round_params(n_rounds, &kfd, &this_rate, &prev_rate);
+    int n_s = n_stir_queries(p.soundness, p.security_level, prev_rate);
+    std::vector<size_t> idx = stir_indexes(ts, kfd, n_s);
+    query(ts, cur_tree >= 0 ? tr[cur_tree] : t0, idx);
+    if (kc != final_rounds) throw WhirError(-1, "final sumcheck size mismatch");
+  }
+
+  // Poly::eval_ext on the current expression poly (SplitEq::eval_ext)
+  E4 eval_poly(const std::vector<E4> &pt) {
+    int k = kc;
+    if (k == 0) {
+      E4 *h = (E4 *)ctx->pinned(16);
+      cuda_check(cudaMemcpyAsync(h, P(), 16, cudaMemcpyDeviceToHost, st()), "d2h");
+      ctx->sync();
+      return *h;
+    }
+    int s_lo = std::min(10, k);
+    gpu::Point z;
+    z.k = k;
+    for (int i = 0; i < k; i++) z.z[i] = pt[i];
+    E4 *lo = eqbuf.as<E4>(), *hi = lo + ((size_t)1 << s_lo);
+    cuda_check(gpu::eq_split(z, s_lo, e_one(), lo, hi, st()), "eq_split");
+    unsigned long long *a = acc.as<unsigned long long>();
+    cuda_check(cudaMemsetAsync(a, 0, 32, st()), "memset");
+    cuda_check(gpu::eval_ext(P(), k, lo, s_lo, hi, a, st()), "eval_ext");
+    unsigned long long *h = (unsigned long long *)ctx->pinned(64);
+    cuda_check(cudaMemcpyAsync(h, a, 32, cudaMemcpyDeviceToHost, st()), "d2h");
+    ctx->sync();
+    return reduce_acc(h);
+  }
+};
+
+Prover::Prover(Context *ctx, const Params &p) : m_(new Impl), ctx_(ctx), p_(p) {
+  if (p.folding < 1 || p.folding > 8 || p.k < p.folding || p.k > 26 || p.rate < 0 ||
+      p.rate > 8 || p.initial_reduction < 1 || p.soundness < 0 || p.soundness > 2)
+    throw WhirError(-1, "invalid WHIR parameters");
+  m_->ctx = ctx;
+  m_->p = p;
+  m_->ks = p.folding;
+}
+Prover::~Prover() { delete m_; }
+
+size_t Prover::device_bytes() const {
+  size_t s = 0;
+  const DeviceBuffer *bufs[] = {&m_->stacked, &m_->cw0,   &m_->tree0,  &m_->scratch,
+                                &m_->cw[0],   &m_->cw[1], &m_->trees[0], &m_->trees[1],
+                                &m_->sp[0],   &m_->sp[1], &m_->sw[0],  &m_->sw[1],
+                                &m_->eqbuf,   &m_->acc,   &m_->small,  &m_->gather};
+  for (auto b : bufs) s += b->bytes();
+  return s;
+}
+
+void Prover::commit(Transcript &ts, const uint32_t *polys, bool on_device,
+                    const std::vector<int> &poly_k) {
+  Impl &m = *m_;
+  m.n_polys = (int)poly_k.size();
+  if (m.n_polys == 0) throw WhirError(-1, "no polynomials");
+  m.pk = poly_k;
+  m.make_layout();
+  m.reserve();
+  m.claims.clear();
+  m.virt.clear();
+  cudaStream_t st = ctx_->stream();
+  size_t total = (size_t)1 << p_.k;
+  uint32_t *stk = m.stacked.as<uint32_t>();
+  if (m.n_polys > 1) cuda_check(cudaMemsetAsync(stk, 0, 4 * total, st), "memset");
+  size_t src_off = 0;
+  for (int id = 0; id < m.n_polys; id++) {
+    size_t n = (size_t)1 << poly_k[id];
+    cuda_check(cudaMemcpyAsync(stk + m.poly_off[id], polys + src_off, 4 * n,
+                               on_device ? cudaMemcpyDeviceToDevice : cudaMemcpyHostToDevice, st),
+               "poly copy");
+    src_off += n;
+  }
+  encode_commit(*ctx_, stk, p_.k, p_.rate, p_.folding, 1, m.cw0.as<uint32_t>(),
+                m.scratch.as<uint32_t>(), m.tree0.as<uint32_t>(), &m.t0);
+  ts.write_digest(m.t0.root);
+}
+
+E4 Prover::eval(Transcript &ts, int id, const E4 *point) {
+  Impl &m = *m_;
+  if (id < 0 || id >= m.n_polys) throw WhirError(-1, "unknown polynomial id");
+  for (int i = 0; i < m.pk[id]; i++)
+    for (int c = 0; c < 4; c++)
+      if (point[i].c[c] >= P) throw WhirError(-1, "non-canonical field element");
+  SvoClaim c;
+  c.poly = id;
+  m.svo_claim(c, m.poly_dev(id), m.pk[id], point);
+  ts.write_ext(c.eval);
+  E4 e = c.eval;
+  m.claims.push_back(std::move(c));
+  return e;
+}
+
+void Prover::open(Transcript &ts) { m_->open(ts); }
+
+void Prover::prove(Transcript &ts, const uint32_t *polys, bool on_device,
+                   const std::vector<int> &poly_k, const std::vector<std::vector<int>> &groups) {
+  commit(ts, polys, on_device, poly_k);
+  for (auto &g : groups) {
+    if (g.empty()) throw WhirError(-1, "empty claim group");
+    int kg = poly_k.at(g[0]);
+    std::vector<E4> pt(kg);
+    expand(pt.data(), kg, ts.draw_ext());
+    for (int id : g) {
+      if (poly_k.at(id) != kg) throw WhirError(-1, "claim group mixes polynomial sizes");
+      eval(ts, id, pt.data());
+    }
+  }
+  open(ts);
+}
+
+}  // namespace whir

@@ -1,0 +1,139 @@
+// GPU WHIR prover: the host orchestration of Whir::commit / ProverStack /
+// Whir::open (crates/whir/src/whir.rs:20-359, crates/whir/src/sumcheck/*.rs)
+// with all polynomial-sized data resident on the device.  Per sumcheck round
+// only (c0, c2) come back to the host and only the challenge goes down (as a
+// kernel argument).
+#pragma once
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include <stdexcept>
+#include <string>
+#include <vector>
+
+#include "kb.cuh"
+#include "kernels.h"
+#include "transcript.h"
+
+namespace whir {
+
+struct Params {
+  int k;
+  int folding;
+  int rate;
+  int initial_reduction;
+  int soundness;  // 0 UniqueDecoding, 1 JohnsonBound, 2 CapacityBound
+  int security_level;
+};
+
+// crates/whir/src/params.rs
+int n_ood_queries(int soundness, int security, int log_degree, int log_inv_rate, int field_bits);
+int n_stir_queries(int soundness, int security, int log_inv_rate);
+void number_of_rounds(int folding, int k, int *n_rounds, int *final_rounds);
+constexpr int EXT_BITS = 124;  // bits of |BinomialExtensionField<KoalaBear, 4>|
+
+uint32_t two_adic_generator(int bits);  // Montgomery form
+
+struct WhirError : std::runtime_error {
+  int code;
+  WhirError(int c, const std::string &m) : std::runtime_error(m), code(c) {}
+};
+void cuda_check(cudaError_t e, const char *what);
+
+// device allocation owned by one object
+class DeviceBuffer {
+ public:
+  DeviceBuffer() = default;
+  ~DeviceBuffer();
+  DeviceBuffer(const DeviceBuffer &) = delete;
+  DeviceBuffer &operator=(const DeviceBuffer &) = delete;
+  void reserve(size_t bytes);
+  template <class T>
+  T *as() const { return reinterpret_cast<T *>(ptr_); }
+  size_t bytes() const { return bytes_; }
+
+ private:
+  void *ptr_ = nullptr;
+  size_t bytes_ = 0;
+};
+
+// One device, one stream, the device tables and a pinned staging area.
+class Context {
+ public:
+  explicit Context(int device);
+  ~Context();
+  int device() const { return device_; }
+  cudaStream_t stream() const { return stream_; }
+  void *pinned(size_t bytes);  // staging for D2H results and H2D arguments
+  void sync();
+  // per-kernel-class CUDA-event timing on this stream
+  enum Klass { K_DFT = 0, K_LEAF = 1, K_TREE = 2, K_SUMCHECK = 3, K_NCLASS = 4 };
+  void prof_enable(bool on);
+  void prof_begin(int klass);
+  void prof_end(int klass, double bytes);
+  // drains recorded events: total ms, launches and bytes per class
+  void prof_read(int klass, double *ms, long *launches, double *bytes);
+
+ private:
+  int device_;
+  cudaStream_t stream_ = nullptr;
+  void *pinned_ = nullptr;
+  size_t pinned_bytes_ = 0;
+  bool prof_ = false;
+  struct Ev {
+    cudaEvent_t a, b;
+    int klass;
+    double bytes;
+  };
+  std::vector<Ev> evs_;
+  std::vector<cudaEvent_t> free_events_;
+  double acc_ms_[K_NCLASS] = {0, 0, 0, 0};
+  long acc_n_[K_NCLASS] = {0, 0, 0, 0};
+  double acc_bytes_[K_NCLASS] = {0, 0, 0, 0};
+  int open_klass_ = -1;
+  cudaEvent_t open_ev_ = nullptr;
+  cudaEvent_t take_event();
+};
+
+// Merkle data kept on the device (MerkleData, crates/merkle/src/lib.rs:11-17)
+struct DeviceTree {
+  const uint32_t *rows = nullptr;  // codeword rows (borrowed)
+  uint32_t *nodes = nullptr;       // all levels, leaves first
+  int log_h = 0;
+  int row_len = 0;
+  uint32_t root[8];
+};
+
+// Reed-Solomon encode + Merkle commit of `src` (2^k rows... see commit_rows)
+void encode_commit(Context &ctx, const uint32_t *src, int k, int rate, int folding, int dim,
+                   uint32_t *codeword, uint32_t *scratch, uint32_t *nodes, DeviceTree *out);
+
+class Prover {
+ public:
+  Prover(Context *ctx, const Params &p);
+  ~Prover();
+  const Params &params() const { return p_; }
+  // Whir::commit of the stacked layout of the given polys (ProverStack::layout
+  // order, prover.rs:92-124); a single poly is committed as is.
+  void commit(Transcript &ts, const uint32_t *polys, bool on_device,
+              const std::vector<int> &poly_k);
+  // ProverStack::eval (prover.rs:64-90): claim on poly `id` at `point` (k_id
+  // extension elements); writes and returns the evaluation.
+  kb::E4 eval(Transcript &ts, int id, const kb::E4 *point);
+  // Whir::open (whir.rs:168-359)
+  void open(Transcript &ts);
+  // the whole reference harness (test.rs:218-235) except the final draw:
+  // commit, then each claim group draws one expanded point and evaluates it
+  // on its polys, then open.
+  void prove(Transcript &ts, const uint32_t *polys, bool on_device, const std::vector<int> &poly_k,
+             const std::vector<std::vector<int>> &groups);
+  size_t device_bytes() const;
+
+ private:
+  struct Impl;
+  Impl *m_;
+  Context *ctx_;
+  Params p_;
+};
+
+}  // namespace whir

@@ -1,0 +1,322 @@
+// eq tables, SVO compression, expression build, constraint combination and
+// sumcheck round kernels (crates/poly/src/{point,eq,poly}.rs,
+// crates/whir/src/sumcheck/{svo,expr,combine,prover}.rs).
+//
+// Reductions are exact: every thread sums canonical words mod p, then CTA
+// partials are added as plain integers into 64-bit accumulators with
+// atomicAdd (the sum of canonical words stays far below 2^64), and the host
+// reduces the accumulator mod p.  Any summation order therefore gives the
+// same field element, which is why the results match the CPU restatement
+// bit for bit.
+#include "kernels.h"
+
+namespace whir {
+namespace gpu {
+
+using kb::E4;
+
+__device__ __forceinline__ void acc_add(unsigned long long *a, const E4 &v) {
+#pragma unroll
+  for (int c = 0; c < 4; c++) atomicAdd(a + c, (unsigned long long)v.c[c]);
+}
+
+// eq table entries over z[off .. off+nv) times scale: entry b selects z_i
+// when bit i of b is set, 1 - z_i otherwise (Point::eq, point.rs:159-175).
+__global__ void eq_entries(Point z, int off, int nv, E4 scale, E4 *out) {
+  size_t b = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (b >= ((size_t)1 << nv)) return;
+  E4 acc = scale;
+  for (int i = 0; i < nv; i++) {
+    E4 zi = z.z[off + i];
+    acc = kb::e_mul(acc, ((b >> i) & 1) ? zi : kb::e_sub(kb::e_one(), zi));
+  }
+  out[b] = acc;
+}
+
+static cudaError_t eq_part(const Point &z, int off, int nv, E4 scale, E4 *out, cudaStream_t st) {
+  size_t n = (size_t)1 << nv;
+  unsigned T = 256, G = (unsigned)((n + T - 1) / T);
+  eq_entries<<<G, T, 0, st>>>(z, off, nv, scale, out);
+  return cudaGetLastError();
+}
+
+cudaError_t eq_split(const Point &z, int s, E4 scale, E4 *lo, E4 *hi, cudaStream_t st) {
+  if (s < 0 || s > z.k) return cudaErrorInvalidValue;
+  cudaError_t e = eq_part(z, 0, s, kb::e_one(), lo, st);
+  if (e != cudaSuccess) return e;
+  return eq_part(z, s, z.k - s, scale, hi, st);
+}
+
+__global__ void eq_join(const E4 *lo, const E4 *hi, int s, size_t n, E4 *out) {
+  size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  out[i] = kb::e_mul(lo[i & (((size_t)1 << s) - 1)], hi[i >> s]);
+}
+
+cudaError_t eq_full(const Point &z, E4 scale, E4 *out, E4 *tmp, cudaStream_t st) {
+  int s = z.k / 2;
+  E4 *lo = tmp, *hi = tmp + ((size_t)1 << s);
+  cudaError_t e = eq_split(z, s, scale, lo, hi, st);
+  if (e != cudaSuccess) return e;
+  size_t n = (size_t)1 << z.k;
+  eq_join<<<(unsigned)((n + 255) / 256), 256, 0, st>>>(lo, hi, s, n, out);
+  return cudaGetLastError();
+}
+
+// compress_hi: rows of W = 2^ks words; row h = h_lo + 2^s_lo * h_hi.  A CTA
+// walks whole h_hi blocks (2^s_lo contiguous rows); thread t always sees
+// column j = t mod W, so it keeps one inner sum (over h_lo, weighted by
+// eq_lo) and folds it into its outer sum with eq_hi[h_hi] once per block.
+constexpr int CH_T = 256;
+__global__ void __launch_bounds__(CH_T) compress_hi_kernel(const uint32_t *__restrict__ poly,
+                                                           int k, int ks,
+                                                           const E4 *__restrict__ eq_lo, int s_lo,
+                                                           const E4 *__restrict__ eq_hi,
+                                                           unsigned long long *acc) {
+  extern __shared__ unsigned char smraw[];
+  E4 *lo = reinterpret_cast<E4 *>(smraw);
+  unsigned long long *part = reinterpret_cast<unsigned long long *>(lo + ((size_t)1 << s_lo));
+  const int W = 1 << ks;
+  const int tid = threadIdx.x;
+  for (int i = tid; i < (1 << s_lo); i += CH_T) lo[i] = eq_lo[i];
+  for (int i = tid; i < W * 4; i += CH_T) part[i] = 0;
+  __syncthreads();
+  const size_t block_words = (size_t)W << s_lo;
+  const size_t n_hi = (size_t)1 << (k - ks - s_lo);
+  E4 outer = kb::e_zero();
+  for (size_t hh = blockIdx.x; hh < n_hi; hh += gridDim.x) {
+    const uint32_t *base = poly + hh * block_words;
+    E4 inner = kb::e_zero();
+    for (size_t e = tid; e < block_words; e += CH_T)
+      inner = kb::e_add(inner, kb::e_scale(lo[e >> ks], __ldg(base + e)));
+    outer = kb::e_add(outer, kb::e_mul(inner, eq_hi[hh]));
+  }
+  {
+    const int j = tid & (W - 1);
+#pragma unroll
+    for (int c = 0; c < 4; c++) atomicAdd(part + j * 4 + c, (unsigned long long)outer.c[c]);
+  }
+  __syncthreads();
+  for (int i = tid; i < W * 4; i += CH_T) atomicAdd(acc + i, part[i]);
+}
+
+cudaError_t compress_hi(const uint32_t *poly, int k, int ks, const E4 *eq_lo, int s_lo,
+                        const E4 *eq_hi, unsigned long long *acc, cudaStream_t st) {
+  if ((1 << ks) > CH_T || k < ks + s_lo) return cudaErrorInvalidValue;
+  size_t n_hi = (size_t)1 << (k - ks - s_lo);
+  unsigned grid = (unsigned)(n_hi < 152 * 8 ? n_hi : 152 * 8);
+  size_t smem = ((size_t)1 << s_lo) * sizeof(E4) + ((size_t)4 << ks) * 8;
+  compress_hi_kernel<<<grid, CH_T, smem, st>>>(poly, k, ks, eq_lo, s_lo, eq_hi, acc);
+  return cudaGetLastError();
+}
+
+// compress_lo: out[i] = sum_j eq(rs)[j] * P[i * 2^ks + j]
+__global__ void compress_lo_kernel(const uint32_t *__restrict__ poly, int ks, size_t n_out,
+                                   Point rs, E4 *__restrict__ out) {
+  __shared__ E4 eq[256];
+  const int W = 1 << ks;
+  for (int b = threadIdx.x; b < W; b += blockDim.x) {
+    E4 acc = kb::e_one();
+    for (int i = 0; i < ks; i++)
+      acc = kb::e_mul(acc, ((b >> i) & 1) ? rs.z[i] : kb::e_sub(kb::e_one(), rs.z[i]));
+    eq[b] = acc;
+  }
+  __syncthreads();
+  for (size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x; i < n_out;
+       i += (size_t)gridDim.x * blockDim.x) {
+    const uint32_t *row = poly + i * W;
+    E4 acc = kb::e_zero();
+    for (int j = 0; j < W; j++) acc = kb::e_add(acc, kb::e_scale(eq[j], __ldg(row + j)));
+    out[i] = acc;
+  }
+}
+
+cudaError_t compress_lo(const uint32_t *poly, int k, const Point &rs, E4 *out, cudaStream_t st) {
+  int ks = rs.k;
+  if (ks > 8 || ks > k) return cudaErrorInvalidValue;
+  size_t n_out = (size_t)1 << (k - ks);
+  unsigned T = 256;
+  size_t g = (n_out + T - 1) / T;
+  unsigned grid = (unsigned)(g < 152 * 16 ? g : 152 * 16);
+  compress_lo_kernel<<<grid, T, 0, st>>>(poly, ks, n_out, rs, out);
+  return cudaGetLastError();
+}
+
+// w[i] += sum_t lo_t[i & mask] * hi_t[i >> s]
+__global__ void add_eq_kernel(E4 *w, size_t n, int s, size_t n_lo, size_t n_hi,
+                              const E4 *__restrict__ tables, int n_tables) {
+  for (size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x; i < n;
+       i += (size_t)gridDim.x * blockDim.x) {
+    E4 acc = w[i];
+    for (int t = 0; t < n_tables; t++) {
+      const E4 *lo = tables + t * (n_lo + n_hi), *hi = lo + n_lo;
+      acc = kb::e_add(acc, kb::e_mul(lo[i & (n_lo - 1)], hi[i >> s]));
+    }
+    w[i] = acc;
+  }
+}
+
+cudaError_t add_eq(E4 *w, int k, const E4 *tables, int n_tables, cudaStream_t st) {
+  if (n_tables == 0) return cudaSuccess;
+  int s = k / 2;
+  size_t n = (size_t)1 << k;
+  unsigned T = 256;
+  size_t g = (n + T - 1) / T;
+  unsigned grid = (unsigned)(g < 152 * 16 ? g : 152 * 16);
+  add_eq_kernel<<<grid, T, 0, st>>>(w, n, s, (size_t)1 << s, (size_t)1 << (k - s), tables,
+                                    n_tables);
+  return cudaGetLastError();
+}
+
+// w[i] += sum_t scale_t * var_t^i; a thread owns 16 consecutive i
+__global__ void add_pows_kernel(E4 *w, size_t n, const uint32_t *__restrict__ vars,
+                                const E4 *__restrict__ scales, int n_vars) {
+  size_t i0 = ((size_t)blockIdx.x * blockDim.x + threadIdx.x) * 16;
+  if (i0 >= n) return;
+  int cnt = n - i0 < 16 ? (int)(n - i0) : 16;
+  E4 acc[16];
+  for (int j = 0; j < cnt; j++) acc[j] = w[i0 + j];
+  for (int t = 0; t < n_vars; t++) {
+    uint32_t v = vars[t];
+    uint32_t p = kb::pow(v, i0);
+    E4 sc = scales[t];
+    for (int j = 0; j < cnt; j++) {
+      acc[j] = kb::e_add(acc[j], kb::e_scale(sc, p));
+      p = kb::mul(p, v);
+    }
+  }
+  for (int j = 0; j < cnt; j++) w[i0 + j] = acc[j];
+}
+
+cudaError_t add_pows(E4 *w, int k, const uint32_t *vars, const E4 *scales, int n, cudaStream_t st) {
+  if (n == 0) return cudaSuccess;
+  size_t N = (size_t)1 << k, threads = (N + 15) / 16;
+  unsigned T = 128;
+  add_pows_kernel<<<(unsigned)((threads + T - 1) / T), T, 0, st>>>(w, N, vars, scales, n);
+  return cudaGetLastError();
+}
+
+// block-wide sum of E4 values into 64-bit accumulators
+template <int NV>
+__device__ __forceinline__ void block_acc(const E4 (&v)[NV], unsigned long long *acc) {
+  __shared__ unsigned long long part[NV * 4];
+  for (int i = threadIdx.x; i < NV * 4; i += blockDim.x) part[i] = 0;
+  __syncthreads();
+  // warp pre-sum mod p, then one shared atomic per warp and word
+#pragma unroll
+  for (int q = 0; q < NV; q++)
+#pragma unroll
+    for (int c = 0; c < 4; c++) {
+      uint32_t x = v[q].c[c];
+#pragma unroll
+      for (int off = 16; off; off >>= 1) x = kb::add(x, __shfl_down_sync(0xffffffffu, x, off));
+      if ((threadIdx.x & 31) == 0) atomicAdd(part + q * 4 + c, (unsigned long long)x);
+    }
+  __syncthreads();
+  for (int i = threadIdx.x; i < NV * 4; i += blockDim.x) atomicAdd(acc + i, part[i]);
+}
+
+// One round: new[i] = a[2i] + r (a[2i+1] - a[2i]) for poly and weights (when
+// folding), then c0 += w[2m] p[2m], c2 += (2 w[2m+1] - w[2m]) (2 p[2m+1] - p[2m]).
+__global__ void __launch_bounds__(256) round_kernel(const E4 *__restrict__ p_in,
+                                                    const E4 *__restrict__ w_in, size_t n_in,
+                                                    int fold, E4 r, E4 *__restrict__ p_out,
+                                                    E4 *__restrict__ w_out, int coeffs,
+                                                    unsigned long long *acc) {
+  size_t n = fold ? n_in / 2 : n_in;
+  size_t pairs = (n + 1) / 2;
+  E4 sums[2] = {kb::e_zero(), kb::e_zero()};
+  for (size_t m = (size_t)blockIdx.x * blockDim.x + threadIdx.x; m < pairs;
+       m += (size_t)gridDim.x * blockDim.x) {
+    E4 p0, p1 = kb::e_zero(), w0, w1 = kb::e_zero();
+    if (fold) {
+      const E4 *pp = p_in + 4 * m, *ww = w_in + 4 * m;
+      p0 = kb::e_add(pp[0], kb::e_mul(r, kb::e_sub(pp[1], pp[0])));
+      w0 = kb::e_add(ww[0], kb::e_mul(r, kb::e_sub(ww[1], ww[0])));
+      p_out[2 * m] = p0;
+      w_out[2 * m] = w0;
+      if (2 * m + 1 < n) {
+        p1 = kb::e_add(pp[2], kb::e_mul(r, kb::e_sub(pp[3], pp[2])));
+        w1 = kb::e_add(ww[2], kb::e_mul(r, kb::e_sub(ww[3], ww[2])));
+        p_out[2 * m + 1] = p1;
+        w_out[2 * m + 1] = w1;
+      }
+    } else {
+      p0 = p_in[2 * m]; w0 = w_in[2 * m];
+      if (2 * m + 1 < n) { p1 = p_in[2 * m + 1]; w1 = w_in[2 * m + 1]; }
+    }
+    if (coeffs && 2 * m + 1 < n) {
+      sums[0] = kb::e_add(sums[0], kb::e_mul(w0, p0));
+      E4 dw = kb::e_sub(kb::e_dbl(w1), w0), dp = kb::e_sub(kb::e_dbl(p1), p0);
+      sums[1] = kb::e_add(sums[1], kb::e_mul(dw, dp));
+    }
+  }
+  if (coeffs) block_acc<2>(sums, acc);
+}
+
+cudaError_t sumcheck_round(const E4 *p_in, const E4 *w_in, size_t n_in, bool fold, E4 r,
+                           E4 *p_out, E4 *w_out, bool coeffs, unsigned long long *acc,
+                           cudaStream_t st) {
+  size_t n = fold ? n_in / 2 : n_in;
+  size_t pairs = (n + 1) / 2;
+  unsigned T = 256;
+  size_t g = (pairs + T - 1) / T;
+  unsigned grid = (unsigned)(g < 152 * 8 ? (g ? g : 1) : 152 * 8);
+  round_kernel<<<grid, T, 0, st>>>(p_in, w_in, n_in, fold ? 1 : 0, r, p_out, w_out,
+                                   coeffs ? 1 : 0, acc);
+  return cudaGetLastError();
+}
+
+// <eq(z), poly>: CTA walks hi blocks of 2^s_lo contiguous entries
+__global__ void __launch_bounds__(256) eval_ext_kernel(const E4 *__restrict__ poly, int k,
+                                                       const E4 *__restrict__ eq_lo, int s_lo,
+                                                       const E4 *__restrict__ eq_hi,
+                                                       unsigned long long *acc) {
+  size_t n_lo = (size_t)1 << s_lo, n_hi = (size_t)1 << (k - s_lo);
+  E4 outer = kb::e_zero();
+  for (size_t hh = blockIdx.x; hh < n_hi; hh += gridDim.x) {
+    E4 inner = kb::e_zero();
+    for (size_t l = threadIdx.x; l < n_lo; l += blockDim.x)
+      inner = kb::e_add(inner, kb::e_mul(eq_lo[l], poly[hh * n_lo + l]));
+    outer = kb::e_add(outer, kb::e_mul(inner, eq_hi[hh]));
+  }
+  E4 v[1] = {outer};
+  block_acc<1>(v, acc);
+}
+
+cudaError_t eval_ext(const E4 *poly, int k, const E4 *eq_lo, int s_lo, const E4 *eq_hi,
+                     unsigned long long *acc, cudaStream_t st) {
+  size_t n_hi = (size_t)1 << (k - s_lo);
+  unsigned grid = (unsigned)(n_hi < 152 * 8 ? n_hi : 152 * 8);
+  eval_ext_kernel<<<grid, 256, 0, st>>>(poly, k, eq_lo, s_lo, eq_hi, acc);
+  return cudaGetLastError();
+}
+
+__global__ void row_evals_kernel(const uint32_t *__restrict__ rows, int row_len,
+                                 const uint32_t *__restrict__ idx, int n, Point rs, E4 *out) {
+  __shared__ E4 eq[256];
+  for (int b = threadIdx.x; b < row_len; b += blockDim.x) {
+    E4 a = kb::e_one();
+    for (int i = 0; i < rs.k; i++)
+      a = kb::e_mul(a, ((b >> i) & 1) ? rs.z[i] : kb::e_sub(kb::e_one(), rs.z[i]));
+    eq[b] = a;
+  }
+  __syncthreads();
+  int q = blockIdx.x * blockDim.x + threadIdx.x;
+  if (q >= n) return;
+  const uint32_t *row = rows + (size_t)idx[q] * row_len;
+  E4 a = kb::e_zero();
+  for (int j = 0; j < row_len; j++) a = kb::e_add(a, kb::e_scale(eq[j], row[j]));
+  out[q] = a;
+}
+
+cudaError_t row_evals(const uint32_t *rows, int row_len, const uint32_t *idx, int n,
+                      const Point &rs, E4 *out, cudaStream_t st) {
+  if (n == 0) return cudaSuccess;
+  if (row_len > 256 || (1 << rs.k) != row_len) return cudaErrorInvalidValue;
+  row_evals_kernel<<<(n + 127) / 128, 128, 0, st>>>(rows, row_len, idx, n, rs, out);
+  return cudaGetLastError();
+}
+
+}  // namespace gpu
+}  // namespace whir

@@ -1,0 +1,64 @@
+// Fiat-Shamir transcript on the host: PoseidonWriter over
+// DuplexChallenger<KoalaBear, Poseidon2KoalaBear<16>, 16, 8>
+// (crates/transcript/src/poseidon.rs:13-87, harness crates/whir/src/test.rs:190-200).
+//
+// Byte format (crates/transcript/src/field.rs:1-25, bincode 1.3): a field
+// element is its 32-bit Montgomery word little-endian; an extension element
+// is its 4 coefficients; a digest its 8 words.  write() appends the bytes and
+// observes the elements; write_hint() only appends.
+#pragma once
+#include <stddef.h>
+#include <stdint.h>
+
+#include <vector>
+
+#include "kb.cuh"
+
+namespace whir {
+
+class Challenger {
+ public:
+  Challenger();
+  void observe(uint32_t v);
+  uint32_t sample();
+  size_t sample_bits(int bits);
+
+ private:
+  void duplexing();
+  uint32_t state_[16];
+  uint32_t in_[8];
+  int n_in_ = 0;
+  uint32_t out_[8];
+  int n_out_ = 0;
+};
+
+class Transcript {
+ public:
+  void write_fe(uint32_t v) { put(v); ch_.observe(v); }
+  void write_ext(const kb::E4 &e) {
+    for (int i = 0; i < 4; i++) write_fe(e.c[i]);
+  }
+  void write_digest(const uint32_t *d) {
+    for (int i = 0; i < 8; i++) write_fe(d[i]);
+  }
+  void hint_fe(uint32_t v) { put(v); }
+  void hint_words(const uint32_t *v, size_t n);
+  kb::E4 draw_ext() {
+    kb::E4 e;
+    for (int i = 0; i < 4; i++) e.c[i] = ch_.sample();
+    return e;
+  }
+  uint32_t draw_fe() { return ch_.sample(); }
+  size_t draw_bits(int bits) { return ch_.sample_bits(bits); }
+  const std::vector<uint8_t> &bytes() const { return bytes_; }
+
+ private:
+  void put(uint32_t v) {
+    uint8_t b[4] = {(uint8_t)v, (uint8_t)(v >> 8), (uint8_t)(v >> 16), (uint8_t)(v >> 24)};
+    bytes_.insert(bytes_.end(), b, b + 4);
+  }
+  std::vector<uint8_t> bytes_;
+  Challenger ch_;
+};
+
+}  // namespace whir
