@@ -1,0 +1,338 @@
+#!/usr/bin/env python3
+"""WHIR commit+open proofs per second on GB300.
+
+A step is one complete WHIR proof of the plain single-instance workload:
+commit + open of a seeded 2^24-evaluation KoalaBear multilinear polynomial,
+rate 1/4 (log_inv_rate 2), folding factor 4, initial_reduction 1,
+JohnsonBound at 100-bit security, 4 evaluation claims drawn from the
+transcript as the reference harness draws them (crates/whir/src/test.rs:174-254).
+
+  value   proofs/s with the polynomial already resident in HBM
+  e2e     proofs/s through the C ABI from a pinned host buffer: the
+          polynomial's host->device copy and every device->host read of the
+          proof (roots, evaluations, openings, round messages) are inside the
+          timed region
+  roofline   the dominant kernel class, timed with CUDA events on the
+          library's stream during the timed region
+  cpu_baseline   the C restatement of the reference prover (oracle/) on the
+          host cores, same workload, bounded sample
+
+`--impl reference` times the reference's algorithm on the host CPU: the
+reference (Rust) cannot be built in this environment, so its C restatement in
+oracle/ runs with all host threads on the same workload.
+
+Multi-GPU: proofs are independent, so N GPUs run N replicas (weak scaling);
+value = proofs of all ranks / max rank time.
+"""
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import tempfile
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+WORKLOAD = dict(k=24, folding=4, rate=2, initial_reduction=1, soundness="JohnsonBound",
+                soundness_id=1, security_level=100, claims=4, seed=1)
+METRIC = "proofs/sec and p50/p99 latency, batched/served vs plain, 1 GB300, bit-exact"
+UNIT = "proofs/s"
+# Per-launch DRAM traffic of the dominant kernel from ncu (None until captured);
+# see profiles/ for the capture and its command.
+NCU_TRAFFIC_BYTES = {}
+
+
+def parse():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=30)
+    ap.add_argument("--warmup", type=int, default=5)
+    ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
+    ap.add_argument("--k", type=int, default=WORKLOAD["k"])
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--cpu-seconds", type=float, default=12.0,
+                    help="time budget of the bounded CPU baseline sample")
+    return ap.parse_args()
+
+
+def dist_env():
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", str(rank)))
+    return world, rank, local
+
+
+def workload_config(k):
+    return {
+        "workload": f"WHIR commit+open, 2^{k} KoalaBear evaluations, rate 1/4, folding 4, "
+                    f"{WORKLOAD['claims']} claims, JohnsonBound 100-bit, initial_reduction 1",
+        "k": k, "log_inv_rate": WORKLOAD["rate"], "folding": WORKLOAD["folding"],
+        "initial_reduction": WORKLOAD["initial_reduction"], "soundness": WORKLOAD["soundness"],
+        "security_level": WORKLOAD["security_level"], "claims": WORKLOAD["claims"],
+        "seed": WORKLOAD["seed"], "field": "KoalaBear + degree-4 extension",
+        "hash": "Poseidon2 (width-24 leaf sponge, width-16 compression)",
+        "l2": "no flush needed: each step touches > 2 GB (codewords + trees) >> 129 MB L2",
+    }
+
+
+class ClockSampler:
+    """nvidia-smi clocks and throttle reasons sampled every 200 ms."""
+
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, device):
+        self.device = device
+        self.proc = None
+        self.f = None
+
+    def start(self):
+        try:
+            self.f = tempfile.NamedTemporaryFile("w+", suffix=".csv", delete=False)
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", "-i", str(self.device), f"--query-gpu={self.FIELDS}",
+                 "--format=csv,noheader,nounits", "-lms", "200"],
+                stdout=self.f, stderr=subprocess.DEVNULL)
+        except Exception:
+            self.proc = None
+
+    def stop(self):
+        if self.proc is None:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except Exception:
+            self.proc.kill()
+        self.f.flush()
+        self.f.seek(0)
+        rows = [r.split(",") for r in self.f.read().strip().splitlines() if r.strip()]
+        os.unlink(self.f.name)
+        sm, mx, reasons = [], None, set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for r in rows:
+            r = [x.strip() for x in r]
+            try:
+                sm.append(float(r[1]))
+                mx = float(r[2])
+            except (ValueError, IndexError):
+                continue
+            for name, val in zip(names, r[5:9]):
+                if val.lower() == "active":
+                    reasons.add(name)
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": mx,
+                "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def cpu_baseline(k, seconds, expect_proof=None):
+    """Oracle (C restatement, OpenMP over all host cores) on the same workload."""
+    from oracle import oracle as O
+    params = (k, WORKLOAD["folding"], WORKLOAD["rate"], WORKLOAD["initial_reduction"],
+              WORKLOAD["soundness_id"], WORKLOAD["security_level"])
+    poly = O.rand_fe(WORKLOAD["seed"], 1 << k)
+    groups = [[0]] * WORKLOAD["claims"]
+    n, t0 = 0, time.perf_counter()
+    proof = None
+    while True:
+        proof, _ = O.prove(params, [poly], [k], groups)
+        n += 1
+        el = time.perf_counter() - t0
+        if el >= seconds or el * (n + 1) / n > 30.0:
+            break
+    same = None if expect_proof is None else bool(proof == expect_proof)
+    return {"value": n / el, "unit": UNIT, "cores": O.lib().wo_threads(), "kind": "port",
+            "sample": f"{n} full proofs of the same 2^{k} workload in {el:.1f} s "
+                      f"(oracle/: C restatement of the reference prover, OpenMP)",
+            "gpu_proof_identical": same}
+
+
+def run_reference(args):
+    world, rank, _ = dist_env()
+    if rank != 0:
+        return
+    from oracle import oracle as O
+    k = args.k
+    params = (k, WORKLOAD["folding"], WORKLOAD["rate"], WORKLOAD["initial_reduction"],
+              WORKLOAD["soundness_id"], WORKLOAD["security_level"])
+    poly = O.rand_fe(WORKLOAD["seed"], 1 << k)
+    groups = [[0]] * WORKLOAD["claims"]
+    for _ in range(args.warmup):
+        O.prove(params, [poly], [k], groups)
+    lat = []
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        t = time.perf_counter()
+        O.prove(params, [poly], [k], groups)
+        lat.append(time.perf_counter() - t)
+    el = time.perf_counter() - t0
+    v = args.steps / el
+    cores = O.lib().wo_threads()
+    line = {
+        "impl": "reference", "metric": METRIC, "value": v, "unit": UNIT, "n_gpus": args.gpus,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * el / args.steps,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "u32",
+        "data": "synthetic (seeded Poly::rand)", "config": workload_config(k),
+        "latency_ms": {"p50": 1e3 * float(np.percentile(lat, 50)),
+                       "p99": 1e3 * float(np.percentile(lat, 99))},
+        "cpu_baseline": {"value": v, "unit": UNIT, "cores": cores, "kind": "port",
+                         "sample": f"each step one full proof of the 2^{k} workload "
+                                   f"(oracle/ C restatement; the Rust reference cannot be built "
+                                   f"here: no cargo/rustc, Plonky3 not vendored)"},
+        "e2e": {"value": v, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line), flush=True)
+
+
+def run_gb300(args):
+    import torch
+    import whir_gb300 as W
+
+    world, rank, local = dist_env()
+    if world > 1:
+        import torch.distributed as dist
+        torch.cuda.set_device(local)
+        dist.init_process_group("nccl" if torch.cuda.is_available() else "gloo")
+    k = args.k
+    ctx = W.Context(local)
+    stream = torch.cuda.ExternalStream(ctx.stream(), device=torch.device("cuda", local))
+    params = (k, WORKLOAD["folding"], WORKLOAD["rate"], WORKLOAD["initial_reduction"],
+              WORKLOAD["soundness_id"], WORKLOAD["security_level"])
+    whir = W.Whir(ctx, *params)
+    poly = W.random_field(WORKLOAD["seed"], 1 << k)
+    groups = [[0]] * WORKLOAD["claims"]
+    dev_poly = ctx.to_device(poly)
+
+    def barrier():
+        if world > 1:
+            torch.distributed.barrier()
+
+    def prove_dev():
+        t = W.PoseidonWriter()
+        whir.prove(t, dev_poly, [k], groups)
+        t.draw_base()
+        return t
+
+    for _ in range(args.warmup):
+        first = prove_dev()
+    gpu_proof = first.finalize()
+
+    # ---- value: device-resident input ----
+    clocks = ClockSampler(local)
+    barrier()
+    torch.cuda.synchronize(local)
+    ctx.prof_read(0), ctx.prof_read(1), ctx.prof_read(2), ctx.prof_read(3)
+    ctx.prof_enable(True)
+    launches0, _, _ = ctx.counters()
+    clocks.start()
+    evs = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps + 1)]
+    evs[0].record(stream)
+    for i in range(args.steps):
+        prove_dev()
+        evs[i + 1].record(stream)
+    evs[-1].synchronize()
+    clk = clocks.stop()
+    launches1, _, _ = ctx.counters()
+    ctx.prof_enable(False)
+    barrier()
+    total_ms = evs[0].elapsed_time(evs[-1])
+    lat = [evs[i].elapsed_time(evs[i + 1]) for i in range(args.steps)]
+    prof = {}
+    for klass, name in ((0, "dft"), (1, "leaf_hash"), (2, "merkle_tree"), (3, "sumcheck")):
+        ms, n, b = ctx.prof_read(klass)
+        prof[name] = {"ms_per_step": ms / args.steps, "launches_per_step": n / args.steps,
+                      "share": ms / total_ms if total_ms else None,
+                      "achieved_gbs": (b / (ms * 1e-3) / 1e9) if ms else None,
+                      "bytes_per_step": b / args.steps}
+    if world > 1:
+        t = torch.tensor([total_ms], dtype=torch.float64, device=f"cuda:{local}")
+        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+        total_ms = float(t.item())
+    value = world * args.steps / (total_ms * 1e-3)
+
+    # ---- e2e: pinned host input through the C ABI ----
+    host_t = torch.empty(1 << k, dtype=torch.int32, pin_memory=True)
+    host = host_t.numpy().view(np.uint32)
+    host[:] = poly
+
+    def prove_host():
+        t = W.PoseidonWriter()
+        whir.prove(t, host, [k], groups)
+        t.draw_base()
+        return t.finalize()
+
+    prove_host()
+    barrier()
+    torch.cuda.synchronize(local)
+    _, h2d0, d2h0 = ctx.counters()
+    t0 = time.perf_counter()
+    e2e_lat = []
+    for i in range(args.steps):
+        ts = time.perf_counter()
+        prove_host()
+        e2e_lat.append(time.perf_counter() - ts)
+    e2e_s = time.perf_counter() - t0
+    _, h2d1, d2h1 = ctx.counters()
+    barrier()
+    if world > 1:
+        t = torch.tensor([e2e_s], dtype=torch.float64, device=f"cuda:{local}")
+        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+        e2e_s = float(t.item())
+
+    if rank != 0:
+        return
+    peaks = {}
+    try:
+        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
+            peaks = json.load(f)
+    except Exception:
+        pass
+    hbm_peak = peaks.get("hbm_gbs")
+    peak_src = "measured" if hbm_peak else "fallback"
+    hbm_peak = hbm_peak or 6800.0
+    dom = max(prof, key=lambda n: prof[n]["ms_per_step"])
+    d = prof[dom]
+    per_launch_ms = d["ms_per_step"] / max(d["launches_per_step"], 1e-9)
+    achieved = d["achieved_gbs"]
+    traffic = NCU_TRAFFIC_BYTES.get(dom)
+    line = {
+        "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": total_ms / args.steps, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "u32",
+        "data": "synthetic (seeded Poly::rand, as the reference harness)",
+        "config": workload_config(k),
+        "latency_ms": {"p50": float(np.percentile(lat, 50)), "p99": float(np.percentile(lat, 99))},
+        "e2e": {"value": world * args.steps / e2e_s, "unit": UNIT,
+                "h2d_bytes_per_step": (h2d1 - h2d0) / args.steps,
+                "d2h_bytes_per_step": (d2h1 - d2h0) / args.steps,
+                "latency_ms": {"p50": 1e3 * float(np.percentile(e2e_lat, 50)),
+                               "p99": 1e3 * float(np.percentile(e2e_lat, 99))}},
+        "roofline": {"kernel": dom, "bound": "hbm", "achieved": achieved, "peak": hbm_peak,
+                     "unit": "GB/s", "frac": achieved / hbm_peak if achieved else None,
+                     "peak_source": peak_src, "traffic": traffic,
+                     "per_launch_ms": per_launch_ms,
+                     "note": "Poseidon2 hashing is integer-pipe bound; frac is against HBM"},
+        "kernels": prof,
+        "gpu_launches": int(launches1 - launches0),
+        "clocks": clk,
+    }
+    if not args.no_cpu_baseline and world == 1:
+        line["cpu_baseline"] = cpu_baseline(k, args.cpu_seconds, expect_proof=gpu_proof)
+    print(json.dumps(line), flush=True)
+
+
+def main():
+    args = parse()
+    if args.impl == "reference":
+        run_reference(args)
+    else:
+        run_gb300(args)
+
+
+if __name__ == "__main__":
+    main()

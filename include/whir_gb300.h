@@ -130,6 +130,11 @@ WHIR_API int whir_combine_pows_scaled(whir_ctx *ctx, uint32_t *weights, int k, c
  * (crates/whir/src/test.rs:195-196). */
 WHIR_API int whir_poseidon2_permute(int width, uint32_t *state);
 
+/* n field elements as Poly::rand(&mut rng(seed), ..) draws them (StdRng
+ * seed_from_u64 + StandardUniform<KoalaBear>, crates/poly/src/utils.rs:6-11):
+ * the reference harness's seeded polynomial (crates/whir/src/test.rs:213,219). */
+WHIR_API int whir_random_field(uint64_t seed, uint32_t *out, size_t n);
+
 /* ---- Fiat-Shamir transcript.  Replaces PoseidonWriter<Vec<u8>, KoalaBear,
  * DuplexChallenger<_, Poseidon2<16>, 16, 8>> (crates/transcript/src/poseidon.rs:13-87)
  * with the challenger permutation of the harness (test.rs:195-200). ---- */
@@ -171,6 +176,10 @@ WHIR_API int whir_prove(whir_prover *p, whir_transcript *t, const uint32_t *poly
  * clears total ms, launches and algorithmic bytes since enabling. ---- */
 WHIR_API int whir_prof_enable(whir_ctx *ctx, int on);
 WHIR_API int whir_prof_read(whir_ctx *ctx, int klass, double *ms, long *launches, double *bytes);
+/* kernels launched by this library in this process, and the bytes the
+ * prover of this context copied host->device / device->host, since start */
+WHIR_API int whir_counters(whir_ctx *ctx, uint64_t *kernel_launches, uint64_t *h2d_bytes,
+                           uint64_t *d2h_bytes);
 
 #ifdef __cplusplus
 }

@@ -85,6 +85,10 @@ _SIGS = {
                                       ctypes.POINTER(ctypes.c_long),
                                       ctypes.POINTER(ctypes.c_double)]),
     "whir_poseidon2_permute": (ctypes.c_int, [ctypes.c_int, u32p]),
+    "whir_random_field": (ctypes.c_int, [ctypes.c_uint64, u32p, ctypes.c_size_t]),
+    "whir_counters": (ctypes.c_int, [vp, ctypes.POINTER(ctypes.c_uint64),
+                                     ctypes.POINTER(ctypes.c_uint64),
+                                     ctypes.POINTER(ctypes.c_uint64)]),
 }
 
 
@@ -178,6 +182,12 @@ class Context:
 
     def prof_enable(self, on=True):
         _check(lib().whir_prof_enable(self.h, 1 if on else 0))
+
+    def counters(self):
+        """(kernel launches in this process, prover h2d bytes, prover d2h bytes)"""
+        a, b, c = ctypes.c_uint64(), ctypes.c_uint64(), ctypes.c_uint64()
+        _check(lib().whir_counters(self.h, ctypes.byref(a), ctypes.byref(b), ctypes.byref(c)))
+        return a.value, b.value, c.value
 
     def prof_read(self, klass):
         ms, n, b = ctypes.c_double(), ctypes.c_long(), ctypes.c_double()
@@ -286,6 +296,13 @@ def combine_pows_scaled(ctx, dev_w, k, vars_, n, scales):
     va, vpp = _u32(vars_)
     sc, sp = _u32(scales)
     _check(lib().whir_combine_pows_scaled(ctx.h, dev_w.ptr, k, vpp, n, sp))
+
+
+def random_field(seed, n, out=None):
+    """Poly::rand(&mut rng(seed), ..): n seeded KoalaBear elements (Montgomery words)."""
+    out = np.empty(n, np.uint32) if out is None else out
+    _check(lib().whir_random_field(seed, out.ctypes.data_as(u32p), n))
+    return out
 
 
 def poseidon2_permute(width, state):

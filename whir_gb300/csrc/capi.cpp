@@ -409,6 +409,13 @@ int whir_poseidon2_permute(int width, uint32_t *state) {
   API_END
 }
 
+int whir_random_field(uint64_t seed, uint32_t *out, size_t n) {
+  API_BEGIN
+  need(out != nullptr || n == 0, "null out");
+  whir::std_rng_fill_field(seed, out, n);
+  API_END
+}
+
 int whir_transcript_new(whir_transcript **out) {
   API_BEGIN
   need(out != nullptr, "null out");
@@ -540,6 +547,16 @@ int whir_prof_read(whir_ctx *ctx, int klass, double *ms, long *launches, double 
   need(ctx && ms && launches && bytes, "null argument");
   need(klass >= 0 && klass < Context::K_NCLASS, "bad kernel class");
   ctx->ctx.prof_read(klass, ms, launches, bytes);
+  API_END
+}
+
+int whir_counters(whir_ctx *ctx, uint64_t *kernel_launches, uint64_t *h2d_bytes,
+                  uint64_t *d2h_bytes) {
+  API_BEGIN
+  need(ctx && kernel_launches && h2d_bytes && d2h_bytes, "null argument");
+  *kernel_launches = whir::gpu::launch_count();
+  *h2d_bytes = ctx->ctx.h2d_bytes();
+  *d2h_bytes = ctx->ctx.d2h_bytes();
   API_END
 }
 

@@ -11,6 +11,10 @@
 namespace whir {
 namespace gpu {
 
+// ---- kernel launches issued by this library (all contexts), for reporting ----
+unsigned long long launch_count();
+void count_launches(unsigned n);
+
 // ---- one-time device set-up (constants, twiddle tables) ----
 cudaError_t init_device_tables();
 

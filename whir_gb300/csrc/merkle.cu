@@ -3,6 +3,8 @@
 // opening gather.  Tree shape and hashing follow
 // crates/merkle/src/poseidon_packed.rs:98-143,269-304,344-384 and
 // crates/merkle/src/poseidon.rs:33-74.
+#include <atomic>
+
 #include "kernels.h"
 #include "p2_device.cuh"
 #include "poseidon2_host.h"
@@ -21,6 +23,10 @@ static cudaError_t upload_p2(int width) {
   if (width == 16) return cudaMemcpyToSymbol(c_p2_16, buf, n * 4);
   return cudaMemcpyToSymbol(c_p2_24, buf, n * 4);
 }
+
+static std::atomic<unsigned long long> g_launches{0};
+unsigned long long launch_count() { return g_launches.load(); }
+void count_launches(unsigned n) { g_launches.fetch_add(n, std::memory_order_relaxed); }
 
 cudaError_t init_poseidon2_tables() {
   cudaError_t e = upload_p2(16);
@@ -87,6 +93,7 @@ cudaError_t hash_rows(const uint32_t *rows, size_t n_rows, int row_len, uint32_t
   if (aligned && row_len == 16) hash_rows_fixed<16><<<grid, T, 0, st>>>(rows, n_rows, digests);
   else if (aligned && row_len == 64) hash_rows_fixed<64><<<grid, T, 0, st>>>(rows, n_rows, digests);
   else hash_rows_generic<<<grid, T, 0, st>>>(rows, n_rows, row_len, digests);
+  count_launches(1);
   return cudaGetLastError();
 }
 
@@ -112,6 +119,7 @@ cudaError_t build_tree(uint32_t *nodes, int log_h, cudaStream_t st) {
     uint32_t *src = nodes + level_offset_words(log_h, l);
     uint32_t *dst = nodes + level_offset_words(log_h, l + 1);
     compress_level<<<(unsigned)((half + T - 1) / T), T, 0, st>>>(src, dst, half);
+    count_launches(1);
   }
   return cudaGetLastError();
 }
@@ -140,6 +148,7 @@ cudaError_t gather_openings(const uint32_t *rows, int row_len, const uint32_t *n
                             const uint32_t *idx, int n, uint32_t *out, cudaStream_t st) {
   if (n == 0) return cudaSuccess;
   gather_openings_kernel<<<n, 128, 0, st>>>(rows, row_len, nodes, log_h, idx, n, out);
+  count_launches(1);
   return cudaGetLastError();
 }
 

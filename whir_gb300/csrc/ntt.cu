@@ -115,6 +115,7 @@ static cudaError_t launch_tile(const uint32_t *in, uint32_t *out, int S, size_t 
   dim3 grid((unsigned)n_outer, (unsigned)(width / C));
   dft_tile<C><<<grid, threads, smem, st>>>(in, out, S, width, rows_valid, a_in, b_in, a_out,
                                            b_out, tw_log);
+  count_launches(1);
   return cudaGetLastError();
 }
 

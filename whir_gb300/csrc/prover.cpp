@@ -157,6 +157,15 @@ void Context::prof_read(int klass, double *ms, long *launches, double *bytes) {
   acc_bytes_[klass] = 0;
 }
 
+cudaError_t copy_async(Context &c, void *dst, const void *src, size_t bytes, cudaMemcpyKind kind) {
+  c.count_copy(bytes, kind);
+  return cudaMemcpyAsync(dst, src, bytes, kind, c.stream());
+}
+void Context::count_copy(size_t bytes, int kind) {
+  if (kind == cudaMemcpyHostToDevice) h2d_bytes_ += bytes;
+  if (kind == cudaMemcpyDeviceToHost) d2h_bytes_ += bytes;
+}
+
 // ---------------- host helpers ----------------
 static E4 e_inv2() { return e_from(inv(from_canonical(2))); }
 static void lagrange012(const E4 &r, E4 w[3]) {
@@ -235,7 +244,7 @@ void encode_commit(Context &ctx, const uint32_t *src, int k, int rate, int foldi
   cuda_check(gpu::build_tree(nodes, log_h, st), "build_tree");
   ctx.prof_end(Context::K_TREE, 32.0 * (double)(2 * rows - 2 + rows - 1));
   uint32_t *h = (uint32_t *)ctx.pinned(64);
-  cuda_check(cudaMemcpyAsync(h, nodes + gpu::tree_words(log_h) - 8, 32, cudaMemcpyDeviceToHost, st),
+  cuda_check(copy_async(ctx, h, nodes + gpu::tree_words(log_h) - 8, 32, cudaMemcpyDeviceToHost),
              "root copy");
   ctx.sync();
   out->rows = codeword;
@@ -401,7 +410,7 @@ struct Prover::Impl {
     cuda_check(gpu::compress_hi(poly_dev, kp, ks, lo, s_lo, hi, a, st()), "compress_hi");
     ctx->prof_end(Context::K_SUMCHECK, 4.0 * (double)((size_t)1 << kp));
     unsigned long long *h = (unsigned long long *)ctx->pinned(8 * na);
-    cuda_check(cudaMemcpyAsync(h, a, 8 * na, cudaMemcpyDeviceToHost, st()), "d2h");
+    cuda_check(copy_async(*ctx, h, a, 8 * na, cudaMemcpyDeviceToHost), "d2h");
     ctx->sync();
     size_t n = (size_t)1 << ks;
     c.compressed.resize(n);
@@ -494,7 +503,7 @@ struct Prover::Impl {
 
   void read_c0c2(E4 *c0, E4 *c2) {
     unsigned long long *h = (unsigned long long *)ctx->pinned(64);
-    cuda_check(cudaMemcpyAsync(h, acc.as<unsigned long long>(), 64, cudaMemcpyDeviceToHost, st()),
+    cuda_check(copy_async(*ctx, h, acc.as<unsigned long long>(), 64, cudaMemcpyDeviceToHost),
                "d2h");
     ctx->sync();
     *c0 = reduce_acc(h);
@@ -571,7 +580,7 @@ struct Prover::Impl {
     memcpy(h, scales.data(), scales.size() * 16);
     memcpy(h + scales.size() * 16, vars.data(), vars.size() * 4);
     if (bytes > small.bytes()) small.reserve(bytes);
-    cuda_check(cudaMemcpyAsync(small.as<uint8_t>(), h, bytes, cudaMemcpyHostToDevice, st()), "h2d");
+    cuda_check(copy_async(*ctx, small.as<uint8_t>(), h, bytes, cudaMemcpyHostToDevice), "h2d");
     cuda_check(gpu::add_pows(W(), kc, (const uint32_t *)(small.as<uint8_t>() + scales.size() * 16),
                              small.as<E4>(), (int)vars.size(), st()),
                "add_pows");
@@ -674,11 +683,11 @@ struct Prover::Impl {
     size_t need = 4 * (size_t)n + 4 * per * n;
     if (need > gather.bytes()) gather.reserve(need);
     uint32_t *didx = gather.as<uint32_t>(), *dout = didx + n;
-    cuda_check(cudaMemcpyAsync(didx, hidx, 4 * n, cudaMemcpyHostToDevice, st()), "h2d");
+    cuda_check(copy_async(*ctx, didx, hidx, 4 * n, cudaMemcpyHostToDevice), "h2d");
     cuda_check(gpu::gather_openings(t.rows, t.row_len, t.nodes, t.log_h, didx, n, dout, st()),
                "gather");
     uint32_t *hout = hidx + n;
-    cuda_check(cudaMemcpyAsync(hout, dout, 4 * per * n, cudaMemcpyDeviceToHost, st()), "d2h");
+    cuda_check(copy_async(*ctx, hout, dout, 4 * per * n, cudaMemcpyDeviceToHost), "d2h");
     ctx->sync();
     rows.resize((size_t)t.row_len * n);
     for (int i = 0; i < n; i++) {
@@ -769,13 +778,13 @@ struct Prover::Impl {
       if (need > gather.bytes()) gather.reserve(need);
       uint32_t *didx = gather.as<uint32_t>();
       E4 *dout = reinterpret_cast<E4 *>(didx + ((m + 3) & ~(size_t)3));
-      cuda_check(cudaMemcpyAsync(didx, h, 4 * m, cudaMemcpyHostToDevice, st()), "h2d");
+      cuda_check(copy_async(*ctx, didx, h, 4 * m, cudaMemcpyHostToDevice), "h2d");
       gpu::Point rsp;
       rsp.k = (int)rs.size();
       for (size_t i = 0; i < rs.size(); i++) rsp.z[i] = rs[i];
       cuda_check(gpu::row_evals(t0.rows, t0.row_len, didx, (int)m, rsp, dout, st()), "row_evals");
       E4 *hout = reinterpret_cast<E4 *>(h + ((m + 3) & ~(size_t)3));
-      cuda_check(cudaMemcpyAsync(hout, dout, 16 * m, cudaMemcpyDeviceToHost, st()), "d2h");
+      cuda_check(copy_async(*ctx, hout, dout, 16 * m, cudaMemcpyDeviceToHost), "d2h");
       ctx->sync();
       evals.reserve(m * 2);
       for (size_t i = 0; i < m; i++) evals[ri[i]] = hout[i];
@@ -895,7 +904,7 @@ struct Prover::Impl {
     flush();
     size_t nf = (size_t)1 << kc;
     E4 *hf = (E4 *)ctx->pinned(16 * nf);
-    cuda_check(cudaMemcpyAsync(hf, P(), 16 * nf, cudaMemcpyDeviceToHost, st()), "d2h");
+    cuda_check(copy_async(*ctx, hf, P(), 16 * nf, cudaMemcpyDeviceToHost), "d2h");
     ctx->sync();
     std::vector<E4> fp(hf, hf + nf);
     for (auto &e : fp) ts.write_ext(e);
@@ -912,7 +921,7 @@ struct Prover::Impl {
     int k = kc;
     if (k == 0) {
       E4 *h = (E4 *)ctx->pinned(16);
-      cuda_check(cudaMemcpyAsync(h, P(), 16, cudaMemcpyDeviceToHost, st()), "d2h");
+      cuda_check(copy_async(*ctx, h, P(), 16, cudaMemcpyDeviceToHost), "d2h");
       ctx->sync();
       return *h;
     }
@@ -926,7 +935,7 @@ struct Prover::Impl {
     cuda_check(cudaMemsetAsync(a, 0, 32, st()), "memset");
     cuda_check(gpu::eval_ext(P(), k, lo, s_lo, hi, a, st()), "eval_ext");
     unsigned long long *h = (unsigned long long *)ctx->pinned(64);
-    cuda_check(cudaMemcpyAsync(h, a, 32, cudaMemcpyDeviceToHost, st()), "d2h");
+    cuda_check(copy_async(*ctx, h, a, 32, cudaMemcpyDeviceToHost), "d2h");
     ctx->sync();
     return reduce_acc(h);
   }
@@ -969,8 +978,8 @@ void Prover::commit(Transcript &ts, const uint32_t *polys, bool on_device,
   size_t src_off = 0;
   for (int id = 0; id < m.n_polys; id++) {
     size_t n = (size_t)1 << poly_k[id];
-    cuda_check(cudaMemcpyAsync(stk + m.poly_off[id], polys + src_off, 4 * n,
-                               on_device ? cudaMemcpyDeviceToDevice : cudaMemcpyHostToDevice, st),
+    cuda_check(copy_async(*ctx_, stk + m.poly_off[id], polys + src_off, 4 * n,
+                          on_device ? cudaMemcpyDeviceToDevice : cudaMemcpyHostToDevice),
                "poly copy");
     src_off += n;
   }

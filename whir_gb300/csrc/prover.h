@@ -73,6 +73,10 @@ class Context {
   void prof_end(int klass, double bytes);
   // drains recorded events: total ms, launches and bytes per class
   void prof_read(int klass, double *ms, long *launches, double *bytes);
+  // bytes copied host<->device through copy_async since creation
+  void count_copy(size_t bytes, int kind);
+  unsigned long long h2d_bytes() const { return h2d_bytes_; }
+  unsigned long long d2h_bytes() const { return d2h_bytes_; }
 
  private:
   int device_;
@@ -90,10 +94,14 @@ class Context {
   double acc_ms_[K_NCLASS] = {0, 0, 0, 0};
   long acc_n_[K_NCLASS] = {0, 0, 0, 0};
   double acc_bytes_[K_NCLASS] = {0, 0, 0, 0};
+  unsigned long long h2d_bytes_ = 0, d2h_bytes_ = 0;
   int open_klass_ = -1;
   cudaEvent_t open_ev_ = nullptr;
   cudaEvent_t take_event();
 };
+
+// cudaMemcpyAsync on the context stream, counted in the context's totals
+cudaError_t copy_async(Context &c, void *dst, const void *src, size_t bytes, cudaMemcpyKind kind);
 
 // Merkle data kept on the device (MerkleData, crates/merkle/src/lib.rs:11-17)
 struct DeviceTree {

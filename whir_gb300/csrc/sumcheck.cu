@@ -37,6 +37,7 @@ static cudaError_t eq_part(const Point &z, int off, int nv, E4 scale, E4 *out, c
   size_t n = (size_t)1 << nv;
   unsigned T = 256, G = (unsigned)((n + T - 1) / T);
   eq_entries<<<G, T, 0, st>>>(z, off, nv, scale, out);
+  count_launches(1);
   return cudaGetLastError();
 }
 
@@ -60,6 +61,7 @@ cudaError_t eq_full(const Point &z, E4 scale, E4 *out, E4 *tmp, cudaStream_t st)
   if (e != cudaSuccess) return e;
   size_t n = (size_t)1 << z.k;
   eq_join<<<(unsigned)((n + 255) / 256), 256, 0, st>>>(lo, hi, s, n, out);
+  count_launches(1);
   return cudaGetLastError();
 }
 
@@ -107,6 +109,7 @@ cudaError_t compress_hi(const uint32_t *poly, int k, int ks, const E4 *eq_lo, in
   unsigned grid = (unsigned)(n_hi < 152 * 8 ? n_hi : 152 * 8);
   size_t smem = ((size_t)1 << s_lo) * sizeof(E4) + ((size_t)4 << ks) * 8;
   compress_hi_kernel<<<grid, CH_T, smem, st>>>(poly, k, ks, eq_lo, s_lo, eq_hi, acc);
+  count_launches(1);
   return cudaGetLastError();
 }
 
@@ -139,6 +142,7 @@ cudaError_t compress_lo(const uint32_t *poly, int k, const Point &rs, E4 *out, c
   size_t g = (n_out + T - 1) / T;
   unsigned grid = (unsigned)(g < 152 * 16 ? g : 152 * 16);
   compress_lo_kernel<<<grid, T, 0, st>>>(poly, ks, n_out, rs, out);
+  count_launches(1);
   return cudaGetLastError();
 }
 
@@ -165,6 +169,7 @@ cudaError_t add_eq(E4 *w, int k, const E4 *tables, int n_tables, cudaStream_t st
   unsigned grid = (unsigned)(g < 152 * 16 ? g : 152 * 16);
   add_eq_kernel<<<grid, T, 0, st>>>(w, n, s, (size_t)1 << s, (size_t)1 << (k - s), tables,
                                     n_tables);
+  count_launches(1);
   return cudaGetLastError();
 }
 
@@ -193,6 +198,7 @@ cudaError_t add_pows(E4 *w, int k, const uint32_t *vars, const E4 *scales, int n
   size_t N = (size_t)1 << k, threads = (N + 15) / 16;
   unsigned T = 128;
   add_pows_kernel<<<(unsigned)((threads + T - 1) / T), T, 0, st>>>(w, N, vars, scales, n);
+  count_launches(1);
   return cudaGetLastError();
 }
 
@@ -264,6 +270,7 @@ cudaError_t sumcheck_round(const E4 *p_in, const E4 *w_in, size_t n_in, bool fol
   unsigned grid = (unsigned)(g < 152 * 8 ? (g ? g : 1) : 152 * 8);
   round_kernel<<<grid, T, 0, st>>>(p_in, w_in, n_in, fold ? 1 : 0, r, p_out, w_out,
                                    coeffs ? 1 : 0, acc);
+  count_launches(1);
   return cudaGetLastError();
 }
 
@@ -289,6 +296,7 @@ cudaError_t eval_ext(const E4 *poly, int k, const E4 *eq_lo, int s_lo, const E4 
   size_t n_hi = (size_t)1 << (k - s_lo);
   unsigned grid = (unsigned)(n_hi < 152 * 8 ? n_hi : 152 * 8);
   eval_ext_kernel<<<grid, 256, 0, st>>>(poly, k, eq_lo, s_lo, eq_hi, acc);
+  count_launches(1);
   return cudaGetLastError();
 }
 
@@ -315,6 +323,7 @@ cudaError_t row_evals(const uint32_t *rows, int row_len, const uint32_t *idx, in
   if (n == 0) return cudaSuccess;
   if (row_len > 256 || (1 << rs.k) != row_len) return cudaErrorInvalidValue;
   row_evals_kernel<<<(n + 127) / 128, 128, 0, st>>>(rows, row_len, idx, n, rs, out);
+  count_launches(1);
   return cudaGetLastError();
 }
 
