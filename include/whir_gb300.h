@@ -171,6 +171,22 @@ WHIR_API int whir_prove(whir_prover *p, whir_transcript *t, const uint32_t *poly
                const int32_t *poly_k, int n_polys, const int32_t *group_n, int n_groups,
                const int32_t *group_ids);
 
+/* ---- allocation-free SVO compression.  No counterpart in the reference:
+ * an extra entry point for callers that must not allocate device memory (a
+ * host whose GPU memory is all owned by its own pool, or code that cannot
+ * afford the device-wide synchronisation cudaMalloc/cudaFree may cause
+ * mid-proof).  Same result as whir_compress_hi, but it allocates nothing:
+ * its scratch is one fixed 40 KiB device array inside the library, held by
+ * every GPU that loads it until exit.  Limits: kz <= 20 fixed variables and
+ * k - kz <= 8 kept ones; larger sizes return WHIR_ERR_ARG.  Runs on
+ * cuda_stream (NULL: the default stream) of the current device and returns
+ * once out (host, 2^(k-kz) extension elements) is written.  The first call
+ * on a device looks up the array's device address; make it before any
+ * stream capture.  All calls share the array: calls that overlap on the GPU
+ * (other streams, other threads) race; calls on one stream are safe. ---- */
+WHIR_API int whir_compress_hi_noalloc(void *cuda_stream, const uint32_t *poly, int k,
+                                      const uint32_t *point, int kz, uint32_t *out);
+
 /* ---- per-kernel-class timing with CUDA events on the context stream:
  * klass 0 DFT, 1 leaf hash, 2 tree, 3 sumcheck passes.  read returns and
  * clears total ms, launches and algorithmic bytes since enabling. ---- */

@@ -18,7 +18,7 @@ BUILD = os.path.join(HERE, "_build")
 LIBDIR = os.path.join(HERE, "_lib")
 LIB = os.path.join(LIBDIR, "libwhir_gb300.so")
 
-CU_SOURCES = ["ntt.cu", "merkle.cu", "sumcheck.cu"]
+CU_SOURCES = ["ntt.cu", "merkle.cu", "sumcheck.cu", "noalloc.cu"]
 CPP_SOURCES = ["poseidon2_host.cpp", "transcript.cpp", "prover.cpp", "capi.cpp"]
 GENCODE = ["-gencode", "arch=compute_103a,code=sm_103a"]
 

@@ -59,6 +59,9 @@ static thread_local std::string g_err;
     return WHIR_ERR_INTERNAL;                            \
   }
 
+// error text for entry points defined outside this file
+void whir_record_error(const char *msg) { g_err = msg; }
+
 static void need(bool ok, const char *what) {
   if (!ok) throw WhirError(-1, what);
 }
