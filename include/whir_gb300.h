@@ -188,7 +188,8 @@ WHIR_API int whir_compress_hi_noalloc(void *cuda_stream, const uint32_t *poly, i
                                       const uint32_t *point, int kz, uint32_t *out);
 
 /* ---- per-kernel-class timing with CUDA events on the context stream:
- * klass 0 DFT, 1 leaf hash, 2 tree, 3 sumcheck passes.  read returns and
+ * klass 0 DFT, 1 leaf hash, 2 tree, 3 sumcheck passes; klass 4 is host time
+ * blocked waiting for the stream (ms and number of waits).  read returns and
  * clears total ms, launches and algorithmic bytes since enabling. ---- */
 WHIR_API int whir_prof_enable(whir_ctx *ctx, int on);
 WHIR_API int whir_prof_read(whir_ctx *ctx, int klass, double *ms, long *launches, double *bytes);

@@ -20,7 +20,7 @@ from . import build as _build
 
 P = 0x7F000001
 SOUNDNESS = {"UniqueDecoding": 0, "JohnsonBound": 1, "CapacityBound": 2}
-PROF_DFT, PROF_LEAF, PROF_TREE, PROF_SUMCHECK = 0, 1, 2, 3
+PROF_DFT, PROF_LEAF, PROF_TREE, PROF_SUMCHECK, PROF_SYNC = 0, 1, 2, 3, 4
 
 _lib = None
 u32p = ctypes.POINTER(ctypes.c_uint32)

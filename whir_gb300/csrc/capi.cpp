@@ -366,10 +366,11 @@ static void combine_pows_impl(whir_ctx *ctx, uint32_t *weights, int k, const uin
   whir::cuda_check(cudaMemcpyAsync(ctx->small.as<uint8_t>(), h.data(), bytes,
                                    cudaMemcpyHostToDevice, st),
                    "h2d");
+  ctx->eq.reserve(4 * whir::gpu::add_pows_scratch_words(k, n));
   whir::cuda_check(whir::gpu::add_pows(reinterpret_cast<E4 *>(weights), k,
                                        reinterpret_cast<const uint32_t *>(ctx->small.as<uint8_t>() +
                                                                           16 * (size_t)n),
-                                       ctx->small.as<E4>(), n, st),
+                                       ctx->small.as<E4>(), n, ctx->eq.as<uint32_t>(), st),
                    "add_pows");
   ctx->ctx.sync();
 }

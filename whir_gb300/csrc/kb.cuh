@@ -42,8 +42,8 @@ KB_HD uint32_t mul(uint32_t a, uint32_t b) {
   uint32_t lo = a * b, hi = mulhi(a, b);
   uint32_t t = lo * MU;
   uint32_t th = mulhi(t, P);
-  uint32_t r = hi - th;
-  return hi < th ? r + P : r;
+  uint32_t r = hi - th;  // in (-p, p); as u32, r + p is the smaller one iff r < 0
+  return umin(r, r + P);
 }
 // reduction of a 64-bit sum x < 2p * 2^32 (e.g. four products of canonical words)
 KB_HD uint32_t reduce_wide(uint64_t x) {
@@ -54,6 +54,8 @@ KB_HD uint32_t reduce_wide(uint64_t x) {
   if (hi < th) return r + P;
   return umin(r, r - P);
 }
+// a + b and a - b of canonical words: one add and an unsigned min (measured
+// on GB300 to be the fastest reduction of the alternatives tried).
 KB_HD uint32_t add(uint32_t a, uint32_t b) {
   uint32_t r = a + b;
   return umin(r, r - P);

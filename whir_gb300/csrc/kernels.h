@@ -50,6 +50,11 @@ struct Point {
 // lo/hi hold 2^s and 2^(k-s) E4.
 cudaError_t eq_split(const Point &z, int s, kb::E4 scale, kb::E4 *lo, kb::E4 *hi,
                      cudaStream_t st);
+// n split tables at once: pts (device) n x k extension elements, scales (device)
+// n; table t at out + t * (2^s + 2^(k-s)): lo over pts[t][0..s), hi over the
+// rest times scales[t]
+cudaError_t eq_tables(const kb::E4 *pts, const kb::E4 *scales, int n, int k, int s, kb::E4 *out,
+                      cudaStream_t st);
 // full table eq(z) * scale of 2^k entries (k <= 24)
 cudaError_t eq_full(const Point &z, kb::E4 scale, kb::E4 *out, kb::E4 *tmp, cudaStream_t st);
 
@@ -65,9 +70,11 @@ cudaError_t compress_lo(const uint32_t *poly, int k, const Point &rs, kb::E4 *ou
 // stored back to back (lo0, hi0, lo1, hi1, ...), s = k / 2, each lo 2^s and
 // hi 2^(k-s) entries.
 cudaError_t add_eq(kb::E4 *w, int k, const kb::E4 *tables, int n_tables, cudaStream_t st);
-// w[i] += sum_t scale_t * var_t^i  (pow::combine_pows(_scaled), combine.rs:408-468)
+// w[i] += sum_t scale_t * var_t^i  (pow::combine_pows(_scaled), combine.rs:408-468);
+// tab: add_pows_scratch_words(k, n) words for the split power tables
+size_t add_pows_scratch_words(int k, int n);
 cudaError_t add_pows(kb::E4 *w, int k, const uint32_t *vars, const kb::E4 *scales, int n,
-                     cudaStream_t st);
+                     uint32_t *tab, cudaStream_t st);
 // one sumcheck round (expr.rs:14-27, poly.rs:131-142): optionally fold both
 // arrays by r into (p_out, w_out), then add (c0, c2) of the result into acc
 // (u64[8], unreduced canonical) when coeffs != 0.

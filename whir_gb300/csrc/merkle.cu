@@ -112,13 +112,122 @@ __global__ void __launch_bounds__(128) compress_level(const uint32_t *__restrict
   d[1] = make_uint4(s[4], s[5], s[6], s[7]);
 }
 
+// ---- warp-cooperative width-16 permutation for the small tree levels ----
+// A level with few nodes is bound by the latency of one permutation, not by
+// throughput.  Here the 16 lanes of a half-warp hold the 16 state words, so
+// the S-boxes of a full round run in parallel and the linear layers are a
+// few shuffles: mat4 inside each group of 4 lanes, column sums by xor
+// shuffles across groups, and the internal layer's sum by a 4-step xor
+// reduction.  Two nodes per warp (lanes 0-15 and 16-31).
+constexpr unsigned FULL = 0xffffffffu;
+
+__device__ __forceinline__ uint32_t p2w_mds(uint32_t x, int l) {
+  using namespace kb;
+  const int g = l & ~3;  // first lane of this group of 4 (shuffle width 16)
+  uint32_t x0 = __shfl_sync(FULL, x, g, 16), x1 = __shfl_sync(FULL, x, g + 1, 16);
+  uint32_t x2 = __shfl_sync(FULL, x, g + 2, 16), x3 = __shfl_sync(FULL, x, g + 3, 16);
+  uint32_t t01 = add(x0, x1), t23 = add(x2, x3), t0123 = add(t01, t23);
+  uint32_t t01123 = add(t0123, x1), t01233 = add(t0123, x3);
+  uint32_t y;
+  switch (l & 3) {
+    case 0: y = add(t01123, t01); break;
+    case 1: y = add(t01123, dbl(x2)); break;
+    case 2: y = add(t01233, t23); break;
+    default: y = add(t01233, dbl(x0)); break;
+  }
+  uint32_t s = add(y, __shfl_xor_sync(FULL, y, 4, 16));
+  s = add(s, __shfl_xor_sync(FULL, s, 8, 16));
+  return add(y, s);
+}
+
+struct P2WarpConsts {
+  uint32_t ext[8];  // this lane's external round constants
+  uint32_t diag;    // this lane's internal diagonal entry
+};
+__device__ __forceinline__ P2WarpConsts p2w_consts(int l) {
+  P2WarpConsts k;
+#pragma unroll
+  for (int r = 0; r < 8; r++) k.ext[r] = c_p2_16[r * 16 + l];
+  k.diag = c_p2_16[8 * 16 + 20 + l];
+  return k;
+}
+
+__device__ __forceinline__ uint32_t p2w_permute(uint32_t x, int l, const P2WarpConsts &k) {
+  using namespace kb;
+  x = p2w_mds(x, l);
+#pragma unroll
+  for (int r = 0; r < 4; r++) x = p2w_mds(cube(add(x, k.ext[r])), l);
+#pragma unroll 4
+  for (int r = 0; r < 20; r++) {
+    uint32_t y = cube(add(x, c_p2_16[8 * 16 + r]));
+    x = l == 0 ? y : x;
+    uint32_t s = add(x, __shfl_xor_sync(FULL, x, 1, 16));
+    s = add(s, __shfl_xor_sync(FULL, s, 2, 16));
+    s = add(s, __shfl_xor_sync(FULL, s, 4, 16));
+    s = add(s, __shfl_xor_sync(FULL, s, 8, 16));
+    x = add(s, mul(k.diag, x));
+  }
+#pragma unroll
+  for (int r = 4; r < 8; r++) x = p2w_mds(cube(add(x, k.ext[r])), l);
+  return x;
+}
+
+// node i of the next level = C(src[i], src[i + half]); half-warp per node
+__device__ __forceinline__ void p2w_compress(const uint32_t *src, uint32_t *dst, size_t half,
+                                             size_t node, int l, const P2WarpConsts &k) {
+  bool live = node < half;
+  uint32_t x = 0;
+  if (live) x = l < 8 ? src[node * 8 + l] : src[(node + half) * 8 + (l - 8)];
+  x = p2w_permute(x, l, k);  // every lane of the warp takes part in the shuffles
+  if (live && l < 8) dst[node * 8 + l] = x;
+}
+
+__global__ void __launch_bounds__(256) compress_level_warp(const uint32_t *__restrict__ src,
+                                                           uint32_t *__restrict__ dst,
+                                                           size_t half) {
+  const int l = threadIdx.x & 15;
+  const P2WarpConsts k = p2w_consts(l);
+  size_t node = ((size_t)blockIdx.x * blockDim.x + threadIdx.x) >> 4;
+  p2w_compress(src, dst, half, node, l, k);
+}
+
+// the last levels of a tree (each at most 2^TOP_LOG nodes) in one CTA
+constexpr int TOP_LOG = 9;
+__global__ void __launch_bounds__(1024) tree_top(uint32_t *nodes, int log_h, int from_level) {
+  const int l = threadIdx.x & 15;
+  const P2WarpConsts k = p2w_consts(l);
+  const size_t slots = blockDim.x >> 4;
+  for (int lev = from_level; lev < log_h; lev++) {
+    size_t half = ((size_t)1 << (log_h - lev)) / 2;
+    const uint32_t *src = nodes + level_offset_words(log_h, lev);
+    uint32_t *dst = nodes + level_offset_words(log_h, lev + 1);
+    for (size_t base = 0; base < half; base += slots)
+      p2w_compress(src, dst, half, base + (threadIdx.x >> 4), l, k);
+    __syncthreads();
+  }
+}
+
 cudaError_t build_tree(uint32_t *nodes, int log_h, cudaStream_t st) {
   const int T = 128;
-  for (int l = 0; l < log_h; l++) {
+  int l = 0;
+  // wide levels: one thread per node (throughput)
+  for (; l < log_h && ((size_t)1 << (log_h - l)) / 2 >= ((size_t)1 << 15); l++) {
     size_t half = ((size_t)1 << (log_h - l)) / 2;
-    uint32_t *src = nodes + level_offset_words(log_h, l);
-    uint32_t *dst = nodes + level_offset_words(log_h, l + 1);
-    compress_level<<<(unsigned)((half + T - 1) / T), T, 0, st>>>(src, dst, half);
+    compress_level<<<(unsigned)((half + T - 1) / T), T, 0, st>>>(
+        nodes + level_offset_words(log_h, l), nodes + level_offset_words(log_h, l + 1), half);
+    count_launches(1);
+  }
+  // middle levels: half a warp per node (latency)
+  for (; l < log_h && ((size_t)1 << (log_h - l)) / 2 > ((size_t)1 << TOP_LOG); l++) {
+    size_t half = ((size_t)1 << (log_h - l)) / 2;
+    size_t threads = half * 16;
+    compress_level_warp<<<(unsigned)((threads + 255) / 256), 256, 0, st>>>(
+        nodes + level_offset_words(log_h, l), nodes + level_offset_words(log_h, l + 1), half);
+    count_launches(1);
+  }
+  // top levels: one CTA, one launch
+  if (l < log_h) {
+    tree_top<<<1, 1024, 0, st>>>(nodes, log_h, l);
     count_launches(1);
   }
   return cudaGetLastError();

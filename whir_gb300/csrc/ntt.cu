@@ -4,7 +4,11 @@
 //
 // A row-major matrix of `width` columns is transformed down each column.
 // Sizes up to 2^11 run in one pass: a CTA stages one column slice of the
-// whole column in shared memory and runs radix-2 stages there.  Larger sizes
+// whole column in shared memory and runs a decimation-in-frequency transform
+// there, three radix-2 stages per step in registers.  When the nonzero input
+// has at most 2^12 rows (every WHIR round after the first, whose rate grows),
+// the codeword is a set of independent coset transforms of that input and
+// also takes one pass.  Otherwise sizes
 // use the four-step split M = M1 * M2:
 //   pass 1: for each n2, a size-M1 DFT of x[M2 n1 + n2] (stride M2 rows),
 //           times w_M^(n2 k1), stored at row M2 k1 + n2;
@@ -51,88 +55,184 @@ __device__ __forceinline__ uint32_t brev(uint32_t i, int bits) {
 
 constexpr int MAX_TILE_LOG = 12;
 
-// o = blockIdx.x selects the sub-transform; in_row = o*a_in + i*b_in,
-// out_row = o*a_out + k*b_out.  tw_log > 0 multiplies output k by
-// w_{2^tw_log}^(o*k) (the four-step twiddle).
+// Shared-memory tile index of (row, column): rows are permuted inside each
+// aligned group of 4 by XOR with bits 3..4 of the row, so that the 4 rows a
+// warp touches at once (consecutive rows, or rows 8 apart in the last radix
+// steps) fall in different 8-bank groups.
 template <int C>
-__global__ void __launch_bounds__(512) dft_tile(const uint32_t *__restrict__ in,
-                                                uint32_t *__restrict__ out, int S, size_t width,
-                                                size_t rows_valid, size_t a_in, size_t b_in,
-                                                size_t a_out, size_t b_out, int tw_log) {
+__device__ __forceinline__ int sidx(int row, int c) {
+  return (row ^ ((row >> 3) & 3)) * C + c;
+}
+
+// One decimation-in-frequency step of R radix-2 stages done in registers:
+// the first stage has half-size H = 2^lh (blocks of 2H, never straddling two
+// sub-transforms), each task owns the 2^R elements j + t*q (q = H / 2^(R-1))
+// of one block and one column.
+// Butterfly at half h, position pos: (a, b) -> (a + b, (a - b) * w_{2h}^pos),
+// with w_{2h}^pos stored at twl[h + pos] (one contiguous table per level, so
+// consecutive positions read consecutive banks).
+template <int C, int R>
+__device__ __forceinline__ void dif_step(uint32_t *tile, const uint32_t *twl, int S_rows, int lh) {
+  constexpr int T = 1 << R;
+  const int lq = lh - (R - 1);
+  const int q = 1 << lq, H = 1 << lh;
+  const int tasks = (1 << (S_rows - R)) * C;  // all 2^S_rows tile rows, 2^R per task
+  for (int task = threadIdx.x; task < tasks; task += blockDim.x) {
+    const int c = task % C, rest = task / C;
+    const int j = rest & (q - 1), blk = rest >> lq;
+    const int base = blk * 2 * H + j;
+    uint32_t v[T];
+#pragma unroll
+    for (int t = 0; t < T; t++) v[t] = tile[sidx<C>(base + t * q, c)];
+#pragma unroll
+    for (int st = 0; st < R; st++) {
+      const int span = T >> (st + 1);
+      const int hh = H >> st;
+      if (hh == 1) {  // the last stage of the transform: every twiddle is 1
+#pragma unroll
+        for (int t = 0; t < T; t += 2) {
+          uint32_t a = v[t], b = v[t + 1];
+          v[t] = kb::add(a, b);
+          v[t + 1] = kb::sub(a, b);
+        }
+        continue;
+      }
+#pragma unroll
+      for (int t = 0; t < T; t++) {
+        if (t & span) continue;
+        const int pos = j + (t & (span - 1)) * q;
+        uint32_t a = v[t], b = v[t + span];
+        v[t] = kb::add(a, b);
+        // a - b + p < 2^32 needs no reduction before a Montgomery product
+        // with a canonical twiddle (the product stays below p 2^32)
+        v[t + span] = kb::mul(a - b + kb::P, twl[hh + pos]);
+      }
+    }
+#pragma unroll
+    for (int t = 0; t < T; t++) tile[sidx<C>(base + t * q, c)] = v[t];
+  }
+}
+
+// blockIdx.x selects the column slice (fastest, so the CTAs sharing a row's
+// 32-byte sectors run together and the row is fetched from DRAM once);
+// blockIdx.y selects 2^lg consecutive sub-transforms o, each of size 2^S,
+// held back to back in the tile.  in_row = o*a_in + i*b_in and out_row =
+// o*a_out + k*b_out.  pre_log > 0 multiplies input i by w_{2^pre_log}^(o*i)
+// (coset transforms of a zero-padded input); tw_log > 0 multiplies output k
+// by w_{2^tw_log}^(o*k) (the four-step twiddle).  The DIF leaves X[k] at
+// position bitrev(k) of its sub-transform.  Index arithmetic is 32-bit: the
+// launcher only uses this kernel when every word offset fits.
+template <int C>
+__global__ void __launch_bounds__(256) dft_tile(const uint32_t *__restrict__ in,
+                                                uint32_t *__restrict__ out, int S, int lg,
+                                                uint32_t width, uint32_t rows_valid,
+                                                uint32_t a_in, uint32_t b_in, uint32_t a_out,
+                                                uint32_t b_out, int pre_log, int tw_log) {
   extern __shared__ uint32_t sm[];
-  const int n = 1 << S;
+  const int n = 1 << S, rows = n << lg;
   uint32_t *tile = sm;
-  uint32_t *tw = sm + n * C;
-  const size_t o = blockIdx.x;
-  const size_t col0 = (size_t)blockIdx.y * C;
+  // aux holds, in turn: the per-row input twiddles, the DIF twiddles
+  // (aux[h + pos] = w_{2h}^pos for h = 1, 2, .., n/2), the per-row output twiddles
+  uint32_t *aux = sm + rows * C;
+  const uint32_t o0 = blockIdx.y << lg;
+  const uint32_t col0 = blockIdx.x * C;
   const int tid = threadIdx.x, nt = blockDim.x;
 
-  for (int j = tid; j < n / 2; j += nt) tw[j] = root_pow((uint32_t)j << (24 - S));
-  for (int e = tid; e < n * C; e += nt) {
-    int i = e / C, c = e % C;
-    size_t row = o * a_in + (size_t)i * b_in;
-    uint32_t v = row < rows_valid ? __ldg(in + row * width + col0 + c) : 0u;
-    tile[brev(i, S) * C + c] = v;
-  }
-  __syncthreads();
-  for (int s = 1; s <= S; s++) {
-    const int half = 1 << (s - 1);
-    for (int b = tid; b < (n / 2) * C; b += nt) {
-      int c = b % C, j = b / C;
-      int pos = j & (half - 1);
-      int i0 = ((j >> (s - 1)) << s) + pos, i1 = i0 + half;
-      uint32_t u = tile[i0 * C + c];
-      uint32_t v = kb::mul(tile[i1 * C + c], tw[pos << (S - s)]);
-      tile[i0 * C + c] = kb::add(u, v);
-      tile[i1 * C + c] = kb::sub(u, v);
+  if (pre_log) {
+    const uint32_t m = (1u << pre_log) - 1u;
+    for (int r = tid; r < rows; r += nt) {
+      uint32_t o = o0 + (uint32_t)(r >> S), i = (uint32_t)(r & (n - 1));
+      aux[r] = root_pow(((o * i) & m) << (24 - pre_log));
     }
     __syncthreads();
   }
-  for (int e = tid; e < n * C; e += nt) {
-    int k = e / C, c = e % C;
-    uint32_t v = tile[k * C + c];
-    if (tw_log) {
-      uint64_t ex = ((uint64_t)o * (uint64_t)k) & ((1ull << tw_log) - 1);
-      v = kb::mul(v, root_pow((uint32_t)(ex << (24 - tw_log))));
+  for (int e = tid; e < rows * C; e += nt) {
+    int r = e / C, c = e % C;
+    uint32_t o = o0 + (uint32_t)(r >> S), i = (uint32_t)(r & (n - 1));
+    uint32_t row = o * a_in + i * b_in;
+    uint32_t v = row < rows_valid ? __ldg(in + row * width + col0 + c) : 0u;
+    if (pre_log) v = kb::mul(v, aux[r]);
+    tile[sidx<C>(r, c)] = v;
+  }
+  __syncthreads();
+  for (int x = tid + 1; x < n; x += nt) {
+    int lh = 31 - __clz(x);
+    uint32_t pos = (uint32_t)(x - (1 << lh));
+    aux[x] = root_pow(pos << (24 - 1 - lh));  // w_{2^(lh+1)}^pos
+  }
+  __syncthreads();
+  int left = S, lh = S - 1;
+  while (left >= 3) {
+    dif_step<C, 3>(tile, aux, S + lg, lh);
+    __syncthreads();
+    left -= 3;
+    lh -= 3;
+  }
+  if (left == 2) {
+    dif_step<C, 2>(tile, aux, S + lg, lh);
+    __syncthreads();
+  } else if (left == 1) {
+    dif_step<C, 1>(tile, aux, S + lg, lh);
+    __syncthreads();
+  }
+  if (tw_log) {
+    const uint32_t m = (1u << tw_log) - 1u;
+    for (int r = tid; r < rows; r += nt) {
+      uint32_t o = o0 + (uint32_t)(r >> S), k = brev((uint32_t)(r & (n - 1)), S);
+      aux[r] = root_pow(((o * k) & m) << (24 - tw_log));
     }
-    out[(o * a_out + (size_t)k * b_out) * width + col0 + c] = v;
+    __syncthreads();
+  }
+  for (int e = tid; e < rows * C; e += nt) {
+    int r = e / C, c = e % C;
+    uint32_t v = tile[sidx<C>(r, c)];
+    uint32_t o = o0 + (uint32_t)(r >> S);
+    uint32_t k = brev((uint32_t)(r & (n - 1)), S);
+    if (tw_log) v = kb::mul(v, aux[r]);
+    out[(o * a_out + k * b_out) * width + col0 + c] = v;
   }
 }
 
 template <int C>
 static cudaError_t launch_tile(const uint32_t *in, uint32_t *out, int S, size_t width,
                                size_t rows_valid, size_t n_outer, size_t a_in, size_t b_in,
-                               size_t a_out, size_t b_out, int tw_log, cudaStream_t st) {
-  size_t smem = ((size_t)(1 << S) * C + (1 << S) / 2 + 1) * 4;
+                               size_t a_out, size_t b_out, int pre_log, int tw_log,
+                               cudaStream_t st) {
+  // pack small sub-transforms so that a CTA holds at least 2^11 rows
+  int lg = 0;
+  while (S + lg < 11 && ((size_t)2 << lg) <= n_outer) lg++;
+  size_t rows = (size_t)1 << (S + lg);
+  size_t smem = (rows * C + rows) * 4;  // tile + aux (rows >= 2^S)
   static bool attr_set = false;
   if (!attr_set) {
     cudaFuncSetAttribute(dft_tile<C>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                         ((1 << MAX_TILE_LOG) * C + (1 << MAX_TILE_LOG) / 2 + 1) * 4);
+                         ((1 << MAX_TILE_LOG) * C + (1 << MAX_TILE_LOG)) * 4);
     attr_set = true;
   }
-  int threads = (1 << S) * C / 2;
-  threads = threads < 32 ? 32 : (threads > 512 ? 512 : threads);
-  dim3 grid((unsigned)n_outer, (unsigned)(width / C));
-  dft_tile<C><<<grid, threads, smem, st>>>(in, out, S, width, rows_valid, a_in, b_in, a_out,
-                                           b_out, tw_log);
+  int threads = (int)(rows * C / 8);
+  threads = threads < 32 ? 32 : (threads > 256 ? 256 : threads);
+  dim3 grid((unsigned)(width / C), (unsigned)(n_outer >> lg));
+  dft_tile<C><<<grid, threads, smem, st>>>(in, out, S, lg, (uint32_t)width, (uint32_t)rows_valid,
+                                           (uint32_t)a_in, (uint32_t)b_in, (uint32_t)a_out,
+                                           (uint32_t)b_out, pre_log, tw_log);
   count_launches(1);
   return cudaGetLastError();
 }
 
 static cudaError_t tile_any(const uint32_t *in, uint32_t *out, int S, size_t width,
                             size_t rows_valid, size_t n_outer, size_t a_in, size_t b_in,
-                            size_t a_out, size_t b_out, int tw_log, cudaStream_t st) {
+                            size_t a_out, size_t b_out, int pre_log, int tw_log, cudaStream_t st) {
   if (width % 8 == 0)
     return launch_tile<8>(in, out, S, width, rows_valid, n_outer, a_in, b_in, a_out, b_out,
-                          tw_log, st);
+                          pre_log, tw_log, st);
   if (width % 4 == 0)
     return launch_tile<4>(in, out, S, width, rows_valid, n_outer, a_in, b_in, a_out, b_out,
-                          tw_log, st);
+                          pre_log, tw_log, st);
   if (width % 2 == 0)
     return launch_tile<2>(in, out, S, width, rows_valid, n_outer, a_in, b_in, a_out, b_out,
-                          tw_log, st);
+                          pre_log, tw_log, st);
   return launch_tile<1>(in, out, S, width, rows_valid, n_outer, a_in, b_in, a_out, b_out,
-                        tw_log, st);
+                        pre_log, tw_log, st);
 }
 
 cudaError_t dft_batch(const uint32_t *in, size_t h_in, size_t width, int log_h, uint32_t *out,
@@ -140,14 +240,25 @@ cudaError_t dft_batch(const uint32_t *in, size_t h_in, size_t width, int log_h, 
   if (log_h < 0 || log_h > 24 || width == 0) return cudaErrorInvalidValue;
   size_t h = (size_t)1 << log_h;
   if (h_in > h) return cudaErrorInvalidValue;
+  // the kernel indexes words with 32-bit arithmetic
+  if (width >= (1u << 16) || (h * width) >= ((size_t)1 << 32)) return cudaErrorInvalidValue;
   if (log_h <= 11)
-    return tile_any(in, out, log_h, width, h_in, 1, 0, 1, 0, 1, 0, st);
+    return tile_any(in, out, log_h, width, h_in, 1, 0, 1, 0, 1, 0, 0, st);
+  int L0 = 0;
+  while (((size_t)1 << L0) < h_in) L0++;
+  if (L0 <= 11 && log_h - L0 <= 15) {
+    // coset form: with N0 = 2^L0 >= h_in and M1 = 2^(log_h - L0),
+    // out[k1 + M1 k2] = sum_{n < N0} (x[n] w^(n k1)) w_{N0}^(n k2): M1 transforms
+    // of size N0 of the pre-twiddled input, one pass, no scratch
+    size_t M1 = h >> L0;
+    return tile_any(in, out, L0, width, h_in, M1, 0, 1, 1, M1, log_h, 0, st);
+  }
   int L1 = (log_h + 1) / 2, L2 = log_h - L1;
   if (L1 > MAX_TILE_LOG) return cudaErrorInvalidValue;
   size_t M1 = (size_t)1 << L1, M2 = (size_t)1 << L2;
-  cudaError_t e = tile_any(in, scratch, L1, width, h_in, M2, 1, M2, 1, M2, log_h, st);
+  cudaError_t e = tile_any(in, scratch, L1, width, h_in, M2, 1, M2, 1, M2, 0, log_h, st);
   if (e != cudaSuccess) return e;
-  return tile_any(scratch, out, L2, width, h, M1, M2, 1, 1, M1, 0, st);
+  return tile_any(scratch, out, L2, width, h, M1, M2, 1, 1, M1, 0, 0, st);
 }
 
 }  // namespace gpu

@@ -9,6 +9,8 @@
 // crates/whir/src/test.rs:188-189): light MDS, 4 external rounds, rounds_p
 // internal rounds (S-box on lane 0, then 1 1^T + diag), 4 external rounds.
 #pragma once
+#include <utility>
+
 #include "kb.cuh"
 
 namespace whir {
@@ -65,6 +67,63 @@ __device__ __forceinline__ void p2_mds_light(uint32_t (&s)[W]) {
   for (int i = 0; i < W; i++) s[i] = kb::add(s[i], sum[i & 3]);
 }
 
+// Internal diagonals of p3-koala-bear's Poseidon2 as sign * num / 2^log_den
+// (the same values poseidon2_host.cpp uploads for the generic path).  Every
+// entry is 1, 2, 3, 4 or 2^-e up to sign, so the product needs no multiplier.
+struct DiagEntry {
+  int sign, num, log_den;
+};
+__host__ __device__ constexpr DiagEntry diag_entry16(int i) {
+  constexpr DiagEntry v[16] = {{-1, 2, 0}, {1, 1, 0},  {1, 2, 0},  {1, 1, 1},
+                               {1, 3, 0},  {1, 4, 0},  {-1, 1, 1}, {-1, 3, 0},
+                               {-1, 4, 0}, {1, 1, 8},  {1, 1, 3},  {1, 1, 24},
+                               {-1, 1, 8}, {-1, 1, 3}, {-1, 1, 4}, {-1, 1, 24}};
+  return v[i];
+}
+__host__ __device__ constexpr DiagEntry diag_entry24(int i) {
+  constexpr DiagEntry v[24] = {{-1, 2, 0}, {1, 1, 0},  {1, 2, 0},  {1, 1, 1},  {1, 3, 0},
+                               {1, 4, 0},  {-1, 1, 1}, {-1, 3, 0}, {-1, 4, 0}, {1, 1, 8},
+                               {1, 1, 2},  {1, 1, 3},  {1, 1, 4},  {1, 1, 5},  {1, 1, 6},
+                               {1, 1, 24}, {-1, 1, 8}, {-1, 1, 3}, {-1, 1, 4}, {-1, 1, 5},
+                               {-1, 1, 6}, {-1, 1, 7}, {-1, 1, 9}, {-1, 1, 24}};
+  return v[i];
+}
+
+// x * num / 2^log_den mod p on a canonical word (Montgomery form is linear,
+// so scaling the word scales the element).  Division by 2^e (e <= 24): with
+// m = -x mod 2^e, x + m p is divisible by 2^e because p = 127 * 2^24 + 1, and
+// (x + m p) / 2^e = (x + m) / 2^e + m * 127 * 2^(24-e) < p.
+template <int NUM, int LOGD>
+__device__ __forceinline__ uint32_t mul_small(uint32_t x) {
+  using namespace kb;
+  if constexpr (LOGD > 0) {
+    static_assert(NUM == 1 && LOGD <= 24, "only 2^-e");
+    uint32_t m = (0u - x) & ((1u << LOGD) - 1u);
+    return ((x + m) >> LOGD) + m * (127u << (24 - LOGD));
+  } else if constexpr (NUM == 1) {
+    return x;
+  } else if constexpr (NUM == 2) {
+    return dbl(x);
+  } else if constexpr (NUM == 3) {
+    return add(dbl(x), x);
+  } else {
+    static_assert(NUM == 4, "diag entry");
+    return dbl(dbl(x));
+  }
+}
+
+template <int W, int I>
+__device__ __forceinline__ void p2_internal_lane(uint32_t (&s)[W], uint32_t sum) {
+  constexpr DiagEntry d = W == 16 ? diag_entry16(I) : diag_entry24(I);
+  uint32_t y = mul_small<d.num, d.log_den>(s[I]);
+  s[I] = d.sign > 0 ? kb::add(sum, y) : kb::sub(sum, y);
+}
+template <int W, int... I>
+__device__ __forceinline__ void p2_internal_all(uint32_t (&s)[W], uint32_t sum,
+                                                std::integer_sequence<int, I...>) {
+  (p2_internal_lane<W, I>(s, sum), ...);
+}
+
 template <int W>
 __device__ __forceinline__ void p2_permute(uint32_t (&s)[W]) {
   using namespace kb;
@@ -79,14 +138,18 @@ __device__ __forceinline__ void p2_permute(uint32_t (&s)[W]) {
     for (int i = 0; i < W; i++) s[i] = cube(add(s[i], C[r * W + i]));
     p2_mds_light<W>(s);
   }
+  (void)D;  // the diagonal is applied by shifts and adds (mul_small)
 #pragma unroll
   for (int r = 0; r < RP; r++) {
     s[0] = cube(add(s[0], I[r]));
-    uint32_t sum = s[0];
+    // sum of the W canonical lanes in 64 bits (< W p < 2^36), then one
+    // reduction: 2^31 = 2^24 - 1 (mod p) folds the high part, leaving < 2p
+    uint64_t wide = 0;
 #pragma unroll
-    for (int i = 1; i < W; i++) sum = add(sum, s[i]);
-#pragma unroll
-    for (int i = 0; i < W; i++) s[i] = add(sum, mul(D[i], s[i]));
+    for (int i = 0; i < W; i++) wide += s[i];
+    uint32_t folded = (uint32_t)(wide & 0x7fffffffu) + (uint32_t)(wide >> 31) * 0x00ffffffu;
+    uint32_t sum = kb::umin(folded, folded - P);
+    p2_internal_all<W>(s, sum, std::make_integer_sequence<int, W>{});
   }
 #pragma unroll
   for (int r = 4; r < 8; r++) {

@@ -5,6 +5,7 @@
 #include <string.h>
 
 #include <algorithm>
+#include <chrono>
 #include <functional>
 #include <map>
 #include <unordered_map>
@@ -109,7 +110,16 @@ void *Context::pinned(size_t bytes) {
   }
   return pinned_;
 }
-void Context::sync() { cuda_check(cudaStreamSynchronize(stream_), "stream sync"); }
+void Context::sync() {
+  if (!prof_) {
+    cuda_check(cudaStreamSynchronize(stream_), "stream sync");
+    return;
+  }
+  auto t0 = std::chrono::steady_clock::now();
+  cuda_check(cudaStreamSynchronize(stream_), "stream sync");
+  acc_ms_[K_SYNC] += std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t0).count();
+  acc_n_[K_SYNC] += 1;
+}
 
 cudaEvent_t Context::take_event() {
   if (!free_events_.empty()) {
@@ -137,7 +147,7 @@ void Context::prof_end(int klass, double bytes) {
 }
 void Context::prof_read(int klass, double *ms, long *launches, double *bytes) {
   if (!evs_.empty()) {
-    sync();
+    cuda_check(cudaStreamSynchronize(stream_), "stream sync");
     for (auto &e : evs_) {
       float t = 0;
       cudaEventElapsedTime(&t, e.a, e.b);
@@ -273,6 +283,28 @@ struct VirtClaim {
   std::vector<E4> acc;
 };
 
+// page-locked host memory owned by one object
+class PinnedBuffer {
+ public:
+  ~PinnedBuffer() {
+    if (p_) cudaFreeHost(p_);
+  }
+  void reserve(size_t bytes) {
+    if (bytes <= bytes_) return;
+    if (p_) cudaFreeHost(p_);
+    p_ = nullptr;
+    bytes_ = 0;
+    cuda_check(cudaMallocHost(&p_, bytes), "cudaMallocHost");
+    bytes_ = bytes;
+  }
+  uint8_t *data() const { return static_cast<uint8_t *>(p_); }
+  size_t bytes() const { return bytes_; }
+
+ private:
+  void *p_ = nullptr;
+  size_t bytes_ = 0;
+};
+
 struct LayEntry {
   int nbits;
   uint8_t bits[32];
@@ -293,9 +325,20 @@ struct Prover::Impl {
   std::vector<size_t> poly_off;  // word offset of each poly inside the stacked poly
   // device memory
   DeviceBuffer stacked, cw0, tree0, scratch, cw[2], trees[2], sp[2], sw[2], eqbuf, acc, small,
-      gather;
+      gather, ptsbuf;
   DeviceTree t0, tr[2];
   int cur_tree = -1;  // index into tr of the latest round commitment
+  std::vector<std::vector<uint32_t>> svo_eq;  // per round: eq tables of the {0,1,2} grid
+  // pinned staging: `args` holds host->device arguments and is reused after
+  // every sync; `defer` receives opening rows and row evaluations whose
+  // device->host copies complete at a later sync (hints are filled into the
+  // transcript at the end of the proof)
+  PinnedBuffer args_pin, defer_pin;
+  size_t args_off = 0, defer_off = 0;
+  struct PendingHint {
+    size_t ts_off, pin_off, words;
+  };
+  std::vector<PendingHint> pending_hints;
   // claims
   std::vector<SvoClaim> claims;
   std::vector<VirtClaim> virt;
@@ -314,6 +357,64 @@ struct Prover::Impl {
     for (int r = 0; r < ks; r++) s += 2 * ipow3(r);
     return s;
   }
+
+  void sync() {
+    ctx->sync();
+    args_off = 0;
+  }
+  // pinned argument space for host->device copies issued before the next sync
+  uint8_t *args_alloc(size_t bytes) {
+    bytes = (bytes + 15) & ~(size_t)15;
+    if (args_off + bytes > args_pin.bytes()) {
+      sync();
+      if (bytes > args_pin.bytes()) args_pin.reserve(std::max(bytes, (size_t)1 << 20));
+    }
+    uint8_t *p = args_pin.data() + args_off;
+    args_off += bytes;
+    return p;
+  }
+  // copy host bytes to `dst` (device) through the argument space
+  void upload(void *dst, const void *src, size_t bytes) {
+    uint8_t *h = args_alloc(bytes);
+    memcpy(h, src, bytes);
+    cuda_check(copy_async(*ctx, dst, h, bytes, cudaMemcpyHostToDevice), "h2d");
+  }
+  // split eq tables of n points (k variables each, lo over the first s) with
+  // per-table scales, written back to back at `out` (one upload, one launch)
+  void make_eq_tables(const std::vector<const E4 *> &pts, int k, const std::vector<E4> &scales,
+                      int s, E4 *out) {
+    size_t n = pts.size();
+    if (n == 0) return;
+    std::vector<E4> host(n * k + n);
+    for (size_t t = 0; t < n; t++) {
+      std::copy(pts[t], pts[t] + k, host.begin() + t * k);
+      host[n * k + t] = scales[t];
+    }
+    size_t bytes = host.size() * sizeof(E4);
+    if (bytes > ptsbuf.bytes()) ptsbuf.reserve(2 * bytes);
+    upload(ptsbuf.as<E4>(), host.data(), bytes);
+    cuda_check(gpu::eq_tables(ptsbuf.as<E4>(), ptsbuf.as<E4>() + n * k, (int)n, k, s, out, st()),
+               "eq_tables");
+  }
+  void fill_pending_hints(Transcript &ts) {
+    for (auto &h : pending_hints)
+      ts.hint_fill(h.ts_off, reinterpret_cast<const uint32_t *>(defer_pin.data()) + h.pin_off, h.words);
+    pending_hints.clear();
+    defer_off = 0;
+  }
+  // pinned space (in words) for device->host results read after a later sync
+  size_t defer_alloc(size_t words, Transcript &ts) {
+    words = (words + 3) & ~(size_t)3;
+    if (4 * (defer_off + words) > defer_pin.bytes()) {
+      sync();  // everything pending has landed: emit it and start over
+      fill_pending_hints(ts);
+      if (4 * words > defer_pin.bytes()) defer_pin.reserve(std::max(4 * words, (size_t)16 << 20));
+    }
+    size_t off = defer_off;
+    defer_off += words;
+    return off;
+  }
+  uint32_t *defer_ptr(size_t off) { return reinterpret_cast<uint32_t *>(defer_pin.data()) + off; }
 
   // ---- layout (ProverStack::layout, prover.rs:92-124) ----
   void make_layout() {
@@ -378,6 +479,9 @@ struct Prover::Impl {
       sw[i].reserve(sizeof(E4) * n);
     }
     eqbuf.reserve(sizeof(E4) * (size_t)64 * 8192);
+    args_pin.reserve((size_t)1 << 20);
+    ptsbuf.reserve(64 << 10);
+    defer_pin.reserve((size_t)16 << 20);
     acc.reserve(8 * 4096);
     small.reserve(1 << 20);
     gather.reserve((size_t)4 * 4096 * (((size_t)4 << f) + 8 * 32));
@@ -397,12 +501,9 @@ struct Prover::Impl {
     c.k = kp;
     c.point.assign(point, point + kp);
     int nz = kp - ks;
-    gpu::Point z;
-    z.k = nz;
-    for (int i = 0; i < nz; i++) z.z[i] = point[ks + i];
     int s_lo = std::min(10, nz);
     E4 *lo = eqbuf.as<E4>(), *hi = lo + ((size_t)1 << s_lo);
-    cuda_check(gpu::eq_split(z, s_lo, e_one(), lo, hi, st()), "eq_split");
+    make_eq_tables({point + ks}, nz, {e_one()}, s_lo, lo);
     size_t na = (size_t)4 << ks;
     unsigned long long *a = acc.as<unsigned long long>();
     cuda_check(cudaMemsetAsync(a, 0, 8 * na, st()), "memset");
@@ -411,7 +512,7 @@ struct Prover::Impl {
     ctx->prof_end(Context::K_SUMCHECK, 4.0 * (double)((size_t)1 << kp));
     unsigned long long *h = (unsigned long long *)ctx->pinned(8 * na);
     cuda_check(copy_async(*ctx, h, a, 8 * na, cudaMemcpyDeviceToHost), "d2h");
-    ctx->sync();
+    sync();
     size_t n = (size_t)1 << ks;
     c.compressed.resize(n);
     for (size_t j = 0; j < n; j++) c.compressed[j] = reduce_acc(h + 4 * j);
@@ -435,30 +536,70 @@ struct Prover::Impl {
 
   // Svo::calculate_accumulators for one claim weighted by `w` (svo.rs:225-278);
   // accumulators are linear in the weighted partial evals, so summing per
-  // claim equals the reference's per-point grouping.
-  void accumulate(std::vector<E4> &accv, const SvoClaim &c, const E4 &w) const {
+  // claim equals the reference's per-point grouping.  For each round r and
+  // grid point u in {0,1,2}^r x {0 or 2}: acc += eq(u, svo[..r+1]) * <w pe_r, eq_u>.
+  // The eq tables eq_u have base-field entries and do not depend on the claim
+  // (Svo::new, svo.rs:158-222), so they are built once per prover (svo_eq).
+  void build_svo_tables() {
+    if (!svo_eq.empty()) return;
+    svo_eq.resize(ks);
+    const uint32_t vals[3][2] = {{ONE, 0}, {0, ONE}, {neg(ONE), dbl(ONE)}};  // (1-u, u)
+    for (int r = 0; r < ks; r++) {
+      int l = r + 1;
+      size_t n = ipow3(r), na = (size_t)1 << l;
+      std::vector<uint32_t> &tab = svo_eq[r];
+      tab.assign(2 * n * na, 0);
+      for (int which = 0; which < 2; which++)
+        for (size_t t = 0; t < n; t++) {
+          int dig[16];
+          size_t tt = t;
+          for (int i = 0; i < r; i++) {
+            dig[i] = (int)(tt % 3);
+            tt /= 3;
+          }
+          dig[r] = which ? 2 : 0;
+          uint32_t *e = tab.data() + (which * n + t) * na;
+          for (size_t a = 0; a < na; a++) {
+            uint32_t v = ONE;
+            for (int i = 0; i < l; i++) v = mul(v, vals[dig[i]][(a >> i) & 1]);
+            e[a] = v;
+          }
+        }
+    }
+  }
+  void accumulate(std::vector<E4> &accv, const SvoClaim &c, const E4 &w) {
+    build_svo_tables();
     size_t off = 0;
-    std::vector<E4> eq, u;
+    std::vector<E4> wpe, fac, nxt;
     for (int r = 0; r < ks; r++) {
       int l = r + 1;
       size_t n = ipow3(r), na = (size_t)1 << l;
       const E4 *pe = c.partial.data() + partial_off(l);
-      eq.resize(na);
-      u.resize(l);
-      std::vector<E4> wpe(na);
+      wpe.resize(na);
       for (size_t a = 0; a < na; a++) wpe[a] = e_mul(w, pe[a]);
+      // eval_eq_xy(u, y) = prod_i f(u_i, y_i) with f(0,y) = 1-y, f(1,y) = y,
+      // f(2,y) = 3y-1; the 3^r prefix products in base-3 digit order
+      fac.assign(1, e_one());
+      for (int i = 0; i < r; i++) {
+        const E4 &y = c.point[i];
+        E4 f3[3] = {e_sub(e_one(), y), y, e_sub(e_add(e_dbl(y), y), e_one())};
+        nxt.resize(fac.size() * 3);
+        for (int d = 0; d < 3; d++)
+          for (size_t t = 0; t < fac.size(); t++) nxt[d * fac.size() + t] = e_mul(fac[t], f3[d]);
+        fac.swap(nxt);
+      }
+      const E4 &yl = c.point[r];
+      E4 last[2] = {e_sub(e_one(), yl), e_sub(e_add(e_dbl(yl), yl), e_one())};
+      const uint32_t *tab = svo_eq[r].data();
       for (int which = 0; which < 2; which++)
         for (size_t t = 0; t < n; t++) {
-          size_t tt = t;
-          for (int i = 0; i < r; i++) {
-            u[i] = e_from(from_canonical((uint32_t)(tt % 3)));
-            tt /= 3;
-          }
-          u[r] = which ? e_dbl(e_one()) : e_zero();
-          eq_host(u.data(), l, e_one(), eq.data());
-          E4 dot = e_zero();
-          for (size_t a = 0; a < na; a++) dot = e_add(dot, e_mul(wpe[a], eq[a]));
-          E4 v = e_mul(eval_eq_xy(u.data(), c.point.data(), l), dot);
+          const uint32_t *eq = tab + (which * n + t) * na;
+          uint64_t s4[4] = {0, 0, 0, 0};
+          for (size_t a = 0; a < na; a++)
+            for (int q = 0; q < 4; q++) s4[q] += (uint64_t)mul(wpe[a].c[q], eq[a]);
+          E4 dot;
+          for (int q = 0; q < 4; q++) dot.c[q] = (uint32_t)(s4[q] % kb::P);
+          E4 v = e_mul(e_mul(fac[t], last[which]), dot);
           accv[off + which * n + t] = e_add(accv[off + which * n + t], v);
         }
       off += 2 * n;
@@ -505,7 +646,7 @@ struct Prover::Impl {
     unsigned long long *h = (unsigned long long *)ctx->pinned(64);
     cuda_check(copy_async(*ctx, h, acc.as<unsigned long long>(), 64, cudaMemcpyDeviceToHost),
                "d2h");
-    ctx->sync();
+    sync();
     *c0 = reduce_acc(h);
     *c2 = reduce_acc(h + 4);
   }
@@ -562,29 +703,27 @@ struct Prover::Impl {
     size_t per = ((size_t)1 << s) + ((size_t)1 << (kt - s));
     if (per * pts.size() * sizeof(E4) > eqbuf.bytes())
       eqbuf.reserve(per * pts.size() * sizeof(E4));
-    E4 *tab = eqbuf.as<E4>();
-    for (size_t t = 0; t < pts.size(); t++) {
-      gpu::Point z;
-      z.k = kt;
-      for (int i = 0; i < kt; i++) z.z[i] = pts[t][i];
-      cuda_check(gpu::eq_split(z, s, scales[t], tab + t * per, tab + t * per + ((size_t)1 << s), st()),
-                 "eq_split");
-    }
-    cuda_check(gpu::add_eq(w, kt, tab, (int)pts.size(), st()), "add_eq");
+    std::vector<const E4 *> pp;
+    for (auto &q : pts) pp.push_back(q.data());
+    make_eq_tables(pp, kt, scales, s, eqbuf.as<E4>());
+    cuda_check(gpu::add_eq(w, kt, eqbuf.as<E4>(), (int)pts.size(), st()), "add_eq");
   }
 
+  // w += sum_t scales_t var_t^i; arguments go through the pinned argument
+  // space, so no sync is needed here
   void add_pows(const std::vector<uint32_t> &vars, const std::vector<E4> &scales) {
     if (vars.empty()) return;
     size_t bytes = vars.size() * 4 + scales.size() * 16;
-    uint8_t *h = (uint8_t *)ctx->pinned(bytes + 64);
-    memcpy(h, scales.data(), scales.size() * 16);
-    memcpy(h + scales.size() * 16, vars.data(), vars.size() * 4);
-    if (bytes > small.bytes()) small.reserve(bytes);
-    cuda_check(copy_async(*ctx, small.as<uint8_t>(), h, bytes, cudaMemcpyHostToDevice), "h2d");
+    std::vector<uint8_t> h(bytes);
+    memcpy(h.data(), scales.data(), scales.size() * 16);
+    memcpy(h.data() + scales.size() * 16, vars.data(), vars.size() * 4);
+    if (bytes > small.bytes()) small.reserve(2 * bytes);
+    upload(small.as<uint8_t>(), h.data(), bytes);
+    size_t tw = gpu::add_pows_scratch_words(kc, (int)vars.size());
+    if (4 * tw > eqbuf.bytes()) eqbuf.reserve(4 * tw);
     cuda_check(gpu::add_pows(W(), kc, (const uint32_t *)(small.as<uint8_t>() + scales.size() * 16),
-                             small.as<E4>(), (int)vars.size(), st()),
+                             small.as<E4>(), (int)vars.size(), eqbuf.as<uint32_t>(), st()),
                "add_pows");
-    ctx->sync();  // the staging area is reused right after
   }
 
   // ---- new_prover (prover.rs:280-354) incl. expression (185-229) ----
@@ -672,30 +811,30 @@ struct Prover::Impl {
   }
 
   // ---- queries (MerkleTree::query, poseidon_packed.rs:145-233) ----
-  // writes leaf + sibling hints for each index; returns the gathered leaves
-  std::vector<uint32_t> query(Transcript &ts, const DeviceTree &t, const std::vector<size_t> &idx) {
+  // Reserves the leaf + sibling hints of each index in the transcript and
+  // starts their gather; the rows land in the deferred pinned area (word
+  // offset returned, `per` words per index) and are readable after the next
+  // sync; the hint bytes are filled in at the end of the proof.
+  size_t query_async(Transcript &ts, const DeviceTree &t, const std::vector<size_t> &idx) {
     int n = (int)idx.size();
-    std::vector<uint32_t> rows;
-    if (n == 0) return rows;
+    if (n == 0) return 0;
     size_t per = (size_t)t.row_len + 8 * (size_t)t.log_h;
-    uint32_t *hidx = (uint32_t *)ctx->pinned(4 * n + 4 * per * n);
+    size_t need = 4 * (size_t)n + 4 * per * n + 16;
+    if (need > gather.bytes()) {
+      sync();  // an earlier gather may still be in flight
+      gather.reserve(2 * need);
+    }
+    std::vector<uint32_t> hidx(n);
     for (int i = 0; i < n; i++) hidx[i] = (uint32_t)idx[i];
-    size_t need = 4 * (size_t)n + 4 * per * n;
-    if (need > gather.bytes()) gather.reserve(need);
-    uint32_t *didx = gather.as<uint32_t>(), *dout = didx + n;
-    cuda_check(copy_async(*ctx, didx, hidx, 4 * n, cudaMemcpyHostToDevice), "h2d");
+    uint32_t *didx = gather.as<uint32_t>(), *dout = didx + ((n + 3) & ~3);
+    upload(didx, hidx.data(), 4 * (size_t)n);
     cuda_check(gpu::gather_openings(t.rows, t.row_len, t.nodes, t.log_h, didx, n, dout, st()),
                "gather");
-    uint32_t *hout = hidx + n;
-    cuda_check(copy_async(*ctx, hout, dout, 4 * per * n, cudaMemcpyDeviceToHost), "d2h");
-    ctx->sync();
-    rows.resize((size_t)t.row_len * n);
-    for (int i = 0; i < n; i++) {
-      const uint32_t *q = hout + per * i;
-      ts.hint_words(q, per);
-      memcpy(rows.data() + (size_t)t.row_len * i, q, 4 * (size_t)t.row_len);
-    }
-    return rows;
+    size_t off = defer_alloc(per * n, ts);
+    cuda_check(copy_async(*ctx, defer_ptr(off), dout, 4 * per * n, cudaMemcpyDeviceToHost), "d2h");
+    for (int i = 0; i < n; i++)
+      pending_hints.push_back(PendingHint{ts.hint_reserve(per), off + per * i, per});
+    return off;
   }
 
   std::vector<size_t> stir_indexes(Transcript &ts, int bits, int n) {  // whir.rs:64-77
@@ -707,13 +846,14 @@ struct Prover::Impl {
   }
 
   // ---- fold (prover.rs:378-397) ----
+  // The pow-claim evaluations come from opening rows still in flight
+  // (rows_off in the deferred area); they only enter `sum`, which is first
+  // needed after the first round's coefficients are read back, so they are
+  // evaluated after that sync.
   std::vector<E4> fold(Transcript &ts, const std::vector<std::vector<E4>> &eq_pts,
                        const std::vector<E4> &eq_evals, const std::vector<uint32_t> &vars,
-                       const std::vector<E4> &pow_evals) {
+                       size_t rows_off, size_t per, int row_len, const std::vector<E4> &point) {
     alpha = ts.draw_ext();
-    std::vector<E4> ev(eq_evals);
-    ev.insert(ev.end(), pow_evals.begin(), pow_evals.end());
-    sum = e_add(sum, horner(ev.data(), ev.size(), alpha));
     flush();
     std::vector<E4> sc;
     E4 a = e_one();
@@ -730,10 +870,24 @@ struct Prover::Impl {
     add_pows(vars, ps);
     std::vector<E4> out;
     for (int i = 0; i < p.folding; i++) {
-      E4 r = round(ts);
+      E4 c0, c2;
+      coeffs(&c0, &c2);
+      if (i == 0) {  // combine_claims' sum update (combine.rs:49-53)
+        std::vector<E4> ev(eq_evals);
+        for (size_t q = 0; q < vars.size(); q++)
+          ev.push_back(eval_ext_small(reinterpret_cast<const E4 *>(defer_ptr(rows_off + per * q)),
+                                      p.folding, point.data()));
+        sum = e_add(sum, horner(ev.data(), ev.size(), alpha));
+      }
+      ts.write_ext(c0);
+      ts.write_ext(c2);
+      E4 r = ts.draw_ext();
+      defer_fold(r);
+      sum = extrapolate012(c0, e_sub(sum, c0), c2, r);
       out.push_back(r);
       rs.push_back(r);
     }
+    (void)row_len;
     return out;
   }
 
@@ -758,7 +912,8 @@ struct Prover::Impl {
       scales[i] = a;
       a = e_mul(a, alpha);
     }
-    // recursive indexes (prover.rs:483-495) and their row evals at eq(rs)
+    // recursive indexes (prover.rs:483-495) and their row evals at eq(rs),
+    // computed on the device and read after the first round's sync
     std::vector<size_t> ri;
     for (int round = 0; round < d; round++) {
       size_t stride = (size_t)1 << (k_data - round - 1), count = (size_t)1 << (round + 1);
@@ -770,39 +925,47 @@ struct Prover::Impl {
     std::sort(ri.begin(), ri.end());
     ri.erase(std::unique(ri.begin(), ri.end()), ri.end());
     std::unordered_map<size_t, E4> evals;
-    if (!ri.empty()) {
-      size_t m = ri.size();
-      uint32_t *h = (uint32_t *)ctx->pinned(4 * m + 16 * m);
+    size_t m = ri.size(), ev_off = 0;
+    if (m) {
+      size_t need = 4 * m + 16 * m + 64;
+      if (need > gather.bytes()) {
+        sync();
+        gather.reserve(2 * need);
+      }
+      std::vector<uint32_t> h(m);
       for (size_t i = 0; i < m; i++) h[i] = (uint32_t)ri[i];
-      size_t need = 4 * m + 16 * m;
-      if (need > gather.bytes()) gather.reserve(need);
       uint32_t *didx = gather.as<uint32_t>();
       E4 *dout = reinterpret_cast<E4 *>(didx + ((m + 3) & ~(size_t)3));
-      cuda_check(copy_async(*ctx, didx, h, 4 * m, cudaMemcpyHostToDevice), "h2d");
+      upload(didx, h.data(), 4 * m);
       gpu::Point rsp;
       rsp.k = (int)rs.size();
       for (size_t i = 0; i < rs.size(); i++) rsp.z[i] = rs[i];
       cuda_check(gpu::row_evals(t0.rows, t0.row_len, didx, (int)m, rsp, dout, st()), "row_evals");
-      E4 *hout = reinterpret_cast<E4 *>(h + ((m + 3) & ~(size_t)3));
-      cuda_check(copy_async(*ctx, hout, dout, 16 * m, cudaMemcpyDeviceToHost), "d2h");
-      ctx->sync();
-      evals.reserve(m * 2);
-      for (size_t i = 0; i < m; i++) evals[ri[i]] = hout[i];
+      ev_off = defer_alloc(4 * m, ts);
+      cuda_check(copy_async(*ctx, defer_ptr(ev_off), dout, 16 * m, cudaMemcpyDeviceToHost), "d2h");
     }
-    for (int i = 0; i < n; i++) sum = e_add(sum, e_mul(scales[i], evals.at(idx[i])));
     uint32_t omega = two_adic_generator(k_data);
+    // w^-e for e < 2^k_data as lo[e & 2047] * hi[e >> 11] (w = two_adic_generator(k_data));
+    // the level-r generator of g is w^(2^(r-1)), so its inverse powers are w^-(e 2^(r-1))
+    uint32_t winv = inv(omega);
+    std::vector<uint32_t> ilo(2048), ihi((((size_t)1 << k_data) >> 11) + 1);
+    ilo[0] = ONE;
+    for (size_t i = 1; i < ilo.size(); i++) ilo[i] = mul(ilo[i - 1], winv);
+    uint32_t w2048 = mul(ilo[2047], winv);
+    ihi[0] = ONE;
+    for (size_t i = 1; i < ihi.size(); i++) ihi[i] = mul(ihi[i - 1], w2048);
+    const size_t emask = ((size_t)1 << k_data) - 1;
+    auto winv_pow = [&](size_t e) { e &= emask; return mul(ilo[e & 2047], ihi[e >> 11]); };
     size_t mid0 = ((size_t)1 << k_data) / 2;
     std::vector<uint32_t> ws(n), tw(n);
     for (int i = 0; i < n; i++) {
       ws[i] = kb::pow(omega, idx[i]);
-      tw[i] = inv(kb::pow(omega, idx[i] & (mid0 - 1)));
+      tw[i] = winv_pow(idx[i] & (mid0 - 1));
     }
     uint32_t two_inv = inv(from_canonical(2));
     std::vector<E4> rc;  // rs of this call
     // g (prover.rs:437-461), memoised per (round, index)
     std::unordered_map<uint64_t, E4> memo;
-    std::vector<uint32_t> omega_inv(d + 1);
-    for (int r = 1; r <= d; r++) omega_inv[r] = inv(two_adic_generator(k_data - (r - 1)));
     std::function<E4(int, size_t)> g = [&](int round, size_t index) -> E4 {
       if (round == 0) return evals.at(index);
       uint64_t key = ((uint64_t)round << 48) | index;
@@ -812,7 +975,7 @@ struct Prover::Impl {
       size_t i_lo = index & (mid - 1), i_hi = i_lo + mid;
       E4 glo = g(round - 1, i_lo), ghi = g(round - 1, i_hi);
       E4 even = e_scale(e_add(glo, ghi), two_inv);
-      E4 odd = e_scale(e_scale(e_sub(glo, ghi), two_inv), kb::pow(omega_inv[round], i_lo));
+      E4 odd = e_scale(e_scale(e_sub(glo, ghi), two_inv), winv_pow(i_lo << (round - 1)));
       E4 v = e_add(even, e_mul(rc[round - 1], e_sub(odd, even)));
       memo[key] = v;
       return v;
@@ -820,6 +983,12 @@ struct Prover::Impl {
     for (int round = 0; round < d; round++) {
       E4 c0, c2;
       coeffs(&c0, &c2);
+      if (round == 0) {  // the row evals have landed (prover.rs:426-435)
+        const E4 *hv = reinterpret_cast<const E4 *>(defer_ptr(ev_off));
+        evals.reserve(m * 2);
+        for (size_t i = 0; i < m; i++) evals[ri[i]] = hv[i];
+        for (int i = 0; i < n; i++) sum = e_add(sum, e_mul(scales[i], evals.at(idx[i])));
+      }
       size_t l = (size_t)1 << (k_data - round), mid = l / 2;
       for (int i = 0; i < n; i++) {
         size_t i_lo = idx[i] & (mid - 1), i_hi = i_lo + mid;
@@ -852,6 +1021,8 @@ struct Prover::Impl {
 
   // ---- Whir::open (whir.rs:168-359) ----
   void open(Transcript &ts) {
+    pending_hints.clear();
+    defer_off = 0;
     int n_ood = n_ood_queries(p.soundness, p.security_level, p.k, p.rate, EXT_BITS);
     for (int i = 0; i < n_ood; i++) write_virtual_eval(ts);
     new_prover(ts);
@@ -883,20 +1054,16 @@ struct Prover::Impl {
       std::vector<size_t> idx = stir_indexes(ts, kfd, n_s);
       std::vector<E4> rnew;
       if (round == 0) {
-        query(ts, t0, idx);
+        query_async(ts, t0, idx);
         rnew = fold_with_code(ts, pts, evs, idx);
       } else {
         const DeviceTree &prev = tr[cur_tree];
-        std::vector<uint32_t> rows = query(ts, prev, idx);
+        size_t rows_off = query_async(ts, prev, idx);
+        size_t per = (size_t)prev.row_len + 8 * (size_t)prev.log_h;
         uint32_t omega = two_adic_generator(kfd);
         std::vector<uint32_t> vars(idx.size());
-        std::vector<E4> pev(idx.size());
-        for (size_t i = 0; i < idx.size(); i++) {
-          vars[i] = kb::pow(omega, idx[i]);
-          pev[i] = eval_ext_small(reinterpret_cast<const E4 *>(rows.data() + prev.row_len * i),
-                                  p.folding, round_point.data());
-        }
-        rnew = fold(ts, pts, evs, vars, pev);
+        for (size_t i = 0; i < idx.size(); i++) vars[i] = kb::pow(omega, idx[i]);
+        rnew = fold(ts, pts, evs, vars, rows_off, per, prev.row_len, round_point);
       }
       round_point = rnew;
       cur_tree = slot;
@@ -905,14 +1072,16 @@ struct Prover::Impl {
     size_t nf = (size_t)1 << kc;
     E4 *hf = (E4 *)ctx->pinned(16 * nf);
     cuda_check(copy_async(*ctx, hf, P(), 16 * nf, cudaMemcpyDeviceToHost), "d2h");
-    ctx->sync();
+    sync();
     std::vector<E4> fp(hf, hf + nf);
     for (auto &e : fp) ts.write_ext(e);
     int kfd, this_rate, prev_rate;
     round_params(n_rounds, &kfd, &this_rate, &prev_rate);
     int n_s = n_stir_queries(p.soundness, p.security_level, prev_rate);
     std::vector<size_t> idx = stir_indexes(ts, kfd, n_s);
-    query(ts, cur_tree >= 0 ? tr[cur_tree] : t0, idx);
+    query_async(ts, cur_tree >= 0 ? tr[cur_tree] : t0, idx);
+    sync();
+    fill_pending_hints(ts);
     if (kc != final_rounds) throw WhirError(-1, "final sumcheck size mismatch");
   }
 
@@ -922,21 +1091,18 @@ struct Prover::Impl {
     if (k == 0) {
       E4 *h = (E4 *)ctx->pinned(16);
       cuda_check(copy_async(*ctx, h, P(), 16, cudaMemcpyDeviceToHost), "d2h");
-      ctx->sync();
+      sync();
       return *h;
     }
     int s_lo = std::min(10, k);
-    gpu::Point z;
-    z.k = k;
-    for (int i = 0; i < k; i++) z.z[i] = pt[i];
     E4 *lo = eqbuf.as<E4>(), *hi = lo + ((size_t)1 << s_lo);
-    cuda_check(gpu::eq_split(z, s_lo, e_one(), lo, hi, st()), "eq_split");
+    make_eq_tables({pt.data()}, k, {e_one()}, s_lo, lo);
     unsigned long long *a = acc.as<unsigned long long>();
     cuda_check(cudaMemsetAsync(a, 0, 32, st()), "memset");
     cuda_check(gpu::eval_ext(P(), k, lo, s_lo, hi, a, st()), "eval_ext");
     unsigned long long *h = (unsigned long long *)ctx->pinned(64);
     cuda_check(copy_async(*ctx, h, a, 32, cudaMemcpyDeviceToHost), "d2h");
-    ctx->sync();
+    sync();
     return reduce_acc(h);
   }
 };

@@ -67,7 +67,8 @@ class Context {
   void *pinned(size_t bytes);  // staging for D2H results and H2D arguments
   void sync();
   // per-kernel-class CUDA-event timing on this stream
-  enum Klass { K_DFT = 0, K_LEAF = 1, K_TREE = 2, K_SUMCHECK = 3, K_NCLASS = 4 };
+  // kernel classes timed with events, and K_SYNC: host time blocked in sync()
+  enum Klass { K_DFT = 0, K_LEAF = 1, K_TREE = 2, K_SUMCHECK = 3, K_SYNC = 4, K_NCLASS = 5 };
   void prof_enable(bool on);
   void prof_begin(int klass);
   void prof_end(int klass, double bytes);
@@ -91,9 +92,9 @@ class Context {
   };
   std::vector<Ev> evs_;
   std::vector<cudaEvent_t> free_events_;
-  double acc_ms_[K_NCLASS] = {0, 0, 0, 0};
-  long acc_n_[K_NCLASS] = {0, 0, 0, 0};
-  double acc_bytes_[K_NCLASS] = {0, 0, 0, 0};
+  double acc_ms_[K_NCLASS] = {0, 0, 0, 0, 0};
+  long acc_n_[K_NCLASS] = {0, 0, 0, 0, 0};
+  double acc_bytes_[K_NCLASS] = {0, 0, 0, 0, 0};
   unsigned long long h2d_bytes_ = 0, d2h_bytes_ = 0;
   int open_klass_ = -1;
   cudaEvent_t open_ev_ = nullptr;

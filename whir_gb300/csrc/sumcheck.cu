@@ -33,6 +33,42 @@ __global__ void eq_entries(Point z, int off, int nv, E4 scale, E4 *out) {
   out[b] = acc;
 }
 
+// n_tables split eq tables in one launch: table t = (lo: 2^s entries over
+// pts[t][0..s), hi: 2^(k-s) entries over pts[t][s..k) times scales[t]),
+// stored back to back as add_eq expects.
+__global__ void eq_tables_kernel(const E4 *__restrict__ pts, const E4 *__restrict__ scales, int k,
+                                 int s, E4 *__restrict__ out) {
+  const int t = blockIdx.y;
+  const size_t nlo = (size_t)1 << s, per = nlo + ((size_t)1 << (k - s));
+  size_t x = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (x >= per) return;
+  const E4 *z = pts + (size_t)t * k;
+  E4 acc;
+  int off, nv;
+  size_t b;
+  if (x < nlo) {
+    acc = kb::e_one(); off = 0; nv = s; b = x;
+  } else {
+    acc = scales[t]; off = s; nv = k - s; b = x - nlo;
+  }
+  for (int i = 0; i < nv; i++) {
+    E4 zi = z[off + i];
+    acc = kb::e_mul(acc, ((b >> i) & 1) ? zi : kb::e_sub(kb::e_one(), zi));
+  }
+  out[(size_t)t * per + x] = acc;
+}
+
+cudaError_t eq_tables(const E4 *pts, const E4 *scales, int n, int k, int s, E4 *out,
+                      cudaStream_t st) {
+  if (n == 0) return cudaSuccess;
+  if (s < 0 || s > k || n > 65535) return cudaErrorInvalidValue;
+  size_t per = ((size_t)1 << s) + ((size_t)1 << (k - s));
+  dim3 grid((unsigned)((per + 127) / 128), (unsigned)n);
+  eq_tables_kernel<<<grid, 128, 0, st>>>(pts, scales, k, s, out);
+  count_launches(1);
+  return cudaGetLastError();
+}
+
 static cudaError_t eq_part(const Point &z, int off, int nv, E4 scale, E4 *out, cudaStream_t st) {
   size_t n = (size_t)1 << nv;
   unsigned T = 256, G = (unsigned)((n + T - 1) / T);
@@ -173,31 +209,48 @@ cudaError_t add_eq(E4 *w, int k, const E4 *tables, int n_tables, cudaStream_t st
   return cudaGetLastError();
 }
 
-// w[i] += sum_t scale_t * var_t^i; a thread owns 16 consecutive i
-__global__ void add_pows_kernel(E4 *w, size_t n, const uint32_t *__restrict__ vars,
-                                const E4 *__restrict__ scales, int n_vars) {
-  size_t i0 = ((size_t)blockIdx.x * blockDim.x + threadIdx.x) * 16;
-  if (i0 >= n) return;
-  int cnt = n - i0 < 16 ? (int)(n - i0) : 16;
-  E4 acc[16];
-  for (int j = 0; j < cnt; j++) acc[j] = w[i0 + j];
-  for (int t = 0; t < n_vars; t++) {
-    uint32_t v = vars[t];
-    uint32_t p = kb::pow(v, i0);
-    E4 sc = scales[t];
-    for (int j = 0; j < cnt; j++) {
-      acc[j] = kb::e_add(acc[j], kb::e_scale(sc, p));
-      p = kb::mul(p, v);
-    }
-  }
-  for (int j = 0; j < cnt; j++) w[i0 + j] = acc[j];
+// var_t^i = lo_t[i mod 2^s] * hi_t[i >> s]: per var, 2^s low powers then
+// 2^(k-s) powers of var^(2^s), built by one thread per entry.
+__global__ void pow_tables_kernel(const uint32_t *__restrict__ vars, int n, int s, int k,
+                                  uint32_t *__restrict__ tab) {
+  const size_t nlo = (size_t)1 << s, per = nlo + ((size_t)1 << (k - s));
+  size_t x = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (x >= (size_t)n * per) return;
+  size_t t = x / per, j = x % per;
+  uint64_t e = j < nlo ? j : (uint64_t)(j - nlo) << s;
+  tab[x] = kb::pow(vars[t], e);
 }
 
-cudaError_t add_pows(E4 *w, int k, const uint32_t *vars, const E4 *scales, int n, cudaStream_t st) {
+// w[i] += sum_t scale_t * var_t^i, one thread per i
+__global__ void add_pows_kernel(E4 *__restrict__ w, size_t n_out, int s, int n,
+                                const uint32_t *__restrict__ tab, const E4 *__restrict__ scales) {
+  size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n_out) return;
+  const size_t nlo = (size_t)1 << s, per = nlo + (n_out >> s);
+  const size_t il = i & (nlo - 1), ih = nlo + (i >> s);
+  E4 acc = w[i];
+  for (int t = 0; t < n; t++) {
+    const uint32_t *tb = tab + (size_t)t * per;
+    uint32_t pw = kb::mul(__ldg(tb + il), __ldg(tb + ih));
+    acc = kb::e_add(acc, kb::e_scale(scales[t], pw));
+  }
+  w[i] = acc;
+}
+
+size_t add_pows_scratch_words(int k, int n) {
+  int s = k / 2;
+  return (size_t)n * (((size_t)1 << s) + ((size_t)1 << (k - s)));
+}
+
+cudaError_t add_pows(E4 *w, int k, const uint32_t *vars, const E4 *scales, int n, uint32_t *tab,
+                     cudaStream_t st) {
   if (n == 0) return cudaSuccess;
-  size_t N = (size_t)1 << k, threads = (N + 15) / 16;
-  unsigned T = 128;
-  add_pows_kernel<<<(unsigned)((threads + T - 1) / T), T, 0, st>>>(w, N, vars, scales, n);
+  int s = k / 2;
+  size_t words = add_pows_scratch_words(k, n);
+  pow_tables_kernel<<<(unsigned)((words + 255) / 256), 256, 0, st>>>(vars, n, s, k, tab);
+  count_launches(1);
+  size_t N = (size_t)1 << k;
+  add_pows_kernel<<<(unsigned)((N + 255) / 256), 256, 0, st>>>(w, N, s, n, tab, scales);
   count_launches(1);
   return cudaGetLastError();
 }

@@ -39,9 +39,9 @@ size_t Challenger::sample_bits(int bits) {
   return (size_t)v & (((size_t)1 << bits) - 1);
 }
 
-void Transcript::hint_words(const uint32_t *v, size_t n) {
-  size_t off = bytes_.size();
-  bytes_.resize(off + 4 * n);
+void Transcript::hint_words(const uint32_t *v, size_t n) { hint_fill(hint_reserve(n), v, n); }
+
+void Transcript::hint_fill(size_t off, const uint32_t *v, size_t n) {
   uint8_t *d = bytes_.data() + off;
   for (size_t i = 0; i < n; i++) {
     d[4 * i] = (uint8_t)v[i];

@@ -43,6 +43,14 @@ class Transcript {
   }
   void hint_fe(uint32_t v) { put(v); }
   void hint_words(const uint32_t *v, size_t n);
+  // Hints are never observed, so their bytes may be written after later
+  // transcript operations: reserve n words now, fill them once known.
+  size_t hint_reserve(size_t n) {
+    size_t off = bytes_.size();
+    bytes_.resize(off + 4 * n);
+    return off;
+  }
+  void hint_fill(size_t off, const uint32_t *v, size_t n);
   kb::E4 draw_ext() {
     kb::E4 e;
     for (int i = 0; i < 4; i++) e.c[i] = ch_.sample();
