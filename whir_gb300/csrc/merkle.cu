@@ -112,125 +112,79 @@ __global__ void __launch_bounds__(128) compress_level(const uint32_t *__restrict
   d[1] = make_uint4(s[4], s[5], s[6], s[7]);
 }
 
-// ---- warp-cooperative width-16 permutation for the small tree levels ----
-// A level with few nodes is bound by the latency of one permutation, not by
-// throughput.  Here the 16 lanes of a half-warp hold the 16 state words, so
-// the S-boxes of a full round run in parallel and the linear layers are a
-// few shuffles: mat4 inside each group of 4 lanes, column sums by xor
-// shuffles across groups, and the internal layer's sum by a 4-step xor
-// reduction.  Two nodes per warp (lanes 0-15 and 16-31).
-constexpr unsigned FULL = 0xffffffffu;
-
-__device__ __forceinline__ uint32_t p2w_mds(uint32_t x, int l) {
-  using namespace kb;
-  const int g = l & ~3;  // first lane of this group of 4 (shuffle width 16)
-  uint32_t x0 = __shfl_sync(FULL, x, g, 16), x1 = __shfl_sync(FULL, x, g + 1, 16);
-  uint32_t x2 = __shfl_sync(FULL, x, g + 2, 16), x3 = __shfl_sync(FULL, x, g + 3, 16);
-  uint32_t t01 = add(x0, x1), t23 = add(x2, x3), t0123 = add(t01, t23);
-  uint32_t t01123 = add(t0123, x1), t01233 = add(t0123, x3);
-  uint32_t y;
-  switch (l & 3) {
-    case 0: y = add(t01123, t01); break;
-    case 1: y = add(t01123, dbl(x2)); break;
-    case 2: y = add(t01233, t23); break;
-    default: y = add(t01233, dbl(x0)); break;
-  }
-  uint32_t s = add(y, __shfl_xor_sync(FULL, y, 4, 16));
-  s = add(s, __shfl_xor_sync(FULL, s, 8, 16));
-  return add(y, s);
-}
-
-struct P2WarpConsts {
-  uint32_t ext[8];  // this lane's external round constants
-  uint32_t diag;    // this lane's internal diagonal entry
-};
-__device__ __forceinline__ P2WarpConsts p2w_consts(int l) {
-  P2WarpConsts k;
-#pragma unroll
-  for (int r = 0; r < 8; r++) k.ext[r] = c_p2_16[r * 16 + l];
-  k.diag = c_p2_16[8 * 16 + 20 + l];
-  return k;
-}
-
-__device__ __forceinline__ uint32_t p2w_permute(uint32_t x, int l, const P2WarpConsts &k) {
-  using namespace kb;
-  x = p2w_mds(x, l);
-#pragma unroll
-  for (int r = 0; r < 4; r++) x = p2w_mds(cube(add(x, k.ext[r])), l);
-#pragma unroll 4
-  for (int r = 0; r < 20; r++) {
-    uint32_t y = cube(add(x, c_p2_16[8 * 16 + r]));
-    x = l == 0 ? y : x;
-    uint32_t s = add(x, __shfl_xor_sync(FULL, x, 1, 16));
-    s = add(s, __shfl_xor_sync(FULL, s, 2, 16));
-    s = add(s, __shfl_xor_sync(FULL, s, 4, 16));
-    s = add(s, __shfl_xor_sync(FULL, s, 8, 16));
-    x = add(s, mul(k.diag, x));
-  }
-#pragma unroll
-  for (int r = 4; r < 8; r++) x = p2w_mds(cube(add(x, k.ext[r])), l);
-  return x;
-}
-
-// node i of the next level = C(src[i], src[i + half]); half-warp per node
-__device__ __forceinline__ void p2w_compress(const uint32_t *src, uint32_t *dst, size_t half,
-                                             size_t node, int l, const P2WarpConsts &k) {
-  bool live = node < half;
-  uint32_t x = 0;
-  if (live) x = l < 8 ? src[node * 8 + l] : src[(node + half) * 8 + (l - 8)];
-  x = p2w_permute(x, l, k);  // every lane of the warp takes part in the shuffles
-  if (live && l < 8) dst[node * 8 + l] = x;
-}
-
-__global__ void __launch_bounds__(256) compress_level_warp(const uint32_t *__restrict__ src,
-                                                           uint32_t *__restrict__ dst,
-                                                           size_t half) {
-  const int l = threadIdx.x & 15;
-  const P2WarpConsts k = p2w_consts(l);
-  size_t node = ((size_t)blockIdx.x * blockDim.x + threadIdx.x) >> 4;
-  p2w_compress(src, dst, half, node, l, k);
-}
-
-// the last levels of a tree (each at most 2^TOP_LOG nodes) in one CTA
-constexpr int TOP_LOG = 9;
-__global__ void __launch_bounds__(1024) tree_top(uint32_t *nodes, int log_h, int from_level) {
-  const int l = threadIdx.x & 15;
-  const P2WarpConsts k = p2w_consts(l);
-  const size_t slots = blockDim.x >> 4;
-  for (int lev = from_level; lev < log_h; lev++) {
-    size_t half = ((size_t)1 << (log_h - lev)) / 2;
-    const uint32_t *src = nodes + level_offset_words(log_h, lev);
-    uint32_t *dst = nodes + level_offset_words(log_h, lev + 1);
-    for (size_t base = 0; base < half; base += slots)
-      p2w_compress(src, dst, half, base + (threadIdx.x >> 4), l, k);
+// ---- the narrow levels of a tree ----
+// With halves pairing, node i of a level with H nodes is C(i, i + H/2) of the
+// level below, and i, i + H/2 agree modulo any G dividing H/2.  So the nodes
+// congruent to j mod G form an independent subtree down to the level with G
+// nodes: CTA j keeps its share of a level in shared memory and climbs
+// log2(H/G) levels with one barrier per level, writing every level it makes
+// to the tree in global memory (the openings read them).  A narrow level is
+// bound by the latency of one permutation, so this replaces one launch per
+// level by two launches per tree: G CTAs up to the level of G nodes, then one
+// CTA (G = 1) to the root.
+__global__ void __launch_bounds__(512) tree_subtrees(uint32_t *__restrict__ nodes, int log_h,
+                                                    int l0, int steps) {
+  extern __shared__ uint4 sm[];  // 2 uint4 per node of this CTA's share
+  const size_t G = gridDim.x, j = blockIdx.x;
+  int n = (int)(((size_t)1 << (log_h - l0)) / G);
+  const uint4 *src = reinterpret_cast<const uint4 *>(nodes + level_offset_words(log_h, l0));
+  for (int q = threadIdx.x; q < 2 * n; q += blockDim.x) sm[q] = src[(j + G * (q >> 1)) * 2 + (q & 1)];
+  __syncthreads();
+  for (int st = 0; st < steps; st++) {
+    const int half = n >> 1;
+    const int m = threadIdx.x;
+    uint32_t s[16];
+    if (m < half) {
+      uint4 a0 = sm[2 * m], a1 = sm[2 * m + 1], b0 = sm[2 * (m + half)], b1 = sm[2 * (m + half) + 1];
+      s[0] = a0.x; s[1] = a0.y; s[2] = a0.z; s[3] = a0.w;
+      s[4] = a1.x; s[5] = a1.y; s[6] = a1.z; s[7] = a1.w;
+      s[8] = b0.x; s[9] = b0.y; s[10] = b0.z; s[11] = b0.w;
+      s[12] = b1.x; s[13] = b1.y; s[14] = b1.z; s[15] = b1.w;
+      p2_permute<16>(s);
+      uint4 *dst = reinterpret_cast<uint4 *>(nodes + level_offset_words(log_h, l0 + st + 1));
+      dst[(j + G * m) * 2] = make_uint4(s[0], s[1], s[2], s[3]);
+      dst[(j + G * m) * 2 + 1] = make_uint4(s[4], s[5], s[6], s[7]);
+    }
+    __syncthreads();  // every read of this level's shared copy is done
+    if (m < half) {
+      sm[2 * m] = make_uint4(s[0], s[1], s[2], s[3]);
+      sm[2 * m + 1] = make_uint4(s[4], s[5], s[6], s[7]);
+    }
     __syncthreads();
+    n = half;
   }
+}
+
+// Levels whose step makes at least 2^WIDE_LOG nodes run one thread per node
+// over the whole GPU; the rest (at most 2^(WIDE_LOG+1) nodes at the first
+// narrow level) go through tree_subtrees.
+constexpr int WIDE_LOG = 15;
+
+static cudaError_t launch_subtrees(uint32_t *nodes, int log_h, int l0, int log_g, cudaStream_t st) {
+  int steps = log_h - l0 - log_g;
+  if (steps <= 0) return cudaSuccess;
+  int n = 1 << steps;  // nodes per CTA at level l0
+  int threads = n / 2 < 32 ? 32 : n / 2;
+  tree_subtrees<<<1u << log_g, threads, (size_t)n * 32, st>>>(nodes, log_h, l0, steps);
+  count_launches(1);
+  return cudaGetLastError();
 }
 
 cudaError_t build_tree(uint32_t *nodes, int log_h, cudaStream_t st) {
   const int T = 128;
   int l = 0;
-  // wide levels: one thread per node (throughput)
-  for (; l < log_h && ((size_t)1 << (log_h - l)) / 2 >= ((size_t)1 << 15); l++) {
+  for (; l < log_h && ((size_t)1 << (log_h - l)) / 2 >= ((size_t)1 << WIDE_LOG); l++) {
     size_t half = ((size_t)1 << (log_h - l)) / 2;
     compress_level<<<(unsigned)((half + T - 1) / T), T, 0, st>>>(
         nodes + level_offset_words(log_h, l), nodes + level_offset_words(log_h, l + 1), half);
     count_launches(1);
   }
-  // middle levels: half a warp per node (latency)
-  for (; l < log_h && ((size_t)1 << (log_h - l)) / 2 > ((size_t)1 << TOP_LOG); l++) {
-    size_t half = ((size_t)1 << (log_h - l)) / 2;
-    size_t threads = half * 16;
-    compress_level_warp<<<(unsigned)((threads + 255) / 256), 256, 0, st>>>(
-        nodes + level_offset_words(log_h, l), nodes + level_offset_words(log_h, l + 1), half);
-    count_launches(1);
-  }
-  // top levels: one CTA, one launch
-  if (l < log_h) {
-    tree_top<<<1, 1024, 0, st>>>(nodes, log_h, l);
-    count_launches(1);
-  }
-  return cudaGetLastError();
+  // remaining S = log_h - l steps (S <= WIDE_LOG): G = 2^(S/2) subtrees, then the top
+  int S = log_h - l;
+  int log_g = S / 2;
+  cudaError_t e = launch_subtrees(nodes, log_h, l, log_g, st);
+  if (e != cudaSuccess) return e;
+  return launch_subtrees(nodes, log_h, log_h - log_g, 0, st);
 }
 
 __global__ void gather_openings_kernel(const uint32_t *__restrict__ rows, int row_len,
