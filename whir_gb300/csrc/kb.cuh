@@ -37,19 +37,24 @@ KB_HD uint32_t umin(uint32_t a, uint32_t b) {
 #endif
 }
 
+// t * MU mod 2^32 with MU = 2^31 + 2^24 + 1: two shifted adds instead of a
+// multiply (integer multiplies issue at half rate, their high halves at
+// quarter rate on the SM).
+KB_HD uint32_t times_mu(uint32_t lo) { return lo + (lo << 24) + (lo << 31); }
+
 // Montgomery product: (a*b - t*p) / 2^32 with t = a*b*p^-1 mod 2^32.
+// Valid for a < 2^32 and b < p (the product is below p * 2^32).
 KB_HD uint32_t mul(uint32_t a, uint32_t b) {
-  uint32_t lo = a * b, hi = mulhi(a, b);
-  uint32_t t = lo * MU;
-  uint32_t th = mulhi(t, P);
+  uint64_t prod = (uint64_t)a * b;
+  uint32_t lo = (uint32_t)prod, hi = (uint32_t)(prod >> 32);
+  uint32_t th = mulhi(times_mu(lo), P);
   uint32_t r = hi - th;  // in (-p, p); as u32, r + p is the smaller one iff r < 0
   return umin(r, r + P);
 }
 // reduction of a 64-bit sum x < 2p * 2^32 (e.g. four products of canonical words)
 KB_HD uint32_t reduce_wide(uint64_t x) {
   uint32_t lo = (uint32_t)x, hi = (uint32_t)(x >> 32);
-  uint32_t t = lo * MU;
-  uint32_t th = mulhi(t, P);
+  uint32_t th = mulhi(times_mu(lo), P);
   uint32_t r = hi - th;  // in (-p, 2p)
   if (hi < th) return r + P;
   return umin(r, r - P);

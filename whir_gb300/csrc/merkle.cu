@@ -16,9 +16,10 @@ static cudaError_t upload_p2(int width) {
   const Poseidon2Constants &c = poseidon2_constants(width);
   uint32_t buf[8 * 24 + 23 + 24];
   int n = 0;
+  // round constants minus p, for the signed S-box (p2_device.cuh)
   for (int r = 0; r < 8; r++)
-    for (int i = 0; i < width; i++) buf[n++] = c.ext_rc[r][i];
-  for (int r = 0; r < c.rounds_p; r++) buf[n++] = c.int_rc[r];
+    for (int i = 0; i < width; i++) buf[n++] = c.ext_rc[r][i] - kb::P;
+  for (int r = 0; r < c.rounds_p; r++) buf[n++] = c.int_rc[r] - kb::P;
   for (int i = 0; i < width; i++) buf[n++] = c.diag[i];
   if (width == 16) return cudaMemcpyToSymbol(c_p2_16, buf, n * 4);
   return cudaMemcpyToSymbol(c_p2_24, buf, n * 4);

@@ -193,6 +193,172 @@ __global__ void __launch_bounds__(256) dft_tile(const uint32_t *__restrict__ in,
   }
 }
 
+// ---- vectorised tile: 4 columns per task ----
+// The same transform as dft_tile, for column slices of C = 4 or 8 words held
+// as uint4: a task moves and butterflies 4 columns at once, so shared-memory
+// instructions, index arithmetic and twiddle loads are shared by 4 columns.
+// Rows are permuted inside aligned groups of 32 / C rows (one group spans
+// the 32 banks) by XOR with bits 3.. of the row, which keeps the 8 lanes of
+// a 128-byte phase on distinct banks for row strides 1, 8 and 2^k >= 8.
+template <int C>
+__device__ __forceinline__ int vrow(int row) {
+  return row ^ ((row >> 3) & (32 / C - 1));
+}
+__device__ __forceinline__ uint4 add4(uint4 a, uint4 b) {
+  return make_uint4(kb::add(a.x, b.x), kb::add(a.y, b.y), kb::add(a.z, b.z), kb::add(a.w, b.w));
+}
+__device__ __forceinline__ uint4 sub4(uint4 a, uint4 b) {
+  return make_uint4(kb::sub(a.x, b.x), kb::sub(a.y, b.y), kb::sub(a.z, b.z), kb::sub(a.w, b.w));
+}
+// (a - b) * w for a canonical twiddle w (a - b + p < 2^32 needs no reduction)
+__device__ __forceinline__ uint4 submul4(uint4 a, uint4 b, uint32_t w) {
+  return make_uint4(kb::mul(a.x - b.x + kb::P, w), kb::mul(a.y - b.y + kb::P, w),
+                    kb::mul(a.z - b.z + kb::P, w), kb::mul(a.w - b.w + kb::P, w));
+}
+__device__ __forceinline__ uint4 mul4(uint4 a, uint32_t w) {
+  return make_uint4(kb::mul(a.x, w), kb::mul(a.y, w), kb::mul(a.z, w), kb::mul(a.w, w));
+}
+
+// R radix-2 DIF stages in registers (see dif_step).  LAST: the final step of
+// the transform, where the block stride q is 1, the first half-size is
+// 2^(R-1) and position 0 of every stage has twiddle 1.
+template <int C, int R, bool LAST>
+__device__ __forceinline__ void dif_step_v(uint4 *tile, const uint32_t *twl, int rows_log, int lh) {
+  constexpr int T = 1 << R, V = C / 4, LV = V == 2 ? 1 : 0;
+  const int lq = LAST ? 0 : lh - (R - 1);
+  const int q = 1 << lq;
+  const int H = LAST ? (1 << (R - 1)) : (1 << lh);
+  const int tasks = (1 << (rows_log - R)) << LV;
+  for (int task = threadIdx.x; task < tasks; task += blockDim.x) {
+    const int c = task & (V - 1), rest = task >> LV;
+    const int j = rest & (q - 1), blk = rest >> lq;
+    const int base = blk * 2 * H + j;
+    uint4 v[T];
+#pragma unroll
+    for (int t = 0; t < T; t++) v[t] = tile[vrow<C>(base + t * q) * V + c];
+#pragma unroll
+    for (int st = 0; st < R; st++) {
+      const int span = T >> (st + 1);
+      const int hh = H >> st;
+#pragma unroll
+      for (int t = 0; t < T; t++) {
+        if (t & span) continue;
+        const int tl = t & (span - 1);
+        uint4 a = v[t], b = v[t + span];
+        v[t] = add4(a, b);
+        if (LAST && tl == 0) v[t + span] = sub4(a, b);  // w^0 = 1
+        else v[t + span] = submul4(a, b, twl[hh + j + tl * q]);
+      }
+    }
+#pragma unroll
+    for (int t = 0; t < T; t++) tile[vrow<C>(base + t * q) * V + c] = v[t];
+  }
+}
+
+template <int C, int R>
+__device__ __forceinline__ void dif_run_v(uint4 *tile, const uint32_t *twl, int rows_log, int lh) {
+  if (lh == R - 1) dif_step_v<C, R, true>(tile, twl, rows_log, lh);
+  else dif_step_v<C, R, false>(tile, twl, rows_log, lh);
+  __syncthreads();
+}
+
+// Arguments as dft_tile; C in {4, 8}; the rows of `in` and `out` start on
+// 16-byte boundaries (width % 4 == 0, aligned base pointers).
+template <int C>
+__global__ void __launch_bounds__(256) dft_tile_v(const uint32_t *__restrict__ in,
+                                                  uint32_t *__restrict__ out, int S, int lg,
+                                                  uint32_t width, uint32_t rows_valid,
+                                                  uint32_t a_in, uint32_t b_in, uint32_t a_out,
+                                                  uint32_t b_out, int pre_log, int tw_log) {
+  constexpr int V = C / 4, LV = V == 2 ? 1 : 0;
+  extern __shared__ uint4 smv[];
+  const int n = 1 << S, rows = n << lg;
+  uint4 *tile = smv;
+  uint32_t *aux = reinterpret_cast<uint32_t *>(smv + rows * V);
+  const uint32_t o0 = blockIdx.y << lg;
+  const uint32_t v0 = blockIdx.x * V;  // first uint4 of the slice in a row
+  const uint32_t wv = width / 4;       // uint4 per matrix row
+  const uint4 *in4 = reinterpret_cast<const uint4 *>(in);
+  uint4 *out4 = reinterpret_cast<uint4 *>(out);
+  const int tid = threadIdx.x, nt = blockDim.x;
+
+  if (pre_log) {
+    const uint32_t m = (1u << pre_log) - 1u;
+    for (int r = tid; r < rows; r += nt) {
+      uint32_t o = o0 + (uint32_t)(r >> S), i = (uint32_t)(r & (n - 1));
+      aux[r] = root_pow(((o * i) & m) << (24 - pre_log));
+    }
+    __syncthreads();
+  }
+  for (int e = tid; e < rows * V; e += nt) {
+    int r = e >> LV, c = e & (V - 1);
+    uint32_t o = o0 + (uint32_t)(r >> S), i = (uint32_t)(r & (n - 1));
+    uint32_t row = o * a_in + i * b_in;
+    uint4 v = make_uint4(0, 0, 0, 0);
+    if (row < rows_valid) v = __ldg(in4 + row * wv + v0 + c);
+    if (pre_log) v = mul4(v, aux[r]);
+    tile[vrow<C>(r) * V + c] = v;
+  }
+  __syncthreads();
+  for (int x = tid + 1; x < n; x += nt) {
+    int lh = 31 - __clz(x);
+    uint32_t pos = (uint32_t)(x - (1 << lh));
+    aux[x] = root_pow(pos << (24 - 1 - lh));  // w_{2^(lh+1)}^pos
+  }
+  __syncthreads();
+  // S % 3 stages first (large block strides), then radix-8 steps; the last
+  // step has block stride 1
+  const int rows_log = S + lg;
+  int lh = S - 1;
+  if (S % 3 == 1) { dif_run_v<C, 1>(tile, aux, rows_log, lh); lh -= 1; }
+  else if (S % 3 == 2) { dif_run_v<C, 2>(tile, aux, rows_log, lh); lh -= 2; }
+  while (lh >= 2) {
+    dif_run_v<C, 3>(tile, aux, rows_log, lh);
+    lh -= 3;
+  }
+  if (tw_log) {
+    const uint32_t m = (1u << tw_log) - 1u;
+    for (int r = tid; r < rows; r += nt) {
+      uint32_t o = o0 + (uint32_t)(r >> S), k = brev((uint32_t)(r & (n - 1)), S);
+      aux[r] = root_pow(((o * k) & m) << (24 - tw_log));
+    }
+    __syncthreads();
+  }
+  for (int e = tid; e < rows * V; e += nt) {
+    int r = e >> LV, c = e & (V - 1);
+    uint4 v = tile[vrow<C>(r) * V + c];
+    uint32_t o = o0 + (uint32_t)(r >> S);
+    uint32_t k = brev((uint32_t)(r & (n - 1)), S);
+    if (tw_log) v = mul4(v, aux[r]);
+    out4[(o * a_out + k * b_out) * wv + v0 + c] = v;
+  }
+}
+
+template <int C>
+static cudaError_t launch_tile_v(const uint32_t *in, uint32_t *out, int S, size_t width,
+                                 size_t rows_valid, size_t n_outer, size_t a_in, size_t b_in,
+                                 size_t a_out, size_t b_out, int pre_log, int tw_log,
+                                 cudaStream_t st) {
+  int lg = 0;
+  while (S + lg < 11 && ((size_t)2 << lg) <= n_outer) lg++;
+  size_t rows = (size_t)1 << (S + lg);
+  size_t smem = (rows * C + rows) * 4;
+  static bool attr_set = false;
+  if (!attr_set) {
+    cudaFuncSetAttribute(dft_tile_v<C>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                         ((1 << MAX_TILE_LOG) * C + (1 << MAX_TILE_LOG)) * 4);
+    attr_set = true;
+  }
+  int threads = (int)(rows * (C / 4) / 8);
+  threads = threads < 32 ? 32 : (threads > 256 ? 256 : threads);
+  dim3 grid((unsigned)(width / C), (unsigned)(n_outer >> lg));
+  dft_tile_v<C><<<grid, threads, smem, st>>>(in, out, S, lg, (uint32_t)width,
+                                             (uint32_t)rows_valid, (uint32_t)a_in, (uint32_t)b_in,
+                                             (uint32_t)a_out, (uint32_t)b_out, pre_log, tw_log);
+  count_launches(1);
+  return cudaGetLastError();
+}
+
 template <int C>
 static cudaError_t launch_tile(const uint32_t *in, uint32_t *out, int S, size_t width,
                                size_t rows_valid, size_t n_outer, size_t a_in, size_t b_in,
@@ -222,6 +388,13 @@ static cudaError_t launch_tile(const uint32_t *in, uint32_t *out, int S, size_t 
 static cudaError_t tile_any(const uint32_t *in, uint32_t *out, int S, size_t width,
                             size_t rows_valid, size_t n_outer, size_t a_in, size_t b_in,
                             size_t a_out, size_t b_out, int pre_log, int tw_log, cudaStream_t st) {
+  const bool aligned = (((uintptr_t)in | (uintptr_t)out) & 15) == 0;
+  if (aligned && width % 8 == 0)
+    return launch_tile_v<8>(in, out, S, width, rows_valid, n_outer, a_in, b_in, a_out, b_out,
+                            pre_log, tw_log, st);
+  if (aligned && width % 4 == 0)
+    return launch_tile_v<4>(in, out, S, width, rows_valid, n_outer, a_in, b_in, a_out, b_out,
+                            pre_log, tw_log, st);
   if (width % 8 == 0)
     return launch_tile<8>(in, out, S, width, rows_valid, n_outer, a_in, b_in, a_out, b_out,
                           pre_log, tw_log, st);

@@ -17,7 +17,9 @@ namespace whir {
 namespace gpu {
 
 // [0 .. 8*W) external constants (round-major), then rounds_p internal, then W
-// diag.  Defined here (one translation unit includes this header: merkle.cu,
+// diag.  The round constants are stored minus p (mod 2^32): state + (c - p)
+// is then the signed value state + c - p in [-p, p), which the signed S-box
+// takes without a reduction.  Defined here (one translation unit includes this header: merkle.cu,
 // which also uploads them).
 __constant__ uint32_t c_p2_16[8 * 16 + 20 + 16];
 __constant__ uint32_t c_p2_24[8 * 24 + 23 + 24];
@@ -124,17 +126,30 @@ __device__ __forceinline__ void p2_internal_all(uint32_t (&s)[W], uint32_t sum,
   (p2_internal_lane<W, I>(s, sum), ...);
 }
 
+// Signed Montgomery product of int32 words with |a * b| < p * 2^31: with t
+// = a*b*p^-1 mod 2^32 read as signed, (a*b - t*p) / 2^32 lies in (-p, p).
+__device__ __forceinline__ int32_t smul(int32_t a, int32_t b) {
+  int64_t prod = (int64_t)a * (int64_t)b;
+  int32_t t = (int32_t)kb::times_mu((uint32_t)prod);
+  return (int32_t)(prod >> 32) - __mulhi(t, (int32_t)kb::P);
+}
+// x^3 for x in [-p, p) (a state word plus a stored constant), canonical out
+__device__ __forceinline__ uint32_t sbox(int32_t x) {
+  uint32_t r = (uint32_t)smul(smul(x, x), x);
+  return kb::umin(r, r + kb::P);
+}
+
 template <int W>
 __device__ __forceinline__ void p2_external_round(uint32_t (&s)[W], const uint32_t *rc) {
 #pragma unroll
-  for (int i = 0; i < W; i++) s[i] = kb::cube(kb::add(s[i], rc[i]));
+  for (int i = 0; i < W; i++) s[i] = sbox((int32_t)(s[i] + rc[i]));
   p2_mds_light<W>(s);
 }
 
 template <int W>
 __device__ __forceinline__ void p2_internal_round(uint32_t (&s)[W], uint32_t rc) {
   using namespace kb;
-  s[0] = cube(add(s[0], rc));
+  s[0] = sbox((int32_t)(s[0] + rc));
   // sum of the W canonical lanes in 64 bits (< W p < 2^36), then one
   // reduction: 2^31 = 2^24 - 1 (mod p) folds the high part, leaving < 2p
   uint64_t wide = 0;
