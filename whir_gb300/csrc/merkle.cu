@@ -113,6 +113,53 @@ __global__ void __launch_bounds__(128) compress_level(const uint32_t *__restrict
   d[1] = make_uint4(s[4], s[5], s[6], s[7]);
 }
 
+// ---- width-16 permutation on a quad of lanes (latency) ----
+// Lane l of an aligned group of 4 holds state words 4l .. 4l+3, which is one
+// group of the light MDS: mat4 stays in registers and the column sums are two
+// xor shuffles.  In an internal round every lane adds its 4 words, two
+// shuffles finish the sum and each lane applies its 4 diagonal entries.  A
+// permutation is then about a quarter of the dependent instructions of the
+// one-thread form, which is what a level with few nodes waits for.
+constexpr unsigned FULL = 0xffffffffu;
+
+__device__ __forceinline__ void p2q_mds(uint32_t (&x)[4]) {
+  p2_mat4(x[0], x[1], x[2], x[3]);
+#pragma unroll
+  for (int c = 0; c < 4; c++) {
+    uint32_t t = kb::add(x[c], __shfl_xor_sync(FULL, x[c], 1, 4));
+    t = kb::add(t, __shfl_xor_sync(FULL, t, 2, 4));
+    x[c] = kb::add(x[c], t);
+  }
+}
+
+// kc: the 8*16 external and 20 internal constants (stored minus p); dg: this
+// lane's 4 diagonal entries (Montgomery form).  Every lane of the warp calls it.
+__device__ __forceinline__ void p2q_permute(uint32_t (&x)[4], int l, const uint32_t *kc,
+                                            const uint32_t (&dg)[4]) {
+  using namespace kb;
+  p2q_mds(x);
+#pragma unroll 1
+  for (int r = 0; r < 8; r++) {
+    if (r == 4) {
+#pragma unroll 1
+      for (int q = 0; q < 20; q++) {
+        uint32_t y = sbox((int32_t)(x[0] + kc[8 * 16 + q]));
+        if (l == 0) x[0] = y;
+        uint64_t w = (uint64_t)x[0] + x[1] + x[2] + x[3];  // < 2^33
+        uint32_t f = (uint32_t)(w & 0x7fffffffu) + (uint32_t)(w >> 31) * 0x00ffffffu;
+        uint32_t sum = kb::umin(f, f - P);
+        sum = add(sum, __shfl_xor_sync(FULL, sum, 1, 4));
+        sum = add(sum, __shfl_xor_sync(FULL, sum, 2, 4));
+#pragma unroll
+        for (int i = 0; i < 4; i++) x[i] = add(sum, mul(x[i], dg[i]));
+      }
+    }
+#pragma unroll
+    for (int i = 0; i < 4; i++) x[i] = sbox((int32_t)(x[i] + kc[r * 16 + 4 * l + i]));
+    p2q_mds(x);
+  }
+}
+
 // ---- the narrow levels of a tree ----
 // With halves pairing, node i of a level with H nodes is C(i, i + H/2) of the
 // level below, and i, i + H/2 agree modulo any G dividing H/2.  So the nodes
@@ -121,11 +168,18 @@ __global__ void __launch_bounds__(128) compress_level(const uint32_t *__restrict
 // log2(H/G) levels with one barrier per level, writing every level it makes
 // to the tree in global memory (the openings read them).  A narrow level is
 // bound by the latency of one permutation, so this replaces one launch per
-// level by two launches per tree: G CTAs up to the level of G nodes, then one
-// CTA (G = 1) to the root.
-__global__ void __launch_bounds__(512) tree_subtrees(uint32_t *__restrict__ nodes, int log_h,
-                                                    int l0, int steps) {
+// level by two launches per tree (G CTAs up to the level of G nodes, then one
+// CTA, G = 1, to the root), and each node is compressed by a quad of lanes.
+// Threads: 4 per node of the first level made (at most 1024).
+__global__ void __launch_bounds__(1024) tree_subtrees(uint32_t *__restrict__ nodes, int log_h,
+                                                     int l0, int steps) {
   extern __shared__ uint4 sm[];  // 2 uint4 per node of this CTA's share
+  __shared__ uint32_t kc[8 * 16 + 20];
+  for (int i = threadIdx.x; i < 8 * 16 + 20; i += blockDim.x) kc[i] = c_p2_16[i];
+  const int l = threadIdx.x & 3, m = threadIdx.x >> 2;
+  uint32_t dg[4];
+#pragma unroll
+  for (int i = 0; i < 4; i++) dg[i] = c_p2_16[8 * 16 + 20 + 4 * l + i];
   const size_t G = gridDim.x, j = blockIdx.x;
   int n = (int)(((size_t)1 << (log_h - l0)) / G);
   const uint4 *src = reinterpret_cast<const uint4 *>(nodes + level_offset_words(log_h, l0));
@@ -133,24 +187,23 @@ __global__ void __launch_bounds__(512) tree_subtrees(uint32_t *__restrict__ node
   __syncthreads();
   for (int st = 0; st < steps; st++) {
     const int half = n >> 1;
-    const int m = threadIdx.x;
-    uint32_t s[16];
-    if (m < half) {
-      uint4 a0 = sm[2 * m], a1 = sm[2 * m + 1], b0 = sm[2 * (m + half)], b1 = sm[2 * (m + half) + 1];
-      s[0] = a0.x; s[1] = a0.y; s[2] = a0.z; s[3] = a0.w;
-      s[4] = a1.x; s[5] = a1.y; s[6] = a1.z; s[7] = a1.w;
-      s[8] = b0.x; s[9] = b0.y; s[10] = b0.z; s[11] = b0.w;
-      s[12] = b1.x; s[13] = b1.y; s[14] = b1.z; s[15] = b1.w;
-      p2_permute<16>(s);
-      uint4 *dst = reinterpret_cast<uint4 *>(nodes + level_offset_words(log_h, l0 + st + 1));
-      dst[(j + G * m) * 2] = make_uint4(s[0], s[1], s[2], s[3]);
-      dst[(j + G * m) * 2 + 1] = make_uint4(s[4], s[5], s[6], s[7]);
+    const bool warp_live = ((threadIdx.x & ~31) >> 2) < half;  // warp-uniform
+    const bool live = m < half;
+    uint32_t x[4] = {0, 0, 0, 0};
+    if (warp_live) {
+      if (live) {
+        // lanes 0, 1: the left child's two halves; lanes 2, 3: the right child's
+        uint4 v = l < 2 ? sm[2 * m + l] : sm[2 * (m + half) + (l - 2)];
+        x[0] = v.x; x[1] = v.y; x[2] = v.z; x[3] = v.w;
+      }
+      p2q_permute(x, l, kc, dg);
+      if (live && l < 2) {
+        uint4 *dst = reinterpret_cast<uint4 *>(nodes + level_offset_words(log_h, l0 + st + 1));
+        dst[(j + G * m) * 2 + l] = make_uint4(x[0], x[1], x[2], x[3]);
+      }
     }
     __syncthreads();  // every read of this level's shared copy is done
-    if (m < half) {
-      sm[2 * m] = make_uint4(s[0], s[1], s[2], s[3]);
-      sm[2 * m + 1] = make_uint4(s[4], s[5], s[6], s[7]);
-    }
+    if (live && l < 2) sm[2 * m + l] = make_uint4(x[0], x[1], x[2], x[3]);
     __syncthreads();
     n = half;
   }
@@ -165,7 +218,7 @@ static cudaError_t launch_subtrees(uint32_t *nodes, int log_h, int l0, int log_g
   int steps = log_h - l0 - log_g;
   if (steps <= 0) return cudaSuccess;
   int n = 1 << steps;  // nodes per CTA at level l0
-  int threads = n / 2 < 32 ? 32 : n / 2;
+  int threads = 2 * n < 32 ? 32 : 2 * n;  // a quad per node made at the first step
   tree_subtrees<<<1u << log_g, threads, (size_t)n * 32, st>>>(nodes, log_h, l0, steps);
   count_launches(1);
   return cudaGetLastError();

@@ -150,11 +150,12 @@ template <int W>
 __device__ __forceinline__ void p2_internal_round(uint32_t (&s)[W], uint32_t rc) {
   using namespace kb;
   s[0] = sbox((int32_t)(s[0] + rc));
-  // sum of the W canonical lanes in 64 bits (< W p < 2^36), then one
-  // reduction: 2^31 = 2^24 - 1 (mod p) folds the high part, leaving < 2p
+  // sum of the W canonical lanes in 64 bits (< W p < 2^36): pairs of lanes
+  // add without overflow in 32 bits (2p < 2^32), then one reduction:
+  // 2^31 = 2^24 - 1 (mod p) folds the high part, leaving < 2p
   uint64_t wide = 0;
 #pragma unroll
-  for (int i = 0; i < W; i++) wide += s[i];
+  for (int i = 0; i < W; i += 2) wide += (uint32_t)(s[i] + s[i + 1]);
   uint32_t folded = (uint32_t)(wide & 0x7fffffffu) + (uint32_t)(wide >> 31) * 0x00ffffffu;
   uint32_t sum = kb::umin(folded, folded - P);
   p2_internal_all<W>(s, sum, std::make_integer_sequence<int, W>{});
