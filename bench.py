@@ -57,6 +57,12 @@ def parse():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--cpu-seconds", type=float, default=12.0,
                     help="time budget of the bounded CPU baseline sample")
+    ap.add_argument("--no-batched", action="store_true",
+                    help="skip the batched / served workloads")
+    ap.add_argument("--workers", type=int, default=0,
+                    help="concurrent provers of the batched / served runs (0: from host cores)")
+    ap.add_argument("--serve-seconds", type=float, default=2.0,
+                    help="length of the served Poisson request stream")
     return ap.parse_args()
 
 
@@ -187,6 +193,107 @@ def run_reference(args):
         "e2e": {"value": v, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
     }
     print(json.dumps(line), flush=True)
+
+
+def _pct(v, q):
+    return 1e3 * float(np.percentile(v, q)) if len(v) else None
+
+
+def run_batched(W, args, device):
+    """Batched and served proving through the persistent worker pool
+    (whir_server_*), each against the plain one-worker loop on the same jobs.
+
+    batched_commit: 64 commitments, k uniform over 14..22 (log-uniform sizes),
+    rate 1/2, folding 4; committed elements/s.  batched: 256 proofs at k=16 and
+    16 at k=22, rate 1/4, folding 4, 2 claims each; proofs/s and completion
+    p50/p99.  served: Poisson arrivals at 200/s, k uniform over 14..24, rate
+    1/2 or 1/4, 1-4 claims, 150 GB device budget; p50/p99 latency from
+    arrival.  Inputs sit in pinned host memory; every proof of the pool is
+    compared with the plain loop's proof of the same job.
+    """
+    import torch
+    workers = args.workers or max(2, min(12, (os.cpu_count() or 4) - 2))
+    rng = np.random.default_rng(WORKLOAD["seed"] + 17)
+    pool = {}
+    for k in range(14, 25):
+        t = torch.empty(1 << k, dtype=torch.int32, pin_memory=True)
+        a = t.numpy().view(np.uint32)
+        W.random_field(WORKLOAD["seed"] + 100 + k, 1 << k, out=a)
+        pool[k] = (t, a)
+
+    def job(k, rate, claims, commit_only=False, arrival=0.0):
+        return W.Job((k, WORKLOAD["folding"], rate, WORKLOAD["initial_reduction"],
+                      WORKLOAD["soundness_id"], WORKLOAD["security_level"]), pool[k][1],
+                     claims=claims, commit_only=commit_only, arrival_s=arrival)
+
+    def same(a, b):
+        return all(x.status == 0 and y.status == 0 and x.proof == y.proof and
+                   x.checkpoint == y.checkpoint for x, y in zip(a, b))
+
+    budget = 150 << 30
+    srv = W.Server(workers=workers, device=device, budget_bytes=budget)
+    one = W.Server(workers=1, device=device, budget_bytes=budget)
+    out = {"workers": workers}
+    try:
+        # warm both pools up to the largest shape (buffers are kept)
+        warm = [job(24, 2, 1) for _ in range(workers)]
+        srv.run(warm)
+        one.run([job(24, 2, 1)])
+
+        # cfg: batched commitment
+        ks = [int(x) for x in rng.integers(14, 23, 64)]
+        mk = lambda: [job(k, 1, 0, commit_only=True) for k in ks]
+        a, b = mk(), mk()
+        srv.run(a)
+        sa, _ = srv.run(a)
+        sb, _ = one.run(b)
+        elems = float(sum(1 << k for k in ks))
+        out["batched_commit"] = {
+            "workload": "64 commitments, k uniform over 14..22 (seeded), rate 1/2, folding 4",
+            "elements_per_s": elems / sa, "plain_loop_elements_per_s": elems / sb,
+            "speedup": sb / sa, "seconds": sa, "bit_exact_vs_plain": same(a, b)}
+
+        # cfg: batched full proofs
+        shapes = [16] * 256 + [22] * 16
+        order = rng.permutation(len(shapes))
+        mk = lambda: [job(shapes[i], 2, 2) for i in order]
+        a, b = mk(), mk()
+        srv.run(a)
+        sa, peak = srv.run(a)
+        sb, _ = one.run(b)
+        lat = [j.done_s for j in a]
+        out["batched"] = {
+            "workload": "256 proofs at k=16 + 16 at k=22, rate 1/4, folding 4, 2 claims each",
+            "proofs_per_s": len(a) / sa, "plain_loop_proofs_per_s": len(b) / sb,
+            "speedup": sb / sa, "p50_ms": _pct(lat, 50), "p99_ms": _pct(lat, 99),
+            "peak_device_gb": peak / 2 ** 30, "bit_exact_vs_plain": same(a, b)}
+
+        # cfg: served Poisson stream
+        arr, t = [], 0.0
+        while True:
+            t += float(rng.exponential(1 / 200.0))
+            if t > args.serve_seconds:
+                break
+            arr.append(t)
+        spec = [(int(rng.integers(14, 25)), int(rng.choice([1, 2])), int(rng.integers(1, 5)))
+                for _ in arr]
+        mk = lambda: [job(k, r, c, arrival=x) for (k, r, c), x in zip(spec, arr)]
+        a, b = mk(), mk()
+        sa, peak = srv.run(a, serve=True)
+        sb, _ = one.run(b, serve=True)
+        la = [j.latency_s for j in a]
+        lb = [j.latency_s for j in b]
+        out["served"] = {
+            "workload": f"Poisson 200 req/s for {args.serve_seconds:g} s ({len(a)} jobs), k uniform "
+                        f"over 14..24, rate 1/2 or 1/4, folding 4, 1-4 claims, 150 GB budget",
+            "proofs_per_s": len(a) / sa, "p50_ms": _pct(la, 50), "p99_ms": _pct(la, 99),
+            "serial_plain": {"proofs_per_s": len(b) / sb, "p50_ms": _pct(lb, 50),
+                             "p99_ms": _pct(lb, 99)},
+            "peak_device_gb": peak / 2 ** 30, "bit_exact_vs_plain": same(a, b)}
+    finally:
+        srv.close()
+        one.close()
+    return out
 
 
 def run_gb300(args):
@@ -330,6 +437,8 @@ def run_gb300(args):
         "gpu_launches": int(launches1 - launches0),
         "clocks": clk,
     }
+    if not args.no_batched:
+        line["batched_served"] = run_batched(W, args, local)
     if not args.no_cpu_baseline and world == 1:
         line["cpu_baseline"] = cpu_baseline(k, args.cpu_seconds, expect_proof=gpu_proof)
     print(json.dumps(line), flush=True)

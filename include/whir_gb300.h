@@ -171,6 +171,65 @@ WHIR_API int whir_prove(whir_prover *p, whir_transcript *t, const uint32_t *poly
                const int32_t *poly_k, int n_polys, const int32_t *group_n, int n_groups,
                const int32_t *group_ids);
 
+/* ---- many proofs on one GPU (batched and served proving).  No
+ * counterpart in the reference, whose harness proves one polynomial per call
+ * (crates/whir/src/test.rs:218-235); each job here is that harness on one
+ * polynomial, with n_claims claim groups of that polynomial, or the
+ * commitment alone.  n_workers host threads each own a stream and a prover
+ * (device buffers are reused from job to job and only grow), so the kernels
+ * of concurrent jobs overlap on the GPU.  Jobs start in arrival order; a job
+ * starts once it has arrived (whir_serve; whir_batch_prove releases all at
+ * once), a worker is free and the device bytes held by all workers
+ * (whir_workspace_bytes per job, buffers never shrink) stay within
+ * device_budget.  A job's proof bytes are the same whichever worker runs it
+ * and whatever runs beside it.  The call returns when every job is done;
+ * per-job failures are reported in job->status, argument errors in the
+ * return value.  Replicas on several GPUs are separate calls. ---- */
+typedef struct whir_job {
+  whir_params params;
+  const uint32_t *poly;   /* 2^params.k words, Montgomery form */
+  int32_t poly_on_device; /* nonzero: poly is device memory of this process */
+  int32_t n_claims;       /* evaluation claims at transcript-drawn points */
+  int32_t commit_only;    /* nonzero: commit only; the proof is the root */
+  double arrival_s;       /* whir_serve: release time after the start of the call */
+  uint8_t *proof;         /* out: caller buffer of proof_cap bytes (NULL with cap 0) */
+  size_t proof_cap;
+  size_t proof_len;       /* out: full proof length (copied up to proof_cap) */
+  uint32_t checkpoint;    /* out: base element drawn after the proof (test.rs:236) */
+  int32_t status;         /* out: WHIR_OK or an error code */
+  int32_t worker;         /* out: the worker that ran it */
+  double start_s, done_s; /* out: seconds after the start of the call */
+} whir_job;
+typedef struct whir_run_stats {
+  double seconds;             /* wall time of the whole call */
+  uint64_t peak_device_bytes; /* largest total held by the workers */
+} whir_run_stats;
+/* A persistent worker pool: workers keep their streams, pinned staging and
+ * prover buffers between runs (the first run on a worker creates them).  One
+ * run at a time per server; honor_arrival as whir_serve. */
+typedef struct whir_server whir_server;
+WHIR_API int whir_server_new(int device, int n_workers, uint64_t device_budget,
+                             whir_server **out);
+WHIR_API int whir_server_run(whir_server *s, whir_job *jobs, int n_jobs, int honor_arrival,
+                             whir_run_stats *stats);
+WHIR_API int whir_server_free(whir_server *s);
+/* one-shot forms on a temporary pool */
+WHIR_API int whir_batch_prove(int device, whir_job *jobs, int n_jobs, int n_workers,
+                              uint64_t device_budget, whir_run_stats *stats);
+WHIR_API int whir_serve(int device, whir_job *jobs, int n_jobs, int n_workers,
+                        uint64_t device_budget, whir_run_stats *stats);
+/* device bytes one worker holds while proving with these parameters */
+WHIR_API int whir_workspace_bytes(const whir_params *params, uint64_t *bytes);
+/* an upper bound of the proof length with n_claims claims (sizes job->proof) */
+WHIR_API int whir_proof_bytes_max(const whir_params *params, int n_claims, uint64_t *bytes);
+/* The admission order of whir_serve with a stand-in for the GPU: job j
+ * occupies a worker for duration_s[j] seconds (a host sleep) and holds
+ * need[j] bytes.  Host only, for testing the scheduling. */
+WHIR_API int whir_serve_simulate(const double *arrival_s, const uint64_t *need,
+                                 const double *duration_s, int n_jobs, int n_workers,
+                                 uint64_t device_budget, double *start_s, double *done_s,
+                                 int32_t *worker, int32_t *status);
+
 /* ---- allocation-free SVO compression.  No counterpart in the reference:
  * an extra entry point for callers that must not allocate device memory (a
  * host whose GPU memory is all owned by its own pool, or code that cannot

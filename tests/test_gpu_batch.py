@@ -1,0 +1,112 @@
+"""Batched and served proving (whir_batch_prove / whir_serve) on the GPU.
+
+Every job's proof must be byte-identical to the same job proved alone by
+the plain prover (and, for the small ones, to the oracle), whichever worker
+ran it and whatever ran beside it.
+"""
+import numpy as np
+import pytest
+
+import whir_gb300 as W
+
+pytestmark = pytest.mark.gpu
+
+
+def mixed_jobs(oracle, seed, n, ks=(10, 12, 14, 16), arrival_gap=0.0):
+    rng = np.random.default_rng(seed)
+    jobs = []
+    for i in range(n):
+        k = int(rng.choice(ks))
+        rate = int(rng.choice([1, 2]))
+        claims = int(rng.integers(1, 5))
+        commit_only = bool(i % 7 == 3)
+        poly = oracle.rand_fe(1000 + seed * 100 + i, 1 << k)
+        jobs.append(W.Job((k, 4, rate, 1, 1, 100), poly, claims=claims,
+                          commit_only=commit_only, arrival_s=i * arrival_gap))
+    return jobs
+
+
+def alone(ctx, job):
+    p = job.params
+    params = (p.k, p.folding, p.rate, p.initial_reduction, p.soundness, p.security_level)
+    if job.commit_only:
+        w = W.Whir(ctx, *params)
+        t = W.PoseidonWriter()
+        w.commit(t, [job.poly], [p.k])
+        cp = t.draw_base()
+        return t.finalize(), cp
+    return W.prove_harness(ctx, params, [job.poly], [p.k], [[0]] * job.claims)
+
+
+def test_batch_matches_alone(ctx, oracle):
+    jobs = mixed_jobs(oracle, 1, 24)
+    W.prove_jobs(jobs, workers=4)
+    for j in jobs:
+        assert j.status == 0
+        proof, cp = alone(ctx, j)
+        assert j.proof == proof
+        assert j.checkpoint == cp
+
+
+def test_batch_matches_oracle(oracle):
+    jobs = mixed_jobs(oracle, 2, 6, ks=(10, 12))
+    W.prove_jobs(jobs, workers=3)
+    for j in jobs:
+        if j.commit_only:
+            continue
+        p = j.params
+        want, wcp = oracle.prove((p.k, p.folding, p.rate, 1, 1, 100), [j.poly], [p.k],
+                                 [[0]] * j.claims)
+        assert j.proof == want and j.checkpoint == wcp
+
+
+def test_served_stream_same_as_batch(oracle):
+    a = mixed_jobs(oracle, 3, 16, arrival_gap=0.004)
+    b = mixed_jobs(oracle, 3, 16)
+    W.prove_jobs(a, workers=4, serve=True)
+    W.prove_jobs(b, workers=2)
+    for x, y in zip(a, b):
+        assert x.status == 0 and y.status == 0
+        assert x.start_s >= x.arrival_s - 1e-3
+        assert x.proof == y.proof and x.checkpoint == y.checkpoint
+
+
+def test_device_resident_inputs(ctx, oracle):
+    jobs = mixed_jobs(oracle, 4, 6, ks=(12, 14))
+    dev = [ctx.to_device(j.poly) for j in jobs]
+    host_proofs = []
+    W.prove_jobs(jobs, workers=2)
+    host_proofs = [(j.proof, j.checkpoint) for j in jobs]
+    for j, d in zip(jobs, dev):
+        j.poly = d
+    W.prove_jobs(jobs, workers=3)
+    for j, hp in zip(jobs, host_proofs):
+        assert (j.proof, j.checkpoint) == hp
+
+
+def test_budget_too_small_fails_job_only(oracle):
+    jobs = mixed_jobs(oracle, 5, 3, ks=(12,))
+    need = W.workspace_bytes(jobs[0].params)
+    big = W.Job((16, 4, 2, 1, 1, 100), oracle.rand_fe(9, 1 << 16), claims=1)
+    W.prove_jobs(jobs + [big], workers=2, budget_bytes=need + (1 << 20))
+    assert all(j.status == 0 for j in jobs)
+    assert big.status == -4
+
+
+def test_server_reuse_across_runs(oracle):
+    srv = W.Server(workers=3)
+    try:
+        a = mixed_jobs(oracle, 6, 10)
+        srv.run(a)
+        b = mixed_jobs(oracle, 6, 10)
+        srv.run(b, serve=True)   # warm workers, arrivals all at 0
+        c = mixed_jobs(oracle, 7, 8, ks=(16, 10))
+        srv.run(c)
+        for x, y in zip(a, b):
+            assert x.status == 0 and x.proof == y.proof and x.checkpoint == y.checkpoint
+        d = mixed_jobs(oracle, 7, 8, ks=(16, 10))
+        W.prove_jobs(d, workers=1)
+        for x, y in zip(c, d):
+            assert x.proof == y.proof and x.checkpoint == y.checkpoint
+    finally:
+        srv.close()

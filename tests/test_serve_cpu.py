@@ -1,0 +1,88 @@
+"""Admission of the batched/served job runner, on the CPU.
+
+whir_serve_simulate runs the same scheduler as whir_serve (arrival order,
+free workers, a device-memory budget over grow-only worker buffers) with a
+host sleep standing in for each proof, so the ordering and memory rules are
+checked without a GPU.
+"""
+import numpy as np
+import pytest
+
+import whir_gb300 as W
+
+
+def held_at_starts(start, need, worker, n_workers):
+    """Total bytes held right after each job starts (buffers only grow)."""
+    order = np.argsort(start, kind="stable")
+    held = np.zeros(n_workers, dtype=np.int64)
+    totals = []
+    for j in order:
+        held[worker[j]] = max(held[worker[j]], need[j])
+        totals.append(held.sum())
+    return totals
+
+
+def test_fifo_and_arrival():
+    rng = np.random.default_rng(3)
+    n = 24
+    arrival = np.sort(rng.uniform(0, 0.05, n))
+    need = rng.integers(1, 10, n)
+    dur = rng.uniform(0.001, 0.01, n)
+    s, e, wk, st = W.serve_simulate(arrival, need, dur, 4, 10 ** 9)
+    assert (st == 0).all()
+    assert (s >= arrival - 1e-4).all()           # nothing starts before it arrives
+    assert (np.diff(s[np.argsort(arrival, kind="stable")]) >= -1e-4).all()  # FIFO
+    assert (e >= s + dur - 1e-4).all()
+    assert set(wk) <= set(range(4))
+
+
+def test_workers_overlap():
+    n = 8
+    s, e, wk, st = W.serve_simulate([0.0] * n, [1] * n, [0.02] * n, 4, 10 ** 9)
+    assert (st == 0).all()
+    # four at a time: the last four start after the first four end
+    assert e.max() < 0.02 * n / 4 + 0.05
+    assert len(set(wk)) == 4
+
+
+def test_budget_bounds_held_bytes():
+    rng = np.random.default_rng(7)
+    n = 30
+    arrival = np.zeros(n)
+    need = rng.integers(10, 60, n)
+    budget = 100
+    s, e, wk, st = W.serve_simulate(arrival, need, [0.002] * n, 6, budget)
+    assert (st == 0).all()
+    assert max(held_at_starts(s, need, wk, 6)) <= budget
+
+
+def test_budget_serialises_when_one_job_fills_it():
+    n = 5
+    s, e, wk, st = W.serve_simulate([0.0] * n, [100] * n, [0.01] * n, 3, 100)
+    assert (st == 0).all()
+    order = np.argsort(s)
+    for a, b in zip(order[:-1], order[1:]):
+        assert s[b] >= e[a] - 1e-4          # never two at once
+    assert len(set(wk)) == 1                 # the first worker keeps the budget
+
+
+def test_job_larger_than_budget_fails_alone():
+    s, e, wk, st = W.serve_simulate([0.0, 0.0, 0.0], [5, 500, 5], [0.001] * 3, 2, 100)
+    assert st[1] == -4                       # WHIR_ERR_CAPACITY
+    assert st[0] == 0 and st[2] == 0
+
+
+def test_workspace_and_proof_bounds():
+    small = W.workspace_bytes((14, 4, 1, 1, 1, 100))
+    big = W.workspace_bytes((24, 4, 2, 1, 1, 100))
+    assert 0 < small < big < 4 << 30
+    assert W.proof_bound((24, 4, 2, 1, 1, 100), 4) > W.proof_bound((24, 4, 2, 1, 1, 100), 1)
+    with pytest.raises(W.WhirError):
+        W.workspace_bytes((3, 4, 1, 1, 1, 100))   # k < folding
+
+
+def test_proof_bound_covers_oracle_proofs(oracle):
+    for (k, f, r, n) in [(10, 4, 1, 1), (12, 2, 1, 3), (13, 3, 2, 4)]:
+        poly = oracle.rand_fe(k, 1 << k)
+        proof, _ = oracle.prove((k, f, r, 1, 1, 100), [poly], [k], [[0]] * n)
+        assert len(proof) <= W.proof_bound((k, f, r, 1, 1, 100), n)

@@ -37,6 +37,21 @@ class Params(ctypes.Structure):
                 ("k", "folding", "rate", "initial_reduction", "soundness", "security_level")]
 
 
+class JobC(ctypes.Structure):
+    """struct whir_job (include/whir_gb300.h)."""
+    _fields_ = [("params", Params), ("poly", ctypes.c_void_p), ("poly_on_device", ctypes.c_int32),
+                ("n_claims", ctypes.c_int32), ("commit_only", ctypes.c_int32),
+                ("arrival_s", ctypes.c_double), ("proof", ctypes.c_void_p),
+                ("proof_cap", ctypes.c_size_t), ("proof_len", ctypes.c_size_t),
+                ("checkpoint", ctypes.c_uint32), ("status", ctypes.c_int32),
+                ("worker", ctypes.c_int32), ("start_s", ctypes.c_double),
+                ("done_s", ctypes.c_double)]
+
+
+class RunStatsC(ctypes.Structure):
+    _fields_ = [("seconds", ctypes.c_double), ("peak_device_bytes", ctypes.c_uint64)]
+
+
 _SIGS = {
     "whir_last_error": (ctypes.c_char_p, []),
     "whir_ctx_create": (ctypes.c_int, [ctypes.c_int, ctypes.POINTER(vp)]),
@@ -86,6 +101,24 @@ _SIGS = {
                                       ctypes.POINTER(ctypes.c_double)]),
     "whir_poseidon2_permute": (ctypes.c_int, [ctypes.c_int, u32p]),
     "whir_random_field": (ctypes.c_int, [ctypes.c_uint64, u32p, ctypes.c_size_t]),
+    "whir_batch_prove": (ctypes.c_int, [ctypes.c_int, ctypes.POINTER(JobC), ctypes.c_int,
+                                        ctypes.c_int, ctypes.c_uint64, ctypes.POINTER(RunStatsC)]),
+    "whir_serve": (ctypes.c_int, [ctypes.c_int, ctypes.POINTER(JobC), ctypes.c_int,
+                                  ctypes.c_int, ctypes.c_uint64, ctypes.POINTER(RunStatsC)]),
+    "whir_server_new": (ctypes.c_int, [ctypes.c_int, ctypes.c_int, ctypes.c_uint64,
+                                       ctypes.POINTER(vp)]),
+    "whir_server_run": (ctypes.c_int, [vp, ctypes.POINTER(JobC), ctypes.c_int, ctypes.c_int,
+                                       ctypes.POINTER(RunStatsC)]),
+    "whir_server_free": (ctypes.c_int, [vp]),
+    "whir_workspace_bytes": (ctypes.c_int, [ctypes.POINTER(Params), ctypes.POINTER(ctypes.c_uint64)]),
+    "whir_proof_bytes_max": (ctypes.c_int, [ctypes.POINTER(Params), ctypes.c_int,
+                                            ctypes.POINTER(ctypes.c_uint64)]),
+    "whir_serve_simulate": (ctypes.c_int, [ctypes.POINTER(ctypes.c_double),
+                                           ctypes.POINTER(ctypes.c_uint64),
+                                           ctypes.POINTER(ctypes.c_double), ctypes.c_int,
+                                           ctypes.c_int, ctypes.c_uint64,
+                                           ctypes.POINTER(ctypes.c_double),
+                                           ctypes.POINTER(ctypes.c_double), i32p, i32p]),
     "whir_counters": (ctypes.c_int, [vp, ctypes.POINTER(ctypes.c_uint64),
                                      ctypes.POINTER(ctypes.c_uint64),
                                      ctypes.POINTER(ctypes.c_uint64)]),
@@ -423,3 +456,146 @@ def prove_harness(ctx, params, polys, poly_k, groups, whir=None):
     w.prove(t, polys, poly_k, groups)
     cp = t.draw_base()
     return t.finalize(), cp
+
+
+class Job:
+    """One proving job for prove_jobs: the harness on one polynomial.
+
+    poly: np.uint32 array of 2^k words (host) or a DeviceArray; claims:
+    number of evaluation claims at transcript-drawn points; commit_only:
+    commitment alone.  After prove_jobs: proof (bytes), checkpoint, status,
+    worker, start_s, done_s, latency_s (done - arrival).
+    """
+
+    def __init__(self, params, poly, claims=1, commit_only=False, arrival_s=0.0):
+        self.params = params if isinstance(params, Params) else Params(*params)
+        self.poly = poly
+        self.claims = claims
+        self.commit_only = commit_only
+        self.arrival_s = arrival_s
+        self.proof = None
+        self.checkpoint = None
+        self.status = None
+        self.worker = None
+        self.start_s = None
+        self.done_s = None
+
+    @property
+    def latency_s(self):
+        return None if self.done_s is None else self.done_s - self.arrival_s
+
+
+def workspace_bytes(params):
+    """Device bytes one worker holds while proving with these parameters."""
+    p = params if isinstance(params, Params) else Params(*params)
+    out = ctypes.c_uint64()
+    _check(lib().whir_workspace_bytes(ctypes.byref(p), ctypes.byref(out)))
+    return out.value
+
+
+def proof_bound(params, claims):
+    """An upper bound of the proof length in bytes (sizes the output buffers)."""
+    p = params if isinstance(params, Params) else Params(*params)
+    out = ctypes.c_uint64()
+    _check(lib().whir_proof_bytes_max(ctypes.byref(p), claims, ctypes.byref(out)))
+    return out.value
+
+
+def _jobs_in(jobs):
+    n = len(jobs)
+    arr = (JobC * max(1, n))()
+    bufs, keep = [], []
+    for i, j in enumerate(jobs):
+        c = arr[i]
+        c.params = j.params
+        if isinstance(j.poly, DeviceArray):
+            c.poly, c.poly_on_device = j.poly.ptr, 1
+        else:
+            a = np.ascontiguousarray(j.poly, np.uint32)
+            if a.size != (1 << j.params.k):
+                raise WhirError("polynomial size does not match params.k")
+            keep.append(a)
+            c.poly, c.poly_on_device = a.ctypes.data, 0
+        c.n_claims = 0 if j.commit_only else j.claims
+        c.commit_only = 1 if j.commit_only else 0
+        c.arrival_s = j.arrival_s
+        cap = 64 if j.commit_only else proof_bound(j.params, j.claims)
+        b = ctypes.create_string_buffer(cap)
+        bufs.append(b)
+        c.proof = ctypes.cast(b, ctypes.c_void_p)
+        c.proof_cap = cap
+    return arr, bufs, keep
+
+
+def _jobs_out(jobs, arr, bufs):
+    for i, j in enumerate(jobs):
+        c = arr[i]
+        j.status = c.status
+        j.worker = c.worker
+        j.start_s, j.done_s = c.start_s, c.done_s
+        j.checkpoint = c.checkpoint
+        j.proof = None
+        if c.status == 0:
+            if c.proof_len > c.proof_cap:
+                raise WhirError("proof longer than its buffer")
+            j.proof = bufs[i].raw[:c.proof_len]
+
+
+class Server:
+    """whir_server: a persistent pool of GPU workers (streams, pinned staging
+    and prover buffers stay allocated between runs)."""
+
+    def __init__(self, workers=8, device=0, budget_bytes=150 << 30):
+        h = vp()
+        _check(lib().whir_server_new(device, workers, budget_bytes, ctypes.byref(h)))
+        self.h = h.value
+        self.workers = workers
+
+    def run(self, jobs, serve=False):
+        """Runs the jobs (serve=True: each released at its arrival_s); fills
+        their results and returns (wall seconds, peak device bytes)."""
+        arr, bufs, keep = _jobs_in(jobs)
+        st = RunStatsC()
+        _check(lib().whir_server_run(self.h, arr, len(jobs), 1 if serve else 0,
+                                     ctypes.byref(st)))
+        _jobs_out(jobs, arr, bufs)
+        return st.seconds, st.peak_device_bytes
+
+    def close(self):
+        if self.h:
+            lib().whir_server_free(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+def prove_jobs(jobs, workers=4, device=0, budget_bytes=150 << 30, serve=False):
+    """whir_batch_prove (serve=False: all jobs released at once) or whir_serve
+    (jobs released at their arrival_s) on a temporary worker pool.  Fills each
+    Job's results; returns (wall seconds, peak device bytes held)."""
+    arr, bufs, keep = _jobs_in(jobs)
+    st = RunStatsC()
+    fn = lib().whir_serve if serve else lib().whir_batch_prove
+    _check(fn(device, arr, len(jobs), workers, budget_bytes, ctypes.byref(st)))
+    _jobs_out(jobs, arr, bufs)
+    return st.seconds, st.peak_device_bytes
+
+
+def serve_simulate(arrival_s, need_bytes, duration_s, workers, budget_bytes):
+    """Admission order of whir_serve with host sleeps standing in for proofs:
+    returns (start_s, done_s, worker, status) arrays."""
+    n = len(arrival_s)
+    A = (ctypes.c_double * max(1, n))(*arrival_s)
+    N = (ctypes.c_uint64 * max(1, n))(*need_bytes)
+    D = (ctypes.c_double * max(1, n))(*duration_s)
+    S = (ctypes.c_double * max(1, n))()
+    E = (ctypes.c_double * max(1, n))()
+    Wk = np.zeros(max(1, n), np.int32)
+    St = np.zeros(max(1, n), np.int32)
+    _check(lib().whir_serve_simulate(A, N, D, n, workers, budget_bytes, S, E,
+                                     Wk.ctypes.data_as(i32p), St.ctypes.data_as(i32p)))
+    return np.array(S[:n]), np.array(E[:n]), Wk[:n], St[:n]

@@ -1,0 +1,212 @@
+// Job runner for batched and served proving (see batch.h).
+#include "batch.h"
+
+#include <algorithm>
+#include <condition_variable>
+#include <memory>
+#include <mutex>
+#include <thread>
+
+namespace whir {
+
+struct Admission::Sync {
+  std::mutex mu;
+  std::condition_variable cv;
+};
+
+Admission::Admission(const std::vector<double> &arrival, const std::vector<size_t> &need,
+                     size_t budget, const std::vector<size_t> &held, bool honor_arrival,
+                     Clock::time_point t0)
+    : arrival_(arrival), need_(need), budget_(budget), honor_(honor_arrival), t0_(t0),
+      held_(held), sync_(new Sync) {
+  order_.resize(arrival.size());
+  for (size_t i = 0; i < order_.size(); i++) order_[i] = i;
+  // ties keep submission order
+  std::stable_sort(order_.begin(), order_.end(),
+                   [&](size_t a, size_t b) { return arrival_[a] < arrival_[b]; });
+  for (size_t h : held_) total_ += h;
+  peak_ = total_;
+}
+
+Admission::~Admission() { delete sync_; }
+
+int Admission::take(int worker, bool *too_big) {
+  std::unique_lock<std::mutex> lock(sync_->mu);
+  *too_big = false;
+  for (;;) {
+    if (head_ >= order_.size()) return -1;
+    size_t j = order_[head_];
+    if (honor_) {
+      auto due = t0_ + std::chrono::duration_cast<Clock::duration>(
+                           std::chrono::duration<double>(arrival_[j]));
+      if (Clock::now() < due) {
+        sync_->cv.wait_until(lock, due);
+        continue;
+      }
+    }
+    if (need_[j] > budget_) {  // can never run: hand it out to be failed
+      head_++;
+      *too_big = true;
+      sync_->cv.notify_all();
+      return (int)j;
+    }
+    // buffers only grow: the worker ends up holding max(held, need)
+    size_t grow = need_[j] > held_[worker] ? need_[j] - held_[worker] : 0;
+    if (total_ + grow <= budget_) {
+      head_++;
+      held_[worker] += grow;
+      total_ += grow;
+      peak_ = std::max(peak_, total_);
+      sync_->cv.notify_all();
+      return (int)j;
+    }
+    sync_->cv.wait(lock);  // a release may free enough
+  }
+}
+
+void Admission::release(int worker, size_t held) {
+  std::lock_guard<std::mutex> lock(sync_->mu);
+  total_ = total_ - held_[worker] + held;
+  held_[worker] = held;
+  peak_ = std::max(peak_, total_);
+  sync_->cv.notify_all();
+}
+
+RunStats run_jobs(std::vector<Job> &jobs, std::vector<void *> &states, std::vector<size_t> &held,
+                  size_t budget, bool honor_arrival,
+                  const std::function<size_t(const Params &)> &need,
+                  const std::function<void *(int worker)> &make_worker,
+                  const std::function<size_t(void *state, Job &job)> &exec) {
+  const int workers = (int)states.size();
+  if (workers < 1 || held.size() != states.size()) throw WhirError(-1, "at least one worker");
+  std::vector<double> arr(jobs.size());
+  std::vector<size_t> nd(jobs.size());
+  for (size_t i = 0; i < jobs.size(); i++) {
+    if (!(jobs[i].arrival >= 0)) throw WhirError(-1, "negative arrival time");
+    arr[i] = jobs[i].arrival;
+    nd[i] = need(jobs[i].params);
+  }
+  auto t0 = Admission::Clock::now();
+  auto secs = [&] {
+    return std::chrono::duration<double>(Admission::Clock::now() - t0).count();
+  };
+  Admission adm(arr, nd, budget, held, honor_arrival, t0);
+  std::vector<std::thread> th;
+  std::vector<std::string> start_err(workers);
+  for (int w = 0; w < workers; w++) {
+    th.emplace_back([&, w] {
+      if (!states[w]) {
+        try {
+          states[w] = make_worker(w);
+        } catch (const std::exception &e) {
+          start_err[w] = e.what();
+        }
+      }
+      void *state = states[w];
+      for (;;) {
+        bool too_big = false;
+        int j = adm.take(w, &too_big);
+        if (j < 0) break;
+        Job &job = jobs[j];
+        job.worker = w;
+        job.start = secs();
+        size_t now_held = adm.held()[w];
+        if (!state) {
+          job.status = -5;
+          job.error = "worker could not start: " + start_err[w];
+          now_held = 0;
+        } else if (too_big) {
+          job.status = -4;
+          job.error = "job needs more device memory than the budget";
+        } else {
+          try {
+            now_held = exec(state, job);
+            job.status = 0;
+          } catch (const WhirError &e) {
+            job.status = e.code;
+            job.error = e.what();
+          } catch (const std::exception &e) {
+            job.status = -5;
+            job.error = e.what();
+          }
+        }
+        job.done = secs();
+        adm.release(w, now_held);
+      }
+    });
+  }
+  for (auto &t : th) t.join();
+  held = adm.held();
+  RunStats st;
+  st.seconds = secs();
+  st.peak_bytes = adm.peak_bytes();
+  return st;
+}
+
+namespace {
+struct GpuWorker {
+  std::unique_ptr<Context> ctx;
+  std::unique_ptr<Prover> prover;
+};
+}  // namespace
+
+struct Server::Lock {
+  std::mutex mu;
+};
+
+Server::Server(int device, int workers, size_t budget)
+    : device_(device), budget_(budget), states_(workers, nullptr), held_(workers, 0),
+      lock_(new Lock) {
+  if (workers < 1 || workers > 256) {
+    delete lock_;
+    throw WhirError(-1, "workers out of range");
+  }
+}
+
+Server::~Server() {
+  for (void *s : states_) {
+    auto *w = static_cast<GpuWorker *>(s);
+    if (!w) continue;
+    cudaSetDevice(device_);
+    if (w->ctx) cudaStreamSynchronize(w->ctx->stream());
+    delete w;
+  }
+  delete lock_;
+}
+
+RunStats Server::run(std::vector<Job> &jobs, bool honor_arrival) {
+  std::lock_guard<std::mutex> guard(lock_->mu);
+  for (auto &j : jobs) {
+    if (!j.poly) throw WhirError(-1, "job without a polynomial");
+    if (j.n_claims < 0 || j.n_claims > 64) throw WhirError(-1, "claims per job out of range");
+    Prover::workspace_bytes(j.params);  // validates the parameters
+  }
+  const int device = device_;
+  auto need = [](const Params &p) { return Prover::workspace_bytes(p); };
+  auto make = [device](int) -> void * {
+    cuda_check(cudaSetDevice(device), "cudaSetDevice");
+    std::unique_ptr<GpuWorker> w(new GpuWorker);
+    w->ctx.reset(new Context(device));
+    return w.release();
+  };
+  auto exec = [device](void *state, Job &job) -> size_t {
+    cuda_check(cudaSetDevice(device), "cudaSetDevice");
+    auto *w = static_cast<GpuWorker *>(state);
+    if (!w->prover) w->prover.reset(new Prover(w->ctx.get(), job.params));
+    else w->prover->set_params(job.params);
+    Transcript ts;
+    std::vector<int> ks{job.params.k};
+    if (job.commit_only) {
+      w->prover->commit(ts, job.poly, job.on_device, ks);
+    } else {
+      std::vector<std::vector<int>> groups(job.n_claims, std::vector<int>{0});
+      w->prover->prove(ts, job.poly, job.on_device, ks, groups);
+    }
+    job.checkpoint = ts.draw_fe();
+    job.proof = ts.bytes();
+    return w->prover->device_bytes();
+  };
+  return run_jobs(jobs, states_, held_, budget_, honor_arrival, need, make, exec);
+}
+
+}  // namespace whir

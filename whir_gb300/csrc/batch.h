@@ -1,0 +1,111 @@
+// Many WHIR proofs on one GPU: a pool of workers, each a host thread with its
+// own stream (Context) and a reusable Prover, so that the kernels of
+// different proofs overlap on the device while each proof waits on its own
+// transcript round trips.  Jobs are released in arrival order; a job is
+// admitted when it has arrived, a worker is free and the device bytes held
+// by all workers stay within a budget.
+//
+// A job is the reference harness (crates/whir/src/test.rs:218-235) on one
+// polynomial: commit, then per claim draw an expanded point and write the
+// evaluation, then open; or the commitment alone.  The proof bytes of a job
+// do not depend on which worker ran it or what ran beside it.
+#pragma once
+#include <stddef.h>
+#include <stdint.h>
+
+#include <chrono>
+#include <functional>
+#include <string>
+#include <vector>
+
+#include "prover.h"
+
+namespace whir {
+
+struct Job {
+  Params params;
+  const uint32_t *poly = nullptr;  // 2^k words, host or device memory
+  bool on_device = false;
+  int n_claims = 0;
+  bool commit_only = false;
+  double arrival = 0;  // seconds after the start of the run
+  // results
+  std::vector<uint8_t> proof;  // transcript bytes (the root is the first 32)
+  uint32_t checkpoint = 0;     // one base element drawn after the proof
+  int status = 0;
+  std::string error;
+  double start = 0, done = 0;  // seconds after the start of the run
+  int worker = -1;
+};
+
+// Release order and memory gate, independent of how a job is executed.
+class Admission {
+ public:
+  using Clock = std::chrono::steady_clock;
+  // need[j]: device bytes a worker holds while running job j; held[w]: bytes
+  // worker w already holds
+  Admission(const std::vector<double> &arrival, const std::vector<size_t> &need, size_t budget,
+            const std::vector<size_t> &held, bool honor_arrival, Clock::time_point t0);
+  ~Admission();
+  Admission(const Admission &) = delete;
+  Admission &operator=(const Admission &) = delete;
+  // Blocks until the next job (in arrival order) may start on `worker`;
+  // returns its index, or -1 when every job has been handed out.  A job whose
+  // need alone exceeds the budget is returned with *too_big set.
+  int take(int worker, bool *too_big);
+  // the worker finished its job and now holds `held` device bytes
+  void release(int worker, size_t held);
+  size_t peak_bytes() const { return peak_; }
+  const std::vector<size_t> &held() const { return held_; }
+
+ private:
+  std::vector<size_t> order_;  // job indices by arrival
+  std::vector<double> arrival_;
+  std::vector<size_t> need_;
+  size_t budget_;
+  bool honor_;
+  Clock::time_point t0_;
+  size_t head_ = 0;
+  std::vector<size_t> held_;  // bytes held per worker
+  size_t total_ = 0, peak_ = 0;
+  struct Sync;
+  Sync *sync_;
+};
+
+struct RunStats {
+  double seconds = 0;
+  size_t peak_bytes = 0;
+};
+
+// Runs `jobs` on one host thread per entry of `states` (a worker's persistent
+// state, created on first use by make_worker on its own thread).  exec(state,
+// job) does the work and returns the device bytes the worker holds
+// afterwards.  held[w] (in/out) is what worker w holds across runs.
+RunStats run_jobs(std::vector<Job> &jobs, std::vector<void *> &states, std::vector<size_t> &held,
+                  size_t budget, bool honor_arrival,
+                  const std::function<size_t(const Params &)> &need,
+                  const std::function<void *(int worker)> &make_worker,
+                  const std::function<size_t(void *state, Job &job)> &exec);
+
+// A pool of GPU workers on one device, kept between runs: each worker's
+// stream, pinned staging and prover buffers stay allocated, so a run starts
+// warm.  One run at a time.
+class Server {
+ public:
+  Server(int device, int workers, size_t budget);
+  ~Server();
+  Server(const Server &) = delete;
+  Server &operator=(const Server &) = delete;
+  RunStats run(std::vector<Job> &jobs, bool honor_arrival);
+  int workers() const { return (int)states_.size(); }
+
+ private:
+  int device_;
+  size_t budget_;
+  std::vector<void *> states_;
+  std::vector<size_t> held_;
+  struct Lock;
+  Lock *lock_;
+};
+
+}  // namespace whir

@@ -4,12 +4,17 @@
 
 #include <string.h>
 
+#include <algorithm>
+#include <chrono>
+#include <thread>
+
 #include <new>
 #include <string>
 #include <vector>
 
 #include "kernels.h"
 #include "poseidon2_host.h"
+#include "batch.h"
 #include "prover.h"
 #include "transcript.h"
 
@@ -537,6 +542,145 @@ int whir_prove(whir_prover *p, whir_transcript *t, const uint32_t *polys, int on
     groups.push_back(ids);
   }
   p->p.prove(t->t, polys, on_device != 0, ks, groups);
+  API_END
+}
+
+static whir::Params params_in(const whir_params *q) {
+  need(q != nullptr, "null parameters");
+  return whir::Params{q->k, q->folding, q->rate, q->initial_reduction, q->soundness,
+                      q->security_level};
+}
+
+struct whir_server {
+  whir::Server s;
+  whir_server(int device, int workers, size_t budget) : s(device, workers, budget) {}
+};
+
+static void run_on(whir::Server &srv, whir_job *jobs, int n_jobs, whir_run_stats *stats,
+                   bool honor_arrival) {
+  need(n_jobs >= 0 && (jobs || n_jobs == 0), "bad job list");
+  std::vector<whir::Job> js(n_jobs);
+  for (int i = 0; i < n_jobs; i++) {
+    const whir_job &q = jobs[i];
+    need(q.poly != nullptr, "job without a polynomial");
+    need(q.proof_cap == 0 || q.proof != nullptr, "proof buffer missing");
+    js[i].params = params_in(&q.params);
+    js[i].poly = q.poly;
+    js[i].on_device = q.poly_on_device != 0;
+    js[i].n_claims = q.commit_only ? 0 : q.n_claims;
+    js[i].commit_only = q.commit_only != 0;
+    js[i].arrival = honor_arrival ? q.arrival_s : 0.0;
+  }
+  whir::RunStats rs = srv.run(js, honor_arrival);
+  for (int i = 0; i < n_jobs; i++) {
+    whir_job &q = jobs[i];
+    const whir::Job &j = js[i];
+    q.proof_len = j.proof.size();
+    if (q.proof) memcpy(q.proof, j.proof.data(), std::min(q.proof_cap, j.proof.size()));
+    q.checkpoint = j.checkpoint;
+    q.status = j.status == 0 ? WHIR_OK
+               : j.status == -2 ? WHIR_ERR_CUDA
+               : j.status == -3 ? WHIR_ERR_NOMEM
+               : j.status == -4 ? WHIR_ERR_CAPACITY
+               : j.status == -5 ? WHIR_ERR_INTERNAL
+                                : WHIR_ERR_ARG;
+    q.worker = j.worker;
+    q.start_s = j.start;
+    q.done_s = j.done;
+  }
+  if (stats) {
+    stats->seconds = rs.seconds;
+    stats->peak_device_bytes = rs.peak_bytes;
+  }
+}
+
+int whir_server_new(int device, int n_workers, uint64_t budget, whir_server **out) {
+  API_BEGIN
+  need(out != nullptr, "null argument");
+  need(n_workers >= 1 && n_workers <= 256, "workers out of range");
+  *out = new whir_server(device, n_workers, (size_t)budget);
+  API_END
+}
+int whir_server_run(whir_server *s, whir_job *jobs, int n_jobs, int honor_arrival,
+                    whir_run_stats *stats) {
+  API_BEGIN
+  need(s != nullptr, "null server");
+  run_on(s->s, jobs, n_jobs, stats, honor_arrival != 0);
+  API_END
+}
+int whir_server_free(whir_server *s) {
+  API_BEGIN
+  delete s;
+  API_END
+}
+
+int whir_batch_prove(int device, whir_job *jobs, int n_jobs, int n_workers, uint64_t budget,
+                     whir_run_stats *stats) {
+  API_BEGIN
+  need(n_workers >= 1 && n_workers <= 256, "workers out of range");
+  whir::Server srv(device, n_workers, (size_t)budget);
+  run_on(srv, jobs, n_jobs, stats, false);
+  API_END
+}
+int whir_serve(int device, whir_job *jobs, int n_jobs, int n_workers, uint64_t budget,
+               whir_run_stats *stats) {
+  API_BEGIN
+  need(n_workers >= 1 && n_workers <= 256, "workers out of range");
+  whir::Server srv(device, n_workers, (size_t)budget);
+  run_on(srv, jobs, n_jobs, stats, true);
+  API_END
+}
+
+int whir_workspace_bytes(const whir_params *params, uint64_t *bytes) {
+  API_BEGIN
+  need(bytes != nullptr, "null argument");
+  *bytes = whir::Prover::workspace_bytes(params_in(params));
+  API_END
+}
+
+int whir_proof_bytes_max(const whir_params *params, int n_claims, uint64_t *bytes) {
+  API_BEGIN
+  need(bytes != nullptr && n_claims >= 0, "bad argument");
+  whir::Params p = params_in(params);
+  whir::Prover::workspace_bytes(p);  // validates
+  *bytes = whir::proof_bytes_max(p, n_claims);
+  API_END
+}
+
+int whir_serve_simulate(const double *arrival_s, const uint64_t *need_b, const double *duration_s,
+                        int n_jobs, int n_workers, uint64_t budget, double *start_s,
+                        double *done_s, int32_t *worker, int32_t *status) {
+  API_BEGIN
+  need(n_jobs >= 0 && n_workers >= 1 && n_workers <= 256, "bad sizes");
+  need(n_jobs == 0 || (arrival_s && need_b && duration_s && start_s && done_s && worker && status),
+       "null argument");
+  std::vector<whir::Job> js(n_jobs);
+  std::vector<size_t> nb(n_jobs);
+  for (int i = 0; i < n_jobs; i++) {
+    need(duration_s[i] >= 0 && duration_s[i] <= 10, "duration out of range");
+    js[i].arrival = arrival_s[i];
+    js[i].params.k = i;  // carries the job index to need()
+    nb[i] = (size_t)need_b[i];
+  }
+  auto needf = [&](const whir::Params &p) { return nb[p.k]; };
+  // a worker's buffers only grow, as a prover's do
+  auto make = [](int) -> void * { return new size_t(0); };
+  auto exec = [&](void *state, whir::Job &j) -> size_t {
+    std::this_thread::sleep_for(std::chrono::duration<double>(duration_s[j.params.k]));
+    size_t *held = static_cast<size_t *>(state);
+    *held = std::max(*held, nb[j.params.k]);
+    return *held;
+  };
+  std::vector<void *> states(n_workers, nullptr);
+  std::vector<size_t> held(n_workers, 0);
+  whir::run_jobs(js, states, held, budget, true, needf, make, exec);
+  for (void *st : states) delete static_cast<size_t *>(st);
+  for (int i = 0; i < n_jobs; i++) {
+    start_s[i] = js[i].start;
+    done_s[i] = js[i].done;
+    worker[i] = js[i].worker;
+    status[i] = js[i].status == 0 ? WHIR_OK : js[i].status == -4 ? WHIR_ERR_CAPACITY : WHIR_ERR_INTERNAL;
+  }
   API_END
 }
 

@@ -17,6 +17,8 @@
 // Each pass reads and writes the matrix once with full 32-byte sectors (a
 // CTA owns 8 columns = 32 bytes of every row it touches).  Zero padding is
 // never materialised: rows >= h_in are read as zero in pass 1.
+#include <mutex>
+
 #include "kernels.h"
 
 namespace whir {
@@ -30,7 +32,7 @@ static const uint32_t ROOT24 = 0x6ac49f88u;  // two_adic_generator(24), canonica
 
 cudaError_t init_poseidon2_tables();
 
-cudaError_t init_device_tables() {
+static cudaError_t upload_device_tables() {
   static uint32_t lo[4096], hi[4096];
   uint32_t w = kb::from_canonical(ROOT24);
   uint32_t w4096 = kb::pow(w, 4096);
@@ -44,6 +46,7 @@ cudaError_t init_device_tables() {
   if (e == cudaSuccess) e = init_poseidon2_tables();
   return e;
 }
+
 
 __device__ __forceinline__ uint32_t root_pow(uint32_t e24) {  // w_24^e, e < 2^24
   return kb::mul(g_tw_lo[e24 & 4095], g_tw_hi[e24 >> 12]);
@@ -343,12 +346,6 @@ static cudaError_t launch_tile_v(const uint32_t *in, uint32_t *out, int S, size_
   while (S + lg < 11 && ((size_t)2 << lg) <= n_outer) lg++;
   size_t rows = (size_t)1 << (S + lg);
   size_t smem = (rows * C + rows) * 4;
-  static bool attr_set = false;
-  if (!attr_set) {
-    cudaFuncSetAttribute(dft_tile_v<C>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                         ((1 << MAX_TILE_LOG) * C + (1 << MAX_TILE_LOG)) * 4);
-    attr_set = true;
-  }
   int threads = (int)(rows * (C / 4) / 8);
   threads = threads < 32 ? 32 : (threads > 256 ? 256 : threads);
   dim3 grid((unsigned)(width / C), (unsigned)(n_outer >> lg));
@@ -369,12 +366,6 @@ static cudaError_t launch_tile(const uint32_t *in, uint32_t *out, int S, size_t 
   while (S + lg < 11 && ((size_t)2 << lg) <= n_outer) lg++;
   size_t rows = (size_t)1 << (S + lg);
   size_t smem = (rows * C + rows) * 4;  // tile + aux (rows >= 2^S)
-  static bool attr_set = false;
-  if (!attr_set) {
-    cudaFuncSetAttribute(dft_tile<C>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                         ((1 << MAX_TILE_LOG) * C + (1 << MAX_TILE_LOG)) * 4);
-    attr_set = true;
-  }
   int threads = (int)(rows * C / 8);
   threads = threads < 32 ? 32 : (threads > 256 ? 256 : threads);
   dim3 grid((unsigned)(width / C), (unsigned)(n_outer >> lg));
@@ -432,6 +423,29 @@ cudaError_t dft_batch(const uint32_t *in, size_t h_in, size_t width, int log_h, 
   cudaError_t e = tile_any(in, scratch, L1, width, h_in, M2, 1, M2, 1, M2, 0, log_h, st);
   if (e != cudaSuccess) return e;
   return tile_any(scratch, out, L2, width, h, M1, M2, 1, 1, M1, 0, 0, st);
+}
+
+static size_t tile_smem_max(int C) { return ((size_t)(1 << MAX_TILE_LOG) * C + (1 << MAX_TILE_LOG)) * 4; }
+
+// Once per process and device; contexts on several host threads may call it.
+cudaError_t init_device_tables() {
+  static std::mutex mu;
+  static bool done[64] = {};
+  int dev = 0;
+  cudaError_t e = cudaGetDevice(&dev);
+  if (e != cudaSuccess) return e;
+  if (dev < 0 || dev >= 64) return cudaErrorInvalidDevice;
+  std::lock_guard<std::mutex> lock(mu);
+  if (done[dev]) return cudaSuccess;
+  e = upload_device_tables();
+  if (e == cudaSuccess) e = cudaFuncSetAttribute(dft_tile<8>, cudaFuncAttributeMaxDynamicSharedMemorySize, tile_smem_max(8));
+  if (e == cudaSuccess) e = cudaFuncSetAttribute(dft_tile<4>, cudaFuncAttributeMaxDynamicSharedMemorySize, tile_smem_max(4));
+  if (e == cudaSuccess) e = cudaFuncSetAttribute(dft_tile<2>, cudaFuncAttributeMaxDynamicSharedMemorySize, tile_smem_max(2));
+  if (e == cudaSuccess) e = cudaFuncSetAttribute(dft_tile<1>, cudaFuncAttributeMaxDynamicSharedMemorySize, tile_smem_max(1));
+  if (e == cudaSuccess) e = cudaFuncSetAttribute(dft_tile_v<8>, cudaFuncAttributeMaxDynamicSharedMemorySize, tile_smem_max(8));
+  if (e == cudaSuccess) e = cudaFuncSetAttribute(dft_tile_v<4>, cudaFuncAttributeMaxDynamicSharedMemorySize, tile_smem_max(4));
+  if (e == cudaSuccess) done[dev] = true;
+  return e;
 }
 
 }  // namespace gpu

@@ -314,6 +314,84 @@ struct LayEntry {
 
 }  // namespace
 
+// crates/whir/src/whir.rs:150-166: the domain, folding and rates of round r
+void round_params(const Params &p, int round, int *kfd, int *this_rate, int *prev_rate) {
+  int prev_red = round == 0 ? 0 : p.initial_reduction + round - 1;
+  int this_red = p.initial_reduction + round;
+  int k_domain = p.rate + p.k - prev_red;
+  *kfd = k_domain - p.folding;
+  *prev_rate = p.rate + round * p.folding - prev_red;
+  *this_rate = p.rate + (round + 1) * p.folding - this_red;
+}
+
+// Device buffers (bytes) a prover holds for one polynomial of 2^p.k
+// evaluations: the base codeword and tree, the two alternating round
+// codewords and trees, the DFT scratch, the sumcheck arrays, and small
+// argument and reduction areas.
+Workspace workspace_plan(const Params &p) {
+  Workspace w;
+  int k = p.k, f = p.folding;
+  size_t cw0_words = ((size_t)1 << (k + p.rate - f)) << f;
+  w.stacked = 4 * ((size_t)1 << k);
+  w.cw0 = 4 * cw0_words;
+  w.tree0 = 4 * gpu::tree_words(k + p.rate - f);
+  int n_rounds, fin;
+  number_of_rounds(f, k, &n_rounds, &fin);
+  size_t max_cw = 16, max_tree = 8;
+  for (int r = 0; r < n_rounds; r++) {
+    int kfd, this_rate, prev_rate;
+    round_params(p, r, &kfd, &this_rate, &prev_rate);
+    int kp = k - f * (r + 1);
+    int log_h = kp + this_rate - f;
+    size_t words = ((size_t)4 << f) << log_h;
+    max_cw = std::max(max_cw, words);
+    max_tree = std::max(max_tree, gpu::tree_words(log_h));
+  }
+  w.scratch = 4 * std::max(cw0_words, max_cw);
+  w.cw = 4 * max_cw;
+  w.tree = 4 * max_tree;
+  w.sumcheck = sizeof(kb::E4) * ((size_t)1 << (k - f));
+  w.eqbuf = sizeof(kb::E4) * (size_t)64 * 8192;
+  w.acc = 8 * 4096;
+  w.small = 1 << 20;
+  w.gather = (size_t)4 * 4096 * (((size_t)4 << f) + 8 * 32);
+  return w;
+}
+
+// Upper bound of the proof length (the byte order of Whir::open,
+// whir.rs:168-359): query hints counted before deduplication.
+size_t proof_bytes_max(const Params &p, int n_claims) {
+  size_t b = 32 + 16 * (size_t)n_claims;
+  b += 16 * (size_t)n_ood_queries(p.soundness, p.security_level, p.k, p.rate, EXT_BITS);
+  b += 32 * (size_t)p.folding;  // SVO rounds
+  int n_rounds, fin;
+  number_of_rounds(p.folding, p.k, &n_rounds, &fin);
+  size_t prev_log_h = (size_t)(p.k + p.rate - p.folding), prev_row = (size_t)1 << p.folding;
+  for (int r = 0; r <= n_rounds; r++) {
+    int kfd, this_rate, prev_rate;
+    round_params(p, r, &kfd, &this_rate, &prev_rate);
+    int kc = p.k - p.folding * (r + 1);
+    if (r < n_rounds) {
+      b += 32 + 16 * (size_t)n_ood_queries(p.soundness, p.security_level, kc, this_rate, EXT_BITS);
+    } else {
+      b += (size_t)16 << fin;  // final polynomial
+    }
+    b += (size_t)n_stir_queries(p.soundness, p.security_level, prev_rate) * 4 *
+         (prev_row + 8 * prev_log_h);
+    if (r < n_rounds) {
+      b += 32 * (size_t)p.folding;
+      prev_log_h = (size_t)(kc + this_rate - p.folding);
+      prev_row = (size_t)4 << p.folding;
+    }
+  }
+  return b;
+}
+
+size_t Workspace::total() const {
+  return stacked + cw0 + tree0 + scratch + 2 * (cw + tree + 2 * sumcheck) + eqbuf + acc + small +
+         gather;
+}
+
 struct Prover::Impl {
   Context *ctx;
   Params p;
@@ -451,49 +529,28 @@ struct Prover::Impl {
 
   // ---- workspace ----
   void reserve() {
-    int k = p.k, f = p.folding;
-    size_t cw0_words = ((size_t)1 << (k + p.rate - f)) << f;
-    stacked.reserve(4 * ((size_t)1 << k));
-    cw0.reserve(4 * cw0_words);
-    tree0.reserve(4 * gpu::tree_words(k + p.rate - f));
-    size_t scratch_words = cw0_words;
-    int n_rounds, fin;
-    number_of_rounds(f, k, &n_rounds, &fin);
-    size_t max_cw = 16, max_tree = 8;
-    for (int r = 0; r < n_rounds; r++) {
-      int kfd, this_rate, prev_rate;
-      round_params(r, &kfd, &this_rate, &prev_rate);
-      int kp = k - f * (r + 1);
-      int log_h = kp + this_rate - f;
-      size_t words = ((size_t)4 << f) << log_h;
-      max_cw = std::max(max_cw, words);
-      max_tree = std::max(max_tree, gpu::tree_words(log_h));
-    }
-    scratch_words = std::max(scratch_words, max_cw);
-    scratch.reserve(4 * scratch_words);
+    Workspace w = workspace_plan(p);
+    stacked.reserve(w.stacked);
+    cw0.reserve(w.cw0);
+    tree0.reserve(w.tree0);
+    scratch.reserve(w.scratch);
     for (int i = 0; i < 2; i++) {
-      cw[i].reserve(4 * max_cw);
-      trees[i].reserve(4 * max_tree);
-      size_t n = (size_t)1 << (k - f);
-      sp[i].reserve(sizeof(E4) * n);
-      sw[i].reserve(sizeof(E4) * n);
+      cw[i].reserve(w.cw);
+      trees[i].reserve(w.tree);
+      sp[i].reserve(w.sumcheck);
+      sw[i].reserve(w.sumcheck);
     }
-    eqbuf.reserve(sizeof(E4) * (size_t)64 * 8192);
+    eqbuf.reserve(w.eqbuf);
     args_pin.reserve((size_t)1 << 20);
     ptsbuf.reserve(64 << 10);
     defer_pin.reserve((size_t)16 << 20);
-    acc.reserve(8 * 4096);
-    small.reserve(1 << 20);
-    gather.reserve((size_t)4 * 4096 * (((size_t)4 << f) + 8 * 32));
+    acc.reserve(w.acc);
+    small.reserve(w.small);
+    gather.reserve(w.gather);
   }
 
   void round_params(int round, int *kfd, int *this_rate, int *prev_rate) const {
-    int prev_red = round == 0 ? 0 : p.initial_reduction + round - 1;
-    int this_red = p.initial_reduction + round;
-    int k_domain = p.rate + p.k - prev_red;
-    *kfd = k_domain - p.folding;
-    *prev_rate = p.rate + round * p.folding - prev_red;
-    *this_rate = p.rate + (round + 1) * p.folding - this_red;
+    whir::round_params(p, round, kfd, this_rate, prev_rate);
   }
 
   // ---- SVO claim (SvoPoint::new + eval, svo.rs:64-91) ----
@@ -1107,13 +1164,29 @@ struct Prover::Impl {
   }
 };
 
-Prover::Prover(Context *ctx, const Params &p) : m_(new Impl), ctx_(ctx), p_(p) {
+static void check_params(const Params &p) {
   if (p.folding < 1 || p.folding > 8 || p.k < p.folding || p.k > 26 || p.rate < 0 ||
       p.rate > 8 || p.initial_reduction < 1 || p.soundness < 0 || p.soundness > 2)
     throw WhirError(-1, "invalid WHIR parameters");
+}
+
+Prover::Prover(Context *ctx, const Params &p) : m_(new Impl), ctx_(ctx), p_(p) {
+  check_params(p);
   m_->ctx = ctx;
   m_->p = p;
   m_->ks = p.folding;
+}
+
+void Prover::set_params(const Params &p) {
+  check_params(p);
+  p_ = p;
+  m_->p = p;
+  m_->ks = p.folding;
+}
+
+size_t Prover::workspace_bytes(const Params &p) {
+  check_params(p);
+  return workspace_plan(p).total();
 }
 Prover::~Prover() { delete m_; }
 

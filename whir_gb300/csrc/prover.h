@@ -34,6 +34,18 @@ constexpr int EXT_BITS = 124;  // bits of |BinomialExtensionField<KoalaBear, 4>|
 
 uint32_t two_adic_generator(int bits);  // Montgomery form
 
+// domain bits, folded-domain bits and rates of WHIR round `round`
+void round_params(const Params &p, int round, int *kfd, int *this_rate, int *prev_rate);
+
+// device buffer sizes (bytes) of one prover for params p
+struct Workspace {
+  size_t stacked, cw0, tree0, scratch, cw, tree, sumcheck, eqbuf, acc, small, gather;
+  size_t total() const;
+};
+Workspace workspace_plan(const Params &p);
+// upper bound of the proof bytes with n_claims claims
+size_t proof_bytes_max(const Params &p, int n_claims);
+
 struct WhirError : std::runtime_error {
   int code;
   WhirError(int c, const std::string &m) : std::runtime_error(m), code(c) {}
@@ -137,6 +149,11 @@ class Prover {
   void prove(Transcript &ts, const uint32_t *polys, bool on_device, const std::vector<int> &poly_k,
              const std::vector<std::vector<int>> &groups);
   size_t device_bytes() const;
+  // re-target the prover at new parameters; device buffers are kept and
+  // grown on the next commit when they are too small
+  void set_params(const Params &p);
+  // device bytes a prover holds after proving with params p
+  static size_t workspace_bytes(const Params &p);
 
  private:
   struct Impl;
