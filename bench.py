@@ -42,9 +42,28 @@ WORKLOAD = dict(k=24, folding=4, rate=2, initial_reduction=1, soundness="Johnson
                 soundness_id=1, security_level=100, claims=4, seed=1)
 METRIC = "proofs/sec and p50/p99 latency, batched/served vs plain, 1 GB300, bit-exact"
 UNIT = "proofs/s"
-# Per-launch DRAM traffic of the dominant kernel from ncu (None until captured);
-# see profiles/ for the capture and its command.
-NCU_TRAFFIC_BYTES = {}
+# Per-launch DRAM traffic (dram__bytes_read.sum + dram__bytes_write.sum) of the
+# kernel classes, from one ncu capture of a full k = 24 proof (the five
+# leaf-hash launches: 1473.0 MB per proof / 5 launches); the capture, its
+# command and the per-launch figures are in profiles/hash_rows_fixed_leaf_hash.md.
+NCU_TRAFFIC_BYTES = {"leaf_hash": 294.6e6}
+NCU_TRAFFIC_K = 24
+
+
+def leaf_permutations(k, folding, rate, initial_reduction):
+    """Width-24 permutations of the leaf hashing of one proof: one per base
+    codeword row, 4 per extension row (64 words), over the commitments of
+    Whir::open's rounds (the round shapes of crates/whir/src/whir.rs:150-166)."""
+    perms = 1 << (k + rate - folding)
+    if k <= 6:
+        return perms
+    nr = (k - 6 + folding - 1) // folding
+    for r in range(nr - 1):
+        this_red = initial_reduction + r
+        this_rate = rate + (r + 1) * folding - this_red
+        kp = k - folding * (r + 1)
+        perms += 4 * (1 << (kp + this_rate - folding))
+    return perms
 
 
 def parse():
@@ -415,7 +434,7 @@ def run_gb300(args):
     d = prof[dom]
     per_launch_ms = d["ms_per_step"] / max(d["launches_per_step"], 1e-9)
     achieved = d["achieved_gbs"]
-    traffic = NCU_TRAFFIC_BYTES.get(dom)
+    traffic = NCU_TRAFFIC_BYTES.get(dom) if k == NCU_TRAFFIC_K else None
     line = {
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": total_ms / args.steps, "higher_is_better": True,
@@ -433,6 +452,14 @@ def run_gb300(args):
                      "peak_source": peak_src, "traffic": traffic,
                      "per_launch_ms": per_launch_ms,
                      "note": "Poseidon2 hashing is integer-pipe bound; frac is against HBM"},
+        "integer_pipe": {
+            "kernel": "leaf_hash",
+            "perm24_per_s": leaf_permutations(k, WORKLOAD["folding"], WORKLOAD["rate"],
+                                              WORKLOAD["initial_reduction"]) /
+                            (prof["leaf_hash"]["ms_per_step"] * 1e-3)
+                            if prof["leaf_hash"]["ms_per_step"] else None,
+            "note": "issue ~68% and FMA-heavy/ALU pipes ~70% busy under ncu "
+                    "(profiles/hash_rows_fixed_leaf_hash.md)"},
         "kernels": prof,
         "gpu_launches": int(launches1 - launches0),
         "clocks": clk,
