@@ -695,20 +695,41 @@ struct Prover::Impl {
     virt.push_back(std::move(v));
   }
 
+  // powers of w^-1 (w = two_adic_generator(k_data)) as lo[e & 2047] * hi[e >> 11],
+  // kept while k_data does not change
+  std::vector<uint32_t> winv_lo, winv_hi;
+  int winv_k = -1;
+  void winv_tables(int k_data) {
+    if (winv_k == k_data) return;
+    uint32_t winv = inv(two_adic_generator(k_data));
+    winv_lo.assign(2048, 0);
+    winv_hi.assign((((size_t)1 << k_data) >> 11) + 1, 0);
+    winv_lo[0] = ONE;
+    for (size_t i = 1; i < winv_lo.size(); i++) winv_lo[i] = mul(winv_lo[i - 1], winv);
+    uint32_t w2048 = mul(winv_lo[2047], winv);
+    winv_hi[0] = ONE;
+    for (size_t i = 1; i < winv_hi.size(); i++) winv_hi[i] = mul(winv_hi[i - 1], w2048);
+    winv_k = k_data;
+  }
+
   // ---- sumcheck arrays on the device ----
   E4 *P() { return sp[ping].as<E4>(); }
   E4 *W() { return sw[ping].as<E4>(); }
 
-  void read_c0c2(E4 *c0, E4 *c2) {
-    unsigned long long *h = (unsigned long long *)ctx->pinned(64);
-    cuda_check(copy_async(*ctx, h, acc.as<unsigned long long>(), 64, cudaMemcpyDeviceToHost),
-               "d2h");
+  // (c0, c2) of the current arrays, applying a pending fold in the same pass;
+  // coeffs_begin queues the pass and the read-back, coeffs_end waits for them
+  // (host work in between overlaps the pass)
+  void coeffs(E4 *c0, E4 *c2) {
+    coeffs_begin();
+    coeffs_end(c0, c2);
+  }
+  void coeffs_end(E4 *c0, E4 *c2) {
+    const unsigned long long *h = (const unsigned long long *)ctx->pinned(64);
     sync();
     *c0 = reduce_acc(h);
     *c2 = reduce_acc(h + 4);
   }
-  // (c0, c2) of the current arrays, applying a pending fold in the same pass
-  void coeffs(E4 *c0, E4 *c2) {
+  void coeffs_begin() {
     unsigned long long *a = acc.as<unsigned long long>();
     cuda_check(cudaMemsetAsync(a, 0, 64, st()), "memset");
     size_t n = (size_t)1 << kc;
@@ -725,7 +746,8 @@ struct Prover::Impl {
                  "round");
       ctx->prof_end(Context::K_SUMCHECK, 2 * 16 * (double)n);
     }
-    read_c0c2(c0, c2);
+    unsigned long long *h = (unsigned long long *)ctx->pinned(64);
+    cuda_check(copy_async(*ctx, h, a, 64, cudaMemcpyDeviceToHost), "d2h");
   }
   void flush() {
     if (!pending) return;
@@ -969,19 +991,23 @@ struct Prover::Impl {
       scales[i] = a;
       a = e_mul(a, alpha);
     }
-    // recursive indexes (prover.rs:483-495) and their row evals at eq(rs),
-    // computed on the device and read after the first round's sync
+    // The recursion g (prover.rs:437-461) of one query index reads, at
+    // round r, g(r, .) at two positions; all of them lie on the 2^d rows
+    // base + t S (S = 2^(k_data - d), base = idx mod S, t < 2^d), the
+    // recursive indexes of prover.rs:483-495.  Per query, G holds g(r, base +
+    // t S) for t < 2^(d-r): G_0 are the row evaluations at eq(rs), and
+    // G_r[t] = combine(G_{r-1}[t], G_{r-1}[t + 2^(d-r)]) once r_{r-1} is
+    // known, in place.  The row evals are computed on the device and read
+    // after the first round's sync.
+    if (k_data < d) throw WhirError(-1, "codeword shorter than the folding");
+    const int lS = k_data - d;
+    const size_t S = (size_t)1 << lS, T = (size_t)1 << d;
     std::vector<size_t> ri;
-    for (int round = 0; round < d; round++) {
-      size_t stride = (size_t)1 << (k_data - round - 1), count = (size_t)1 << (round + 1);
-      for (int i = 0; i < n; i++) {
-        size_t base = idx[i] & (stride - 1);
-        for (size_t t = 0; t < count; t++) ri.push_back(base + t * stride);
-      }
-    }
+    ri.reserve((size_t)n * T);
+    for (int i = 0; i < n; i++)
+      for (size_t t = 0; t < T; t++) ri.push_back((idx[i] & (S - 1)) + t * S);
     std::sort(ri.begin(), ri.end());
     ri.erase(std::unique(ri.begin(), ri.end()), ri.end());
-    std::unordered_map<size_t, E4> evals;
     size_t m = ri.size(), ev_off = 0;
     if (m) {
       size_t need = 4 * m + 16 * m + 64;
@@ -1004,58 +1030,61 @@ struct Prover::Impl {
     uint32_t omega = two_adic_generator(k_data);
     // w^-e for e < 2^k_data as lo[e & 2047] * hi[e >> 11] (w = two_adic_generator(k_data));
     // the level-r generator of g is w^(2^(r-1)), so its inverse powers are w^-(e 2^(r-1))
-    uint32_t winv = inv(omega);
-    std::vector<uint32_t> ilo(2048), ihi((((size_t)1 << k_data) >> 11) + 1);
-    ilo[0] = ONE;
-    for (size_t i = 1; i < ilo.size(); i++) ilo[i] = mul(ilo[i - 1], winv);
-    uint32_t w2048 = mul(ilo[2047], winv);
-    ihi[0] = ONE;
-    for (size_t i = 1; i < ihi.size(); i++) ihi[i] = mul(ihi[i - 1], w2048);
+    winv_tables(k_data);
     const size_t emask = ((size_t)1 << k_data) - 1;
-    auto winv_pow = [&](size_t e) { e &= emask; return mul(ilo[e & 2047], ihi[e >> 11]); };
+    auto winv_pow = [&](size_t e) { e &= emask; return mul(winv_lo[e & 2047], winv_hi[e >> 11]); };
     size_t mid0 = ((size_t)1 << k_data) / 2;
     std::vector<uint32_t> ws(n), tw(n);
     for (int i = 0; i < n; i++) {
       ws[i] = kb::pow(omega, idx[i]);
       tw[i] = winv_pow(idx[i] & (mid0 - 1));
     }
-    uint32_t two_inv = inv(from_canonical(2));
+    const uint32_t two_inv = inv(from_canonical(2));
     std::vector<E4> rc;  // rs of this call
-    // g (prover.rs:437-461), memoised per (round, index)
-    std::unordered_map<uint64_t, E4> memo;
-    std::function<E4(int, size_t)> g = [&](int round, size_t index) -> E4 {
-      if (round == 0) return evals.at(index);
-      uint64_t key = ((uint64_t)round << 48) | index;
-      auto it = memo.find(key);
-      if (it != memo.end()) return it->second;
-      size_t l = (size_t)1 << (k_data - (round - 1)), mid = l / 2;
-      size_t i_lo = index & (mid - 1), i_hi = i_lo + mid;
-      E4 glo = g(round - 1, i_lo), ghi = g(round - 1, i_hi);
-      E4 even = e_scale(e_add(glo, ghi), two_inv);
-      E4 odd = e_scale(e_scale(e_sub(glo, ghi), two_inv), winv_pow(i_lo << (round - 1)));
-      E4 v = e_add(even, e_mul(rc[round - 1], e_sub(odd, even)));
-      memo[key] = v;
-      return v;
-    };
+    std::vector<E4> G((size_t)n * T);
     for (int round = 0; round < d; round++) {
       E4 c0, c2;
-      coeffs(&c0, &c2);
-      if (round == 0) {  // the row evals have landed (prover.rs:426-435)
+      coeffs_begin();
+      if (round == 0) {
+        coeffs_end(&c0, &c2);  // the row evals land with it (prover.rs:426-435)
         const E4 *hv = reinterpret_cast<const E4 *>(defer_ptr(ev_off));
-        evals.reserve(m * 2);
-        for (size_t i = 0; i < m; i++) evals[ri[i]] = hv[i];
-        for (int i = 0; i < n; i++) sum = e_add(sum, e_mul(scales[i], evals.at(idx[i])));
+        for (int i = 0; i < n; i++) {
+          size_t base = idx[i] & (S - 1);
+          for (size_t t = 0; t < T; t++) {
+            size_t pos = std::lower_bound(ri.begin(), ri.end(), base + t * S) - ri.begin();
+            G[(size_t)i * T + t] = hv[pos];
+          }
+          sum = e_add(sum, e_mul(scales[i], G[(size_t)i * T + (idx[i] >> lS)]));
+        }
+      } else {  // G_round from G_(round-1) with r_(round-1)
+        const size_t half = T >> round;
+        const E4 r = rc[round - 1];
+        for (int i = 0; i < n; i++) {
+          E4 *g = &G[(size_t)i * T];
+          size_t base = idx[i] & (S - 1);
+          for (size_t t = 0; t < half; t++) {
+            size_t j = base + t * S;
+            E4 glo = g[t], ghi = g[t + half];
+            E4 even = e_scale(e_add(glo, ghi), two_inv);
+            E4 odd = e_scale(e_sub(glo, ghi), mul(two_inv, winv_pow(j << (round - 1))));
+            g[t] = e_add(even, e_mul(r, e_sub(odd, even)));
+          }
+        }
       }
-      size_t l = (size_t)1 << (k_data - round), mid = l / 2;
+      const size_t hlf = (T >> round) / 2;  // t_hi - t_lo
+      E4 d0 = e_zero(), d2 = e_zero();
       for (int i = 0; i < n; i++) {
-        size_t i_lo = idx[i] & (mid - 1), i_hi = i_lo + mid;
-        E4 glo = g(round, i_lo), ghi = g(round, i_hi);
+        size_t t_lo = (idx[i] >> lS) & (hlf - 1);
+        E4 glo = G[(size_t)i * T + t_lo], ghi = G[(size_t)i * T + t_lo + hlf];
         E4 even = e_scale(e_add(glo, ghi), two_inv);
         E4 odd = e_scale(e_scale(e_sub(glo, ghi), two_inv), tw[i]);
-        c0 = e_add(c0, e_mul(scales[i], even));
+        d0 = e_add(d0, e_mul(scales[i], even));
         uint32_t wt = sub(dbl(ws[i]), ONE);
-        c2 = e_add(c2, e_scale(e_mul(scales[i], e_sub(e_dbl(odd), even)), wt));
+        d2 = e_add(d2, e_scale(e_mul(scales[i], e_sub(e_dbl(odd), even)), wt));
       }
+      if (round > 0) coeffs_end(&c0, &c2);  // the device pass ran meanwhile
+      c0 = e_add(c0, d0);
+      c2 = e_add(c2, d2);
       ts.write_ext(c0);
       ts.write_ext(c2);
       E4 r = ts.draw_ext();
