@@ -182,11 +182,15 @@ RunStats Server::run(std::vector<Job> &jobs, bool honor_arrival) {
     Prover::workspace_bytes(j.params);  // validates the parameters
   }
   const int device = device_;
+  // more than one worker: poll-and-yield waits, so that workers waiting on
+  // the GPU leave the host cores to the workers that have host work
+  const bool yield = states_.size() > 1;
   auto need = [](const Params &p) { return Prover::workspace_bytes(p); };
-  auto make = [device](int) -> void * {
+  auto make = [device, yield](int) -> void * {
     cuda_check(cudaSetDevice(device), "cudaSetDevice");
     std::unique_ptr<GpuWorker> w(new GpuWorker);
     w->ctx.reset(new Context(device));
+    w->ctx->set_yield_wait(yield);
     return w.release();
   };
   auto exec = [device](void *state, Job &job) -> size_t {

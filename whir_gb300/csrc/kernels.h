@@ -85,6 +85,21 @@ cudaError_t sumcheck_round(const kb::E4 *p_in, const kb::E4 *w_in, size_t n_in, 
 cudaError_t eval_ext(const kb::E4 *poly, int k, const kb::E4 *eq_lo, int s_lo,
                      const kb::E4 *eq_hi, unsigned long long *acc, cudaStream_t st);
 // out[q] = <eq(rs), row(idx[q])> over base rows (fold_with_code evals, prover.rs:497-506)
+// fold_with_code's per-query state on the device (see code_round_kernel)
+struct CodeState {
+  const uint32_t *idx;  // n query indexes
+  kb::E4 *G;            // n * 2^d values of g
+  kb::E4 *scales;       // n
+  uint32_t *ws, *tw, *B;  // n each
+  const uint32_t *wd;   // 2^d powers of w^-S
+  int n, d, k_data;
+  uint32_t omega, winv, two_inv;  // w, w^-1 (w = two_adic_generator(k_data)), 1/2
+};
+// round r: G update with r_prev (r >= 1), then this round's part of (c0, c2)
+// added to acc[0..8) (and, at round 0, the sum term to acc[8..12))
+cudaError_t code_round(const CodeState &s, int round, kb::E4 r_prev, unsigned long long *acc,
+                       cudaStream_t st);
+cudaError_t code_finish(const CodeState &s, kb::E4 r_last, cudaStream_t st);
 cudaError_t row_evals(const uint32_t *rows, int row_len, const uint32_t *idx, int n,
                       const Point &rs, kb::E4 *out, cudaStream_t st);
 

@@ -8,6 +8,7 @@
 #include <chrono>
 #include <functional>
 #include <map>
+#include <thread>
 #include <unordered_map>
 
 namespace whir {
@@ -110,13 +111,26 @@ void *Context::pinned(size_t bytes) {
   }
   return pinned_;
 }
-void Context::sync() {
-  if (!prof_) {
+void Context::wait_stream() {
+  if (!yield_) {
     cuda_check(cudaStreamSynchronize(stream_), "stream sync");
     return;
   }
+  // poll, giving the core to other runnable threads between polls
+  for (;;) {
+    cudaError_t e = cudaStreamQuery(stream_);
+    if (e == cudaSuccess) return;
+    if (e != cudaErrorNotReady) cuda_check(e, "stream sync");
+    std::this_thread::yield();
+  }
+}
+void Context::sync() {
+  if (!prof_) {
+    wait_stream();
+    return;
+  }
   auto t0 = std::chrono::steady_clock::now();
-  cuda_check(cudaStreamSynchronize(stream_), "stream sync");
+  wait_stream();
   acc_ms_[K_SYNC] += std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t0).count();
   acc_n_[K_SYNC] += 1;
 }
@@ -403,7 +417,7 @@ struct Prover::Impl {
   std::vector<size_t> poly_off;  // word offset of each poly inside the stacked poly
   // device memory
   DeviceBuffer stacked, cw0, tree0, scratch, cw[2], trees[2], sp[2], sw[2], eqbuf, acc, small,
-      gather, ptsbuf;
+      gather, ptsbuf, codebuf;
   DeviceTree t0, tr[2];
   int cur_tree = -1;  // index into tr of the latest round commitment
   std::vector<std::vector<uint32_t>> svo_eq;  // per round: eq tables of the {0,1,2} grid
@@ -695,23 +709,6 @@ struct Prover::Impl {
     virt.push_back(std::move(v));
   }
 
-  // powers of w^-1 (w = two_adic_generator(k_data)) as lo[e & 2047] * hi[e >> 11],
-  // kept while k_data does not change
-  std::vector<uint32_t> winv_lo, winv_hi;
-  int winv_k = -1;
-  void winv_tables(int k_data) {
-    if (winv_k == k_data) return;
-    uint32_t winv = inv(two_adic_generator(k_data));
-    winv_lo.assign(2048, 0);
-    winv_hi.assign((((size_t)1 << k_data) >> 11) + 1, 0);
-    winv_lo[0] = ONE;
-    for (size_t i = 1; i < winv_lo.size(); i++) winv_lo[i] = mul(winv_lo[i - 1], winv);
-    uint32_t w2048 = mul(winv_lo[2047], winv);
-    winv_hi[0] = ONE;
-    for (size_t i = 1; i < winv_hi.size(); i++) winv_hi[i] = mul(winv_hi[i - 1], w2048);
-    winv_k = k_data;
-  }
-
   // ---- sumcheck arrays on the device ----
   E4 *P() { return sp[ping].as<E4>(); }
   E4 *W() { return sw[ping].as<E4>(); }
@@ -723,15 +720,19 @@ struct Prover::Impl {
     coeffs_begin();
     coeffs_end(c0, c2);
   }
-  void coeffs_end(E4 *c0, E4 *c2) {
-    const unsigned long long *h = (const unsigned long long *)ctx->pinned(64);
+  void coeffs_end(E4 *c0, E4 *c2, E4 *extra = nullptr) {
+    const unsigned long long *h = (const unsigned long long *)ctx->pinned(128);
     sync();
     *c0 = reduce_acc(h);
     *c2 = reduce_acc(h + 4);
+    if (extra) *extra = reduce_acc(h + 8);
   }
-  void coeffs_begin() {
+  // code: fold_with_code's per-query pass of this round, added into the same
+  // slots (and its round-0 sum term into slots 8..12)
+  void coeffs_begin(const gpu::CodeState *code = nullptr, int code_round = 0,
+                    E4 code_r = E4{}) {
     unsigned long long *a = acc.as<unsigned long long>();
-    cuda_check(cudaMemsetAsync(a, 0, 64, st()), "memset");
+    cuda_check(cudaMemsetAsync(a, 0, 96, st()), "memset");
     size_t n = (size_t)1 << kc;
     ctx->prof_begin(Context::K_SUMCHECK);
     if (pending) {
@@ -746,8 +747,9 @@ struct Prover::Impl {
                  "round");
       ctx->prof_end(Context::K_SUMCHECK, 2 * 16 * (double)n);
     }
-    unsigned long long *h = (unsigned long long *)ctx->pinned(64);
-    cuda_check(copy_async(*ctx, h, a, 64, cudaMemcpyDeviceToHost), "d2h");
+    if (code) cuda_check(gpu::code_round(*code, code_round, code_r, a, st()), "code_round");
+    unsigned long long *h = (unsigned long long *)ctx->pinned(128);
+    cuda_check(copy_async(*ctx, h, a, 96, cudaMemcpyDeviceToHost), "d2h");
   }
   void flush() {
     if (!pending) return;
@@ -803,6 +805,14 @@ struct Prover::Impl {
     cuda_check(gpu::add_pows(W(), kc, (const uint32_t *)(small.as<uint8_t>() + scales.size() * 16),
                              small.as<E4>(), (int)vars.size(), eqbuf.as<uint32_t>(), st()),
                "add_pows");
+  }
+
+  // add_pows with vars and scales already on the device
+  void add_pows_dev(const uint32_t *vars, const E4 *scales, int n) {
+    if (n == 0) return;
+    size_t tw = gpu::add_pows_scratch_words(kc, n);
+    if (4 * tw > eqbuf.bytes()) eqbuf.reserve(4 * tw);
+    cuda_check(gpu::add_pows(W(), kc, vars, scales, n, eqbuf.as<uint32_t>(), st()), "add_pows");
   }
 
   // ---- new_prover (prover.rs:280-354) incl. expression (185-229) ----
@@ -991,116 +1001,78 @@ struct Prover::Impl {
       scales[i] = a;
       a = e_mul(a, alpha);
     }
-    // The recursion g (prover.rs:437-461) of one query index reads, at
-    // round r, g(r, .) at two positions; all of them lie on the 2^d rows
-    // base + t S (S = 2^(k_data - d), base = idx mod S, t < 2^d), the
-    // recursive indexes of prover.rs:483-495.  Per query, G holds g(r, base +
-    // t S) for t < 2^(d-r): G_0 are the row evaluations at eq(rs), and
-    // G_r[t] = combine(G_{r-1}[t], G_{r-1}[t + 2^(d-r)]) once r_{r-1} is
-    // known, in place.  The row evals are computed on the device and read
-    // after the first round's sync.
+    // The recursion g (prover.rs:437-461) of one query reads, at round r,
+    // g(r, .) at two positions; all of them lie on the 2^d rows base + t S
+    // (S = 2^(k_data - d), base = idx mod S, t < 2^d), the recursive indexes
+    // of prover.rs:483-495.  The device keeps g per query and folds it round
+    // by round (gpu::code_round); the round's part of (c0, c2) lands in the
+    // same reduction slots as the expression's, so the host reads them with
+    // one sync per round as in a plain round.
     if (k_data < d) throw WhirError(-1, "codeword shorter than the folding");
     const int lS = k_data - d;
     const size_t S = (size_t)1 << lS, T = (size_t)1 << d;
-    std::vector<size_t> ri;
-    ri.reserve((size_t)n * T);
-    for (int i = 0; i < n; i++)
-      for (size_t t = 0; t < T; t++) ri.push_back((idx[i] & (S - 1)) + t * S);
-    std::sort(ri.begin(), ri.end());
-    ri.erase(std::unique(ri.begin(), ri.end()), ri.end());
-    size_t m = ri.size(), ev_off = 0;
-    if (m) {
-      size_t need = 4 * m + 16 * m + 64;
-      if (need > gather.bytes()) {
-        sync();
-        gather.reserve(2 * need);
-      }
-      std::vector<uint32_t> h(m);
-      for (size_t i = 0; i < m; i++) h[i] = (uint32_t)ri[i];
-      uint32_t *didx = gather.as<uint32_t>();
-      E4 *dout = reinterpret_cast<E4 *>(didx + ((m + 3) & ~(size_t)3));
-      upload(didx, h.data(), 4 * m);
-      gpu::Point rsp;
-      rsp.k = (int)rs.size();
-      for (size_t i = 0; i < rs.size(); i++) rsp.z[i] = rs[i];
-      cuda_check(gpu::row_evals(t0.rows, t0.row_len, didx, (int)m, rsp, dout, st()), "row_evals");
-      ev_off = defer_alloc(4 * m, ts);
-      cuda_check(copy_async(*ctx, defer_ptr(ev_off), dout, 16 * m, cudaMemcpyDeviceToHost), "d2h");
+    gpu::CodeState cs;
+    cs.n = n;
+    cs.d = d;
+    cs.k_data = k_data;
+    cs.omega = two_adic_generator(k_data);
+    cs.winv = inv(cs.omega);
+    cs.two_inv = inv(from_canonical(2));
+    // device layout in codebuf: G | scales | idx | ws | tw | B | wd | row list
+    size_t g_bytes = 16 * (size_t)n * T, sc_bytes = 16 * (size_t)n, u_bytes = 4 * (((size_t)n + 3) & ~(size_t)3);
+    size_t wd_bytes = 4 * ((T + 3) & ~(size_t)3), rl_bytes = 4 * (size_t)n * T;
+    size_t need = g_bytes + sc_bytes + 4 * u_bytes + wd_bytes + rl_bytes + 64;
+    if (need > codebuf.bytes()) {
+      sync();
+      codebuf.reserve(2 * need);
     }
-    uint32_t omega = two_adic_generator(k_data);
-    // w^-e for e < 2^k_data as lo[e & 2047] * hi[e >> 11] (w = two_adic_generator(k_data));
-    // the level-r generator of g is w^(2^(r-1)), so its inverse powers are w^-(e 2^(r-1))
-    winv_tables(k_data);
-    const size_t emask = ((size_t)1 << k_data) - 1;
-    auto winv_pow = [&](size_t e) { e &= emask; return mul(winv_lo[e & 2047], winv_hi[e >> 11]); };
-    size_t mid0 = ((size_t)1 << k_data) / 2;
-    std::vector<uint32_t> ws(n), tw(n);
-    for (int i = 0; i < n; i++) {
-      ws[i] = kb::pow(omega, idx[i]);
-      tw[i] = winv_pow(idx[i] & (mid0 - 1));
-    }
-    const uint32_t two_inv = inv(from_canonical(2));
-    std::vector<E4> rc;  // rs of this call
-    std::vector<E4> G((size_t)n * T);
-    for (int round = 0; round < d; round++) {
-      E4 c0, c2;
-      coeffs_begin();
-      if (round == 0) {
-        coeffs_end(&c0, &c2);  // the row evals land with it (prover.rs:426-435)
-        const E4 *hv = reinterpret_cast<const E4 *>(defer_ptr(ev_off));
-        for (int i = 0; i < n; i++) {
-          size_t base = idx[i] & (S - 1);
-          for (size_t t = 0; t < T; t++) {
-            size_t pos = std::lower_bound(ri.begin(), ri.end(), base + t * S) - ri.begin();
-            G[(size_t)i * T + t] = hv[pos];
-          }
-          sum = e_add(sum, e_mul(scales[i], G[(size_t)i * T + (idx[i] >> lS)]));
-        }
-      } else {  // G_round from G_(round-1) with r_(round-1)
-        const size_t half = T >> round;
-        const E4 r = rc[round - 1];
-        for (int i = 0; i < n; i++) {
-          E4 *g = &G[(size_t)i * T];
-          size_t base = idx[i] & (S - 1);
-          for (size_t t = 0; t < half; t++) {
-            size_t j = base + t * S;
-            E4 glo = g[t], ghi = g[t + half];
-            E4 even = e_scale(e_add(glo, ghi), two_inv);
-            E4 odd = e_scale(e_sub(glo, ghi), mul(two_inv, winv_pow(j << (round - 1))));
-            g[t] = e_add(even, e_mul(r, e_sub(odd, even)));
-          }
-        }
-      }
-      const size_t hlf = (T >> round) / 2;  // t_hi - t_lo
-      E4 d0 = e_zero(), d2 = e_zero();
+    uint8_t *cb = codebuf.as<uint8_t>();
+    cs.G = reinterpret_cast<E4 *>(cb);
+    cs.scales = reinterpret_cast<E4 *>(cb + g_bytes);
+    uint32_t *didx = reinterpret_cast<uint32_t *>(cb + g_bytes + sc_bytes);
+    cs.idx = didx;
+    cs.ws = didx + u_bytes / 4;
+    cs.tw = cs.ws + u_bytes / 4;
+    cs.B = cs.tw + u_bytes / 4;
+    uint32_t *dwd = cs.B + u_bytes / 4;
+    cs.wd = dwd;
+    uint32_t *drows = dwd + wd_bytes / 4;
+    {
+      std::vector<uint32_t> h((size_t)n * T), hi(n), hw(T);
       for (int i = 0; i < n; i++) {
-        size_t t_lo = (idx[i] >> lS) & (hlf - 1);
-        E4 glo = G[(size_t)i * T + t_lo], ghi = G[(size_t)i * T + t_lo + hlf];
-        E4 even = e_scale(e_add(glo, ghi), two_inv);
-        E4 odd = e_scale(e_scale(e_sub(glo, ghi), two_inv), tw[i]);
-        d0 = e_add(d0, e_mul(scales[i], even));
-        uint32_t wt = sub(dbl(ws[i]), ONE);
-        d2 = e_add(d2, e_scale(e_mul(scales[i], e_sub(e_dbl(odd), even)), wt));
+        hi[i] = (uint32_t)idx[i];
+        for (size_t t = 0; t < T; t++) h[(size_t)i * T + t] = (uint32_t)((idx[i] & (S - 1)) + t * S);
       }
-      if (round > 0) coeffs_end(&c0, &c2);  // the device pass ran meanwhile
-      c0 = e_add(c0, d0);
-      c2 = e_add(c2, d2);
+      uint32_t wd = kb::pow(cs.winv, S);
+      hw[0] = ONE;
+      for (size_t t = 1; t < T; t++) hw[t] = mul(hw[t - 1], wd);
+      upload(drows, h.data(), 4 * h.size());
+      upload(didx, hi.data(), 4 * (size_t)n);
+      upload(dwd, hw.data(), 4 * T);
+      upload(cs.scales, scales.data(), 16 * (size_t)n);
+    }
+    gpu::Point rsp;
+    rsp.k = (int)rs.size();
+    for (size_t i = 0; i < rs.size(); i++) rsp.z[i] = rs[i];
+    // G_0: row evaluations at eq(rs), written in place (query-major)
+    cuda_check(gpu::row_evals(t0.rows, t0.row_len, drows, (int)((size_t)n * T), rsp, cs.G, st()),
+               "row_evals");
+    std::vector<E4> rc;  // rs of this call
+    for (int round = 0; round < d; round++) {
+      E4 c0, c2, sum_add;
+      coeffs_begin(&cs, round, round ? rc[round - 1] : e_zero());
+      coeffs_end(&c0, &c2, &sum_add);
+      if (round == 0) sum = e_add(sum, sum_add);  // prover.rs:426-435
       ts.write_ext(c0);
       ts.write_ext(c2);
       E4 r = ts.draw_ext();
       sum = extrapolate012(c0, e_sub(sum, c0), c2, r);
       rc.push_back(r);
       defer_fold(r);
-      for (int i = 0; i < n; i++) {
-        E4 f = e_add(e_one(), e_mul(r, e_add(e_neg(e_one()), e_from(ws[i]))));
-        scales[i] = e_mul(scales[i], f);
-        ws[i] = mul(ws[i], ws[i]);
-        tw[i] = mul(tw[i], tw[i]);
-        if ((idx[i] >> (k_data - round - 2)) & 1) tw[i] = neg(tw[i]);
-      }
     }
+    cuda_check(gpu::code_finish(cs, rc.back(), st()), "code_finish");
     flush();
-    add_pows(ws, scales);  // combine_pows_scaled (combine.rs:441-468)
+    add_pows_dev(cs.ws, cs.scales, n);  // combine_pows_scaled (combine.rs:441-468)
     for (auto &r : rc) rs.push_back(r);
     return rc;
   }
@@ -1224,7 +1196,8 @@ size_t Prover::device_bytes() const {
   const DeviceBuffer *bufs[] = {&m_->stacked, &m_->cw0,   &m_->tree0,  &m_->scratch,
                                 &m_->cw[0],   &m_->cw[1], &m_->trees[0], &m_->trees[1],
                                 &m_->sp[0],   &m_->sp[1], &m_->sw[0],  &m_->sw[1],
-                                &m_->eqbuf,   &m_->acc,   &m_->small,  &m_->gather};
+                                &m_->eqbuf,   &m_->acc,   &m_->small,  &m_->gather,
+                                &m_->codebuf};
   for (auto b : bufs) s += b->bytes();
   return s;
 }

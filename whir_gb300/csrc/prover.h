@@ -78,6 +78,10 @@ class Context {
   cudaStream_t stream() const { return stream_; }
   void *pinned(size_t bytes);  // staging for D2H results and H2D arguments
   void sync();
+  // Waiting for the stream: a blocking synchronise (lowest latency, keeps a
+  // core busy), or polling with a yield between polls so that many worker
+  // threads can share the host cores.
+  void set_yield_wait(bool on) { yield_ = on; }
   // per-kernel-class CUDA-event timing on this stream
   // kernel classes timed with events, and K_SYNC: host time blocked in sync()
   enum Klass { K_DFT = 0, K_LEAF = 1, K_TREE = 2, K_SUMCHECK = 3, K_SYNC = 4, K_NCLASS = 5 };
@@ -92,7 +96,9 @@ class Context {
   unsigned long long d2h_bytes() const { return d2h_bytes_; }
 
  private:
+  void wait_stream();
   int device_;
+  bool yield_ = false;
   cudaStream_t stream_ = nullptr;
   void *pinned_ = nullptr;
   size_t pinned_bytes_ = 0;

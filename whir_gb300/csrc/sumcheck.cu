@@ -380,5 +380,107 @@ cudaError_t row_evals(const uint32_t *rows, int row_len, const uint32_t *idx, in
   return cudaGetLastError();
 }
 
+// ---- fold_with_code's code part (crates/whir/src/sumcheck/prover.rs:400-561) ----
+// Query i keeps G[i T .. i T + 2^(d-r)) = g(r, base_i + t S) (S = 2^(k_data -
+// d), base_i = idx_i mod S, T = 2^d): round 0 holds the row evaluations at
+// eq(rs); round r >= 1 folds G with r_(r-1) (prover.rs:437-461), the
+// twiddle of position t being B_i wd^(t 2^(r-1)) with B_i = w^-(base_i
+// 2^(r-1)) and wd = w^-S.  Each query adds its part of (c0, c2)
+// (prover.rs:503-536) to acc[0..8) and, at round 0, scales_i g(0, idx_i) to
+// acc[8..12), as canonical words; the host reduces them with the round pass.
+__device__ __forceinline__ void acc_add_e4(unsigned long long *acc, const E4 &v) {
+#pragma unroll
+  for (int c = 0; c < 4; c++) atomicAdd(acc + c, (unsigned long long)v.c[c]);
+}
+
+__global__ void __launch_bounds__(32) code_round_kernel(CodeState s, int round, E4 r_prev,
+                                                        unsigned long long *acc) {
+  using namespace kb;
+  const int i = blockIdx.x;
+  const int lS = s.k_data - s.d;
+  const int T = 1 << s.d;
+  const uint32_t idx = s.idx[i];
+  const uint32_t base = idx & ((1u << lS) - 1u), tb = idx >> lS;
+  E4 *G = s.G + (size_t)i * T;
+  __shared__ uint32_t pw[3];
+  if (round == 0) {
+    // w^idx, w^-(idx mod 2^(k_data-1)), w^-base: one exponentiation per lane
+    if (threadIdx.x < 3) {
+      uint32_t b = threadIdx.x == 0 ? s.omega : s.winv;
+      uint32_t e = threadIdx.x == 0 ? idx
+                   : threadIdx.x == 1 ? (idx & ((1u << (s.k_data - 1)) - 1u))
+                                      : base;
+      pw[threadIdx.x] = kb::pow(b, e);
+    }
+    __syncthreads();
+    if (threadIdx.x != 0) return;
+    E4 sc = s.scales[i];
+    s.ws[i] = pw[0];
+    s.tw[i] = pw[1];
+    s.B[i] = pw[2];
+    acc_add_e4(acc + 8, e_mul(sc, G[tb]));
+  } else {
+    const int half = T >> round;
+    const uint32_t B = s.B[i];
+    for (int t = threadIdx.x; t < half; t += blockDim.x) {
+      uint32_t tw = mul(B, s.wd[(t << (round - 1)) & (T - 1)]);
+      E4 glo = G[t], ghi = G[t + half];
+      E4 even = e_scale(e_add(glo, ghi), s.two_inv);
+      E4 odd = e_scale(e_sub(glo, ghi), mul(s.two_inv, tw));
+      G[t] = e_add(even, e_mul(r_prev, e_sub(odd, even)));
+    }
+    __syncthreads();
+    if (threadIdx.x != 0) return;
+    // the updates after round r-1 (prover.rs:542-553)
+    uint32_t ws = s.ws[i], tw = s.tw[i];
+    E4 f = e_add(e_one(), e_mul(r_prev, e_add(e_neg(e_one()), e_from(ws))));
+    s.scales[i] = e_mul(s.scales[i], f);
+    ws = mul(ws, ws);
+    tw = mul(tw, tw);
+    if ((idx >> (s.k_data - round - 1)) & 1u) tw = neg(tw);
+    s.ws[i] = ws;
+    s.tw[i] = tw;
+    s.B[i] = mul(B, B);
+  }
+  const E4 sc = s.scales[i];
+  const uint32_t ws = s.ws[i], tw = s.tw[i];
+  const int hlf = (T >> round) / 2;
+  const uint32_t tl = tb & (uint32_t)(hlf - 1);
+  E4 glo = G[tl], ghi = G[tl + hlf];
+  E4 even = e_scale(e_add(glo, ghi), s.two_inv);
+  E4 odd = e_scale(e_scale(e_sub(glo, ghi), s.two_inv), tw);
+  acc_add_e4(acc, e_mul(sc, even));
+  uint32_t wt = sub(dbl(ws), ONE);
+  acc_add_e4(acc + 4, e_scale(e_mul(sc, e_sub(e_dbl(odd), even)), wt));
+}
+
+// the updates after the last round, before combine_pows_scaled (combine.rs:441-468)
+__global__ void code_finish_kernel(CodeState s, E4 r_last) {
+  using namespace kb;
+  int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= s.n) return;
+  uint32_t ws = s.ws[i];
+  E4 f = e_add(e_one(), e_mul(r_last, e_add(e_neg(e_one()), e_from(ws))));
+  s.scales[i] = e_mul(s.scales[i], f);
+  s.ws[i] = mul(ws, ws);
+}
+
+cudaError_t code_round(const CodeState &s, int round, E4 r_prev, unsigned long long *acc,
+                       cudaStream_t st) {
+  if (s.n == 0) return cudaSuccess;
+  if (s.d < 1 || s.d > 8 || s.k_data < s.d || s.k_data > 30 || round < 0 || round >= s.d)
+    return cudaErrorInvalidValue;
+  code_round_kernel<<<s.n, 32, 0, st>>>(s, round, r_prev, acc);
+  count_launches(1);
+  return cudaGetLastError();
+}
+
+cudaError_t code_finish(const CodeState &s, E4 r_last, cudaStream_t st) {
+  if (s.n == 0) return cudaSuccess;
+  code_finish_kernel<<<(s.n + 127) / 128, 128, 0, st>>>(s, r_last);
+  count_launches(1);
+  return cudaGetLastError();
+}
+
 }  // namespace gpu
 }  // namespace whir
