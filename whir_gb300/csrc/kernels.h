@@ -11,6 +11,17 @@
 namespace whir {
 namespace gpu {
 
+// Where a reduction's result goes.  With host set, the last CTA of the
+// reducing launch copies acc[0..words) to host (pinned memory the device can
+// write), then zeroes those words and the counter, so the next reduction
+// starts from zero without a memset and the host reads the result after a
+// stream sync without a copy.  Without host, acc keeps the sums.
+struct Publish {
+  unsigned int *counter = nullptr;
+  unsigned long long *host = nullptr;
+  int words = 0;
+};
+
 // ---- kernel launches issued by this library (all contexts), for reporting ----
 unsigned long long launch_count();
 void count_launches(unsigned n);
@@ -31,7 +42,8 @@ cudaError_t hash_rows(const uint32_t *rows, size_t n_rows, int row_len, uint32_t
                       cudaStream_t st);
 // all levels above the leaves: level l+1 node i = C(level l node i, node i + n/2)
 // nodes: level 0 (2^log_h digests) first, then each level in turn
-cudaError_t build_tree(uint32_t *nodes, int log_h, cudaStream_t st);
+// host_root (optional, device-writable host memory): the root is also written there
+cudaError_t build_tree(uint32_t *nodes, int log_h, cudaStream_t st, uint32_t *host_root = nullptr);
 // per query: the leaf row then log_h sibling digests bottom-up
 cudaError_t gather_openings(const uint32_t *rows, int row_len, const uint32_t *nodes, int log_h,
                             const uint32_t *idx, int n, uint32_t *out, cudaStream_t st);
@@ -62,7 +74,8 @@ cudaError_t eq_full(const Point &z, kb::E4 scale, kb::E4 *out, kb::E4 *tmp, cuda
 // acc[j] += sum_h eq(zrest)[h] * P[h * 2^ks + j]; acc is u64[2^ks][4] of
 // unreduced canonical sums (reduce mod p on read).  eq tables from eq_split.
 cudaError_t compress_hi(const uint32_t *poly, int k, int ks, const kb::E4 *eq_lo, int s_lo,
-                        const kb::E4 *eq_hi, unsigned long long *acc, cudaStream_t st);
+                        const kb::E4 *eq_hi, unsigned long long *acc, cudaStream_t st,
+                        const Publish &pub = Publish());
 // SplitEq::compress_lo_into (eq.rs:491-539): out[i] = sum_j eq(rs)[j] * P[i*2^ks + j]
 cudaError_t compress_lo(const uint32_t *poly, int k, const Point &rs, kb::E4 *out,
                         cudaStream_t st);
@@ -80,11 +93,12 @@ cudaError_t add_pows(kb::E4 *w, int k, const uint32_t *vars, const kb::E4 *scale
 // (u64[8], unreduced canonical) when coeffs != 0.
 cudaError_t sumcheck_round(const kb::E4 *p_in, const kb::E4 *w_in, size_t n_in, bool fold,
                            kb::E4 r, kb::E4 *p_out, kb::E4 *w_out, bool coeffs,
-                           unsigned long long *acc, cudaStream_t st);
+                           unsigned long long *acc, cudaStream_t st,
+                           const Publish &pub = Publish());
 // <eq(z), poly> for an extension poly (SplitEq::eval_ext, eq.rs:179-250) -> acc u64[4]
 cudaError_t eval_ext(const kb::E4 *poly, int k, const kb::E4 *eq_lo, int s_lo,
-                     const kb::E4 *eq_hi, unsigned long long *acc, cudaStream_t st);
-// out[q] = <eq(rs), row(idx[q])> over base rows (fold_with_code evals, prover.rs:497-506)
+                     const kb::E4 *eq_hi, unsigned long long *acc, cudaStream_t st,
+                     const Publish &pub = Publish());
 // fold_with_code's per-query state on the device (see code_round_kernel)
 struct CodeState {
   const uint32_t *idx;  // n query indexes
@@ -98,8 +112,9 @@ struct CodeState {
 // round r: G update with r_prev (r >= 1), then this round's part of (c0, c2)
 // added to acc[0..8) (and, at round 0, the sum term to acc[8..12))
 cudaError_t code_round(const CodeState &s, int round, kb::E4 r_prev, unsigned long long *acc,
-                       cudaStream_t st);
+                       cudaStream_t st, const Publish &pub = Publish());
 cudaError_t code_finish(const CodeState &s, kb::E4 r_last, cudaStream_t st);
+// out[q] = <eq(rs), row(idx[q])> over base rows (fold_with_code evals, prover.rs:497-506)
 cudaError_t row_evals(const uint32_t *rows, int row_len, const uint32_t *idx, int n,
                       const Point &rs, kb::E4 *out, cudaStream_t st);
 

@@ -172,7 +172,7 @@ __device__ __forceinline__ void p2q_permute(uint32_t (&x)[4], int l, const uint3
 // CTA, G = 1, to the root), and each node is compressed by a quad of lanes.
 // Threads: 4 per node of the first level made (at most 1024).
 __global__ void __launch_bounds__(1024) tree_subtrees(uint32_t *__restrict__ nodes, int log_h,
-                                                     int l0, int steps) {
+                                                     int l0, int steps, uint32_t *host_root) {
   extern __shared__ uint4 sm[];  // 2 uint4 per node of this CTA's share
   __shared__ uint32_t kc[8 * 16 + 20];
   for (int i = threadIdx.x; i < 8 * 16 + 20; i += blockDim.x) kc[i] = c_p2_16[i];
@@ -200,6 +200,10 @@ __global__ void __launch_bounds__(1024) tree_subtrees(uint32_t *__restrict__ nod
       if (live && l < 2) {
         uint4 *dst = reinterpret_cast<uint4 *>(nodes + level_offset_words(log_h, l0 + st + 1));
         dst[(j + G * m) * 2 + l] = make_uint4(x[0], x[1], x[2], x[3]);
+        if (host_root && G == 1 && half == 1) {  // the root, also to the host
+#pragma unroll
+          for (int w = 0; w < 4; w++) host_root[4 * l + w] = x[w];
+        }
       }
     }
     __syncthreads();  // every read of this level's shared copy is done
@@ -214,17 +218,19 @@ __global__ void __launch_bounds__(1024) tree_subtrees(uint32_t *__restrict__ nod
 // narrow level) go through tree_subtrees.
 constexpr int WIDE_LOG = 15;
 
-static cudaError_t launch_subtrees(uint32_t *nodes, int log_h, int l0, int log_g, cudaStream_t st) {
+static cudaError_t launch_subtrees(uint32_t *nodes, int log_h, int l0, int log_g, cudaStream_t st,
+                                   uint32_t *host_root) {
   int steps = log_h - l0 - log_g;
   if (steps <= 0) return cudaSuccess;
   int n = 1 << steps;  // nodes per CTA at level l0
   int threads = 2 * n < 32 ? 32 : 2 * n;  // a quad per node made at the first step
-  tree_subtrees<<<1u << log_g, threads, (size_t)n * 32, st>>>(nodes, log_h, l0, steps);
+  tree_subtrees<<<1u << log_g, threads, (size_t)n * 32, st>>>(nodes, log_h, l0, steps,
+                                                              host_root);
   count_launches(1);
   return cudaGetLastError();
 }
 
-cudaError_t build_tree(uint32_t *nodes, int log_h, cudaStream_t st) {
+cudaError_t build_tree(uint32_t *nodes, int log_h, cudaStream_t st, uint32_t *host_root) {
   const int T = 128;
   int l = 0;
   for (; l < log_h && ((size_t)1 << (log_h - l)) / 2 >= ((size_t)1 << WIDE_LOG); l++) {
@@ -236,9 +242,9 @@ cudaError_t build_tree(uint32_t *nodes, int log_h, cudaStream_t st) {
   // remaining S = log_h - l steps (S <= WIDE_LOG): G = 2^(S/2) subtrees, then the top
   int S = log_h - l;
   int log_g = S / 2;
-  cudaError_t e = launch_subtrees(nodes, log_h, l, log_g, st);
+  cudaError_t e = launch_subtrees(nodes, log_h, l, log_g, st, host_root);
   if (e != cudaSuccess) return e;
-  return launch_subtrees(nodes, log_h, log_h - log_g, 0, st);
+  return launch_subtrees(nodes, log_h, log_h - log_g, 0, st, host_root);
 }
 
 __global__ void gather_openings_kernel(const uint32_t *__restrict__ rows, int row_len,

@@ -264,12 +264,13 @@ void encode_commit(Context &ctx, const uint32_t *src, int k, int rate, int foldi
   ctx.prof_begin(Context::K_LEAF);
   cuda_check(gpu::hash_rows(codeword, rows, (int)width, nodes, st), "hash_rows");
   ctx.prof_end(Context::K_LEAF, 4.0 * (double)(rows * width + rows * 8));
-  ctx.prof_begin(Context::K_TREE);
-  cuda_check(gpu::build_tree(nodes, log_h, st), "build_tree");
-  ctx.prof_end(Context::K_TREE, 32.0 * (double)(2 * rows - 2 + rows - 1));
+  // the last tree launch writes the root straight into pinned host memory
   uint32_t *h = (uint32_t *)ctx.pinned(64);
-  cuda_check(copy_async(ctx, h, nodes + gpu::tree_words(log_h) - 8, 32, cudaMemcpyDeviceToHost),
-             "root copy");
+  ctx.prof_begin(Context::K_TREE);
+  cuda_check(gpu::build_tree(nodes, log_h, st, h), "build_tree");
+  ctx.prof_end(Context::K_TREE, 32.0 * (double)(2 * rows - 2 + rows - 1));
+  if (log_h == 0)  // a single leaf is the root; no tree launch ran
+    cuda_check(copy_async(ctx, h, nodes, 32, cudaMemcpyDeviceToHost), "root copy");
   ctx.sync();
   out->rows = codeword;
   out->nodes = nodes;
@@ -454,6 +455,18 @@ struct Prover::Impl {
     ctx->sync();
     args_off = 0;
   }
+  // reduction results land in the context's pinned area (see gpu::Publish);
+  // the counter is the last word of acc
+  static constexpr size_t PUB_WORDS = 1024;
+  gpu::Publish publish(int words) {
+    gpu::Publish p;
+    p.counter = reinterpret_cast<unsigned int *>(acc.as<unsigned long long>() + acc.bytes() / 8 - 1);
+    p.host = published();
+    p.words = words;
+    if ((size_t)words > PUB_WORDS) throw WhirError(-5, "reduction too wide to publish");
+    return p;
+  }
+  unsigned long long *published() { return (unsigned long long *)ctx->pinned(8 * PUB_WORDS); }
   // pinned argument space for host->device copies issued before the next sync
   uint8_t *args_alloc(size_t bytes) {
     bytes = (bytes + 15) & ~(size_t)15;
@@ -577,12 +590,11 @@ struct Prover::Impl {
     make_eq_tables({point + ks}, nz, {e_one()}, s_lo, lo);
     size_t na = (size_t)4 << ks;
     unsigned long long *a = acc.as<unsigned long long>();
-    cuda_check(cudaMemsetAsync(a, 0, 8 * na, st()), "memset");
     ctx->prof_begin(Context::K_SUMCHECK);
-    cuda_check(gpu::compress_hi(poly_dev, kp, ks, lo, s_lo, hi, a, st()), "compress_hi");
+    cuda_check(gpu::compress_hi(poly_dev, kp, ks, lo, s_lo, hi, a, st(), publish((int)na)),
+               "compress_hi");
     ctx->prof_end(Context::K_SUMCHECK, 4.0 * (double)((size_t)1 << kp));
-    unsigned long long *h = (unsigned long long *)ctx->pinned(8 * na);
-    cuda_check(copy_async(*ctx, h, a, 8 * na, cudaMemcpyDeviceToHost), "d2h");
+    const unsigned long long *h = published();
     sync();
     size_t n = (size_t)1 << ks;
     c.compressed.resize(n);
@@ -721,7 +733,7 @@ struct Prover::Impl {
     coeffs_end(c0, c2);
   }
   void coeffs_end(E4 *c0, E4 *c2, E4 *extra = nullptr) {
-    const unsigned long long *h = (const unsigned long long *)ctx->pinned(128);
+    const unsigned long long *h = published();
     sync();
     *c0 = reduce_acc(h);
     *c2 = reduce_acc(h + 4);
@@ -732,24 +744,26 @@ struct Prover::Impl {
   void coeffs_begin(const gpu::CodeState *code = nullptr, int code_round = 0,
                     E4 code_r = E4{}) {
     unsigned long long *a = acc.as<unsigned long long>();
-    cuda_check(cudaMemsetAsync(a, 0, 96, st()), "memset");
+    // the last reducing launch publishes the sums to pinned memory and
+    // re-zeroes them (no memset, no copy)
+    gpu::Publish pub = publish(12);
+    gpu::Publish none;
     size_t n = (size_t)1 << kc;
     ctx->prof_begin(Context::K_SUMCHECK);
     if (pending) {
       cuda_check(gpu::sumcheck_round(P(), W(), 2 * n, true, pending_r, sp[1 - ping].as<E4>(),
-                                     sw[1 - ping].as<E4>(), true, a, st()),
+                                     sw[1 - ping].as<E4>(), true, a, st(), code ? none : pub),
                  "round");
       ping = 1 - ping;
       pending = false;
       ctx->prof_end(Context::K_SUMCHECK, 3.0 * 2 * 16 * (double)n);
     } else {
-      cuda_check(gpu::sumcheck_round(P(), W(), n, false, e_zero(), nullptr, nullptr, true, a, st()),
+      cuda_check(gpu::sumcheck_round(P(), W(), n, false, e_zero(), nullptr, nullptr, true, a, st(),
+                                     code ? none : pub),
                  "round");
       ctx->prof_end(Context::K_SUMCHECK, 2 * 16 * (double)n);
     }
-    if (code) cuda_check(gpu::code_round(*code, code_round, code_r, a, st()), "code_round");
-    unsigned long long *h = (unsigned long long *)ctx->pinned(128);
-    cuda_check(copy_async(*ctx, h, a, 96, cudaMemcpyDeviceToHost), "d2h");
+    if (code) cuda_check(gpu::code_round(*code, code_round, code_r, a, st(), pub), "code_round");
   }
   void flush() {
     if (!pending) return;
@@ -908,19 +922,21 @@ struct Prover::Impl {
     int n = (int)idx.size();
     if (n == 0) return 0;
     size_t per = (size_t)t.row_len + 8 * (size_t)t.log_h;
-    size_t need = 4 * (size_t)n + 4 * per * n + 16;
+    size_t need = 4 * (size_t)n + 16;
     if (need > gather.bytes()) {
       sync();  // an earlier gather may still be in flight
       gather.reserve(2 * need);
     }
     std::vector<uint32_t> hidx(n);
     for (int i = 0; i < n; i++) hidx[i] = (uint32_t)idx[i];
-    uint32_t *didx = gather.as<uint32_t>(), *dout = didx + ((n + 3) & ~3);
+    uint32_t *didx = gather.as<uint32_t>();
     upload(didx, hidx.data(), 4 * (size_t)n);
-    cuda_check(gpu::gather_openings(t.rows, t.row_len, t.nodes, t.log_h, didx, n, dout, st()),
-               "gather");
+    // the gather writes the hint words straight into the deferred pinned area
     size_t off = defer_alloc(per * n, ts);
-    cuda_check(copy_async(*ctx, defer_ptr(off), dout, 4 * per * n, cudaMemcpyDeviceToHost), "d2h");
+    cuda_check(gpu::gather_openings(t.rows, t.row_len, t.nodes, t.log_h, didx, n, defer_ptr(off),
+                                    st()),
+               "gather");
+    ctx->count_copy(4 * per * n, cudaMemcpyDeviceToHost);
     for (int i = 0; i < n; i++)
       pending_hints.push_back(PendingHint{ts.hint_reserve(per), off + per * i, per});
     return off;
@@ -1156,10 +1172,8 @@ struct Prover::Impl {
     E4 *lo = eqbuf.as<E4>(), *hi = lo + ((size_t)1 << s_lo);
     make_eq_tables({pt.data()}, k, {e_one()}, s_lo, lo);
     unsigned long long *a = acc.as<unsigned long long>();
-    cuda_check(cudaMemsetAsync(a, 0, 32, st()), "memset");
-    cuda_check(gpu::eval_ext(P(), k, lo, s_lo, hi, a, st()), "eval_ext");
-    unsigned long long *h = (unsigned long long *)ctx->pinned(64);
-    cuda_check(copy_async(*ctx, h, a, 32, cudaMemcpyDeviceToHost), "d2h");
+    cuda_check(gpu::eval_ext(P(), k, lo, s_lo, hi, a, st(), publish(4)), "eval_ext");
+    const unsigned long long *h = published();
     sync();
     return reduce_acc(h);
   }
@@ -1210,6 +1224,9 @@ void Prover::commit(Transcript &ts, const uint32_t *polys, bool on_device,
   m.pk = poly_k;
   m.make_layout();
   m.reserve();
+  // reductions publish and re-zero their accumulators (Impl::publish); start
+  // every proof from zero
+  cuda_check(cudaMemsetAsync(m.acc.as<void>(), 0, m.acc.bytes(), ctx_->stream()), "memset");
   m.claims.clear();
   m.virt.clear();
   cudaStream_t st = ctx_->stream();

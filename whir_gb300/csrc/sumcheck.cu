@@ -22,6 +22,22 @@ __device__ __forceinline__ void acc_add(unsigned long long *a, const E4 &v) {
 
 // eq table entries over z[off .. off+nv) times scale: entry b selects z_i
 // when bit i of b is set, 1 - z_i otherwise (Point::eq, point.rs:159-175).
+// Publish (kernels.h): after this CTA's atomics into acc, the last CTA of
+// the launch copies the sums out and zeroes them.  Every thread of the CTA
+// calls it.
+__device__ __forceinline__ void publish_if_last(unsigned long long *acc, const Publish &pub) {
+  if (!pub.host) return;
+  __shared__ bool last;
+  __threadfence();  // this CTA's atomics are visible before its ticket
+  __syncthreads();
+  if (threadIdx.x == 0) last = atomicAdd(pub.counter, 1u) == gridDim.x - 1;
+  __syncthreads();
+  if (!last) return;
+  __threadfence();
+  for (int i = threadIdx.x; i < pub.words; i += blockDim.x) pub.host[i] = atomicExch(acc + i, 0ull);
+  if (threadIdx.x == 0) atomicExch(pub.counter, 0u);
+}
+
 __global__ void eq_entries(Point z, int off, int nv, E4 scale, E4 *out) {
   size_t b = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (b >= ((size_t)1 << nv)) return;
@@ -110,7 +126,8 @@ __global__ void __launch_bounds__(CH_T) compress_hi_kernel(const uint32_t *__res
                                                            int k, int ks,
                                                            const E4 *__restrict__ eq_lo, int s_lo,
                                                            const E4 *__restrict__ eq_hi,
-                                                           unsigned long long *acc) {
+                                                           unsigned long long *acc,
+                                                           Publish pub) {
   extern __shared__ unsigned char smraw[];
   E4 *lo = reinterpret_cast<E4 *>(smraw);
   unsigned long long *part = reinterpret_cast<unsigned long long *>(lo + ((size_t)1 << s_lo));
@@ -136,15 +153,17 @@ __global__ void __launch_bounds__(CH_T) compress_hi_kernel(const uint32_t *__res
   }
   __syncthreads();
   for (int i = tid; i < W * 4; i += CH_T) atomicAdd(acc + i, part[i]);
+  publish_if_last(acc, pub);
 }
 
 cudaError_t compress_hi(const uint32_t *poly, int k, int ks, const E4 *eq_lo, int s_lo,
-                        const E4 *eq_hi, unsigned long long *acc, cudaStream_t st) {
+                        const E4 *eq_hi, unsigned long long *acc, cudaStream_t st,
+                        const Publish &pub) {
   if ((1 << ks) > CH_T || k < ks + s_lo) return cudaErrorInvalidValue;
   size_t n_hi = (size_t)1 << (k - ks - s_lo);
   unsigned grid = (unsigned)(n_hi < 152 * 8 ? n_hi : 152 * 8);
   size_t smem = ((size_t)1 << s_lo) * sizeof(E4) + ((size_t)4 << ks) * 8;
-  compress_hi_kernel<<<grid, CH_T, smem, st>>>(poly, k, ks, eq_lo, s_lo, eq_hi, acc);
+  compress_hi_kernel<<<grid, CH_T, smem, st>>>(poly, k, ks, eq_lo, s_lo, eq_hi, acc, pub);
   count_launches(1);
   return cudaGetLastError();
 }
@@ -257,7 +276,8 @@ cudaError_t add_pows(E4 *w, int k, const uint32_t *vars, const E4 *scales, int n
 
 // block-wide sum of E4 values into 64-bit accumulators
 template <int NV>
-__device__ __forceinline__ void block_acc(const E4 (&v)[NV], unsigned long long *acc) {
+__device__ __forceinline__ void block_acc(const E4 (&v)[NV], unsigned long long *acc,
+                                          const Publish &pub) {
   __shared__ unsigned long long part[NV * 4];
   for (int i = threadIdx.x; i < NV * 4; i += blockDim.x) part[i] = 0;
   __syncthreads();
@@ -273,6 +293,7 @@ __device__ __forceinline__ void block_acc(const E4 (&v)[NV], unsigned long long 
     }
   __syncthreads();
   for (int i = threadIdx.x; i < NV * 4; i += blockDim.x) atomicAdd(acc + i, part[i]);
+  publish_if_last(acc, pub);
 }
 
 // One round: new[i] = a[2i] + r (a[2i+1] - a[2i]) for poly and weights (when
@@ -281,7 +302,7 @@ __global__ void __launch_bounds__(256) round_kernel(const E4 *__restrict__ p_in,
                                                     const E4 *__restrict__ w_in, size_t n_in,
                                                     int fold, E4 r, E4 *__restrict__ p_out,
                                                     E4 *__restrict__ w_out, int coeffs,
-                                                    unsigned long long *acc) {
+                                                    unsigned long long *acc, Publish pub) {
   size_t n = fold ? n_in / 2 : n_in;
   size_t pairs = (n + 1) / 2;
   E4 sums[2] = {kb::e_zero(), kb::e_zero()};
@@ -310,19 +331,19 @@ __global__ void __launch_bounds__(256) round_kernel(const E4 *__restrict__ p_in,
       sums[1] = kb::e_add(sums[1], kb::e_mul(dw, dp));
     }
   }
-  if (coeffs) block_acc<2>(sums, acc);
+  if (coeffs) block_acc<2>(sums, acc, pub);
 }
 
 cudaError_t sumcheck_round(const E4 *p_in, const E4 *w_in, size_t n_in, bool fold, E4 r,
                            E4 *p_out, E4 *w_out, bool coeffs, unsigned long long *acc,
-                           cudaStream_t st) {
+                           cudaStream_t st, const Publish &pub) {
   size_t n = fold ? n_in / 2 : n_in;
   size_t pairs = (n + 1) / 2;
   unsigned T = 256;
   size_t g = (pairs + T - 1) / T;
   unsigned grid = (unsigned)(g < 152 * 8 ? (g ? g : 1) : 152 * 8);
   round_kernel<<<grid, T, 0, st>>>(p_in, w_in, n_in, fold ? 1 : 0, r, p_out, w_out,
-                                   coeffs ? 1 : 0, acc);
+                                   coeffs ? 1 : 0, acc, coeffs ? pub : Publish());
   count_launches(1);
   return cudaGetLastError();
 }
@@ -331,7 +352,7 @@ cudaError_t sumcheck_round(const E4 *p_in, const E4 *w_in, size_t n_in, bool fol
 __global__ void __launch_bounds__(256) eval_ext_kernel(const E4 *__restrict__ poly, int k,
                                                        const E4 *__restrict__ eq_lo, int s_lo,
                                                        const E4 *__restrict__ eq_hi,
-                                                       unsigned long long *acc) {
+                                                       unsigned long long *acc, Publish pub) {
   size_t n_lo = (size_t)1 << s_lo, n_hi = (size_t)1 << (k - s_lo);
   E4 outer = kb::e_zero();
   for (size_t hh = blockIdx.x; hh < n_hi; hh += gridDim.x) {
@@ -341,14 +362,14 @@ __global__ void __launch_bounds__(256) eval_ext_kernel(const E4 *__restrict__ po
     outer = kb::e_add(outer, kb::e_mul(inner, eq_hi[hh]));
   }
   E4 v[1] = {outer};
-  block_acc<1>(v, acc);
+  block_acc<1>(v, acc, pub);
 }
 
 cudaError_t eval_ext(const E4 *poly, int k, const E4 *eq_lo, int s_lo, const E4 *eq_hi,
-                     unsigned long long *acc, cudaStream_t st) {
+                     unsigned long long *acc, cudaStream_t st, const Publish &pub) {
   size_t n_hi = (size_t)1 << (k - s_lo);
   unsigned grid = (unsigned)(n_hi < 152 * 8 ? n_hi : 152 * 8);
-  eval_ext_kernel<<<grid, 256, 0, st>>>(poly, k, eq_lo, s_lo, eq_hi, acc);
+  eval_ext_kernel<<<grid, 256, 0, st>>>(poly, k, eq_lo, s_lo, eq_hi, acc, pub);
   count_launches(1);
   return cudaGetLastError();
 }
@@ -393,8 +414,8 @@ __device__ __forceinline__ void acc_add_e4(unsigned long long *acc, const E4 &v)
   for (int c = 0; c < 4; c++) atomicAdd(acc + c, (unsigned long long)v.c[c]);
 }
 
-__global__ void __launch_bounds__(32) code_round_kernel(CodeState s, int round, E4 r_prev,
-                                                        unsigned long long *acc) {
+__device__ __forceinline__ void code_round_query(CodeState s, int round, E4 r_prev,
+                                                 unsigned long long *acc) {
   using namespace kb;
   const int i = blockIdx.x;
   const int lS = s.k_data - s.d;
@@ -454,6 +475,12 @@ __global__ void __launch_bounds__(32) code_round_kernel(CodeState s, int round, 
   acc_add_e4(acc + 4, e_scale(e_mul(sc, e_sub(e_dbl(odd), even)), wt));
 }
 
+__global__ void __launch_bounds__(32) code_round_kernel(CodeState s, int round, E4 r_prev,
+                                                        unsigned long long *acc, Publish pub) {
+  code_round_query(s, round, r_prev, acc);
+  publish_if_last(acc, pub);
+}
+
 // the updates after the last round, before combine_pows_scaled (combine.rs:441-468)
 __global__ void code_finish_kernel(CodeState s, E4 r_last) {
   using namespace kb;
@@ -466,11 +493,11 @@ __global__ void code_finish_kernel(CodeState s, E4 r_last) {
 }
 
 cudaError_t code_round(const CodeState &s, int round, E4 r_prev, unsigned long long *acc,
-                       cudaStream_t st) {
+                       cudaStream_t st, const Publish &pub) {
   if (s.n == 0) return cudaSuccess;
   if (s.d < 1 || s.d > 8 || s.k_data < s.d || s.k_data > 30 || round < 0 || round >= s.d)
     return cudaErrorInvalidValue;
-  code_round_kernel<<<s.n, 32, 0, st>>>(s, round, r_prev, acc);
+  code_round_kernel<<<s.n, 32, 0, st>>>(s, round, r_prev, acc, pub);
   count_launches(1);
   return cudaGetLastError();
 }
