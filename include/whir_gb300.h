@@ -171,6 +171,18 @@ WHIR_API int whir_prove(whir_prover *p, whir_transcript *t, const uint32_t *poly
                const int32_t *poly_k, int n_polys, const int32_t *group_n, int n_groups,
                const int32_t *group_ids);
 
+/* Whir::verify (crates/whir/src/whir.rs:361-522, sumcheck/verifier.rs) on the
+ * host: checks a proof of whir_prove with the same parameters, polynomial
+ * sizes and claim groups.  *result: 0 accepted; 1 the bytes ran out or held a
+ * non-canonical word; 2 a Merkle opening failed; 3 a final opening disagrees
+ * with the final polynomial; 4 the sumcheck's final claim failed; 5 the round
+ * structure does not match.  On acceptance *checkpoint (may be NULL) is the
+ * base element the harness draws after the proof.  Needs no GPU. */
+WHIR_API int whir_verify(const whir_params *params, const int32_t *poly_k, int n_polys,
+                         const int32_t *group_n, int n_groups, const int32_t *group_ids,
+                         const uint8_t *proof, size_t len, int32_t *result,
+                         uint32_t *checkpoint);
+
 /* ---- many proofs on one GPU (batched and served proving).  No
  * counterpart in the reference, whose harness proves one polynomial per call
  * (crates/whir/src/test.rs:218-235); each job here is that harness on one

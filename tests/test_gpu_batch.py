@@ -46,6 +46,10 @@ def test_batch_matches_alone(ctx, oracle):
         proof, cp = alone(ctx, j)
         assert j.proof == proof
         assert j.checkpoint == cp
+        if not j.commit_only:
+            p = j.params
+            params = (p.k, p.folding, p.rate, p.initial_reduction, p.soundness, p.security_level)
+            assert W.verify(params, [p.k], [[0]] * j.claims, j.proof) == (0, cp)
 
 
 def test_batch_matches_oracle(oracle):

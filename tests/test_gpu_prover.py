@@ -30,6 +30,7 @@ def check(ctx, oracle, params, polys, poly_k, groups):
     assert cp == wcp
     rc, vcp = oracle.verify(params, poly_k, groups, proof)
     assert rc == 0 and vcp == cp
+    assert W.verify(params, poly_k, groups, proof) == (0, cp)  # the library's verifier
 
 
 @pytest.mark.parametrize("s,k,f,ir,n", SWEEP)

@@ -1,0 +1,87 @@
+"""The library's host verifier (whir_verify, Whir::verify of
+crates/whir/src/whir.rs:361-522) on the CPU, against proofs from the oracle
+prover: it accepts them with the oracle's checkpoint, over the reference's
+test_whir_poseidon parameter sweep (crates/whir/src/test.rs:256-282) and
+stacked layouts, and rejects tampered, truncated or mismatched proofs.
+"""
+import numpy as np
+import pytest
+
+import whir_gb300 as W
+
+SWEEP = [(s, k, f, ir, n)
+         for s in (1, 2, 0) for k in (4, 6, 9, 12) for f in (1, 2, 3)
+         for ir in range(1, f + 1) for n in (1, 3)
+         if (k + f + ir + n + s) % 4 == 0 or k == 12 and ir == 1 and n == 1]
+
+
+@pytest.mark.parametrize("s,k,f,ir,n", SWEEP)
+def test_accepts_oracle_proofs(oracle, s, k, f, ir, n):
+    poly = oracle.rand_fe(7 + k, 1 << k)
+    params = (k, f, 1, ir, s, 32)
+    proof, cp = oracle.prove(params, [poly], [k], [[0]] * n)
+    res, vcp = W.verify(params, [k], [[0]] * n, proof)
+    assert res == 0 and vcp == cp
+
+
+@pytest.mark.parametrize("k,rate,n", [(10, 2, 2), (14, 1, 1), (12, 2, 4)])
+def test_accepts_folding4_security100(oracle, k, rate, n):
+    poly = oracle.rand_fe(3, 1 << k)
+    params = (k, 4, rate, 1, 1, 100)
+    proof, cp = oracle.prove(params, [poly], [k], [[0]] * n)
+    assert W.verify(params, [k], [[0]] * n, proof) == (0, cp)
+
+
+def test_accepts_stacked_layout(oracle):
+    ks = [8, 6, 6, 8, 5]
+    polys = [oracle.rand_fe(20 + i, 1 << k) for i, k in enumerate(ks)]
+    k = int(np.ceil(np.log2(sum(1 << x for x in ks))))
+    groups = [[0, 3], [1, 2], [4], [3]]
+    params = (k, 3, 1, 1, 1, 32)
+    proof, cp = oracle.prove(params, polys, ks, groups)
+    assert W.verify(params, ks, groups, proof) == (0, cp)
+
+
+@pytest.fixture(scope="module")
+def one_proof(oracle):
+    k, n = 12, 2
+    params = (k, 4, 1, 1, 1, 100)
+    poly = oracle.rand_fe(11, 1 << k)
+    proof, cp = oracle.prove(params, [poly], [k], [[0]] * n)
+    return params, k, n, proof, cp
+
+
+def test_rejects_flipped_bytes(one_proof):
+    params, k, n, proof, cp = one_proof
+    rng = np.random.default_rng(5)
+    # the root, a claim evaluation, the SVO rounds, then spread over the rest
+    spots = [0, 31, 40, 100, 200] + sorted(int(x) for x in rng.integers(0, len(proof), 40))
+    for pos in spots:
+        bad = bytearray(proof)
+        bad[pos] ^= 1 << int(rng.integers(0, 7))   # stays below 2^31 in the top byte
+        res, _ = W.verify(params, [k], [[0]] * n, bytes(bad))
+        assert res != 0, pos
+
+
+def test_rejects_truncated_and_noncanonical(one_proof):
+    params, k, n, proof, cp = one_proof
+    assert W.verify(params, [k], [[0]] * n, proof[:-4])[0] == 1
+    assert W.verify(params, [k], [[0]] * n, b"")[0] == 1
+    bad = bytearray(proof)
+    bad[0:4] = (0x7f000001).to_bytes(4, "little")    # p itself: not canonical
+    assert W.verify(params, [k], [[0]] * n, bytes(bad))[0] == 1
+
+
+def test_rejects_other_statement(one_proof):
+    params, k, n, proof, cp = one_proof
+    # a different number of claims changes every challenge after the root
+    assert W.verify(params, [k], [[0]] * (n + 1), proof)[0] != 0
+    # other security parameters change the query counts
+    assert W.verify((k, 4, 1, 1, 1, 90), [k], [[0]] * n, proof)[0] != 0
+
+
+def test_argument_errors():
+    with pytest.raises(W.WhirError):
+        W.verify((10, 4, 1, 1, 1, 100), [9], [[0]], b"\\0" * 64)   # layout size != 2^k
+    with pytest.raises(W.WhirError):
+        W.verify((10, 4, 1, 1, 1, 100), [10], [[1]], b"\\0" * 64)  # unknown poly id

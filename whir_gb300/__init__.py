@@ -105,6 +105,8 @@ _SIGS = {
                                         ctypes.c_int, ctypes.c_uint64, ctypes.POINTER(RunStatsC)]),
     "whir_serve": (ctypes.c_int, [ctypes.c_int, ctypes.POINTER(JobC), ctypes.c_int,
                                   ctypes.c_int, ctypes.c_uint64, ctypes.POINTER(RunStatsC)]),
+    "whir_verify": (ctypes.c_int, [ctypes.POINTER(Params), i32p, ctypes.c_int, i32p, ctypes.c_int,
+                                   i32p, ctypes.c_char_p, ctypes.c_size_t, i32p, u32p]),
     "whir_server_new": (ctypes.c_int, [ctypes.c_int, ctypes.c_int, ctypes.c_uint64,
                                        ctypes.POINTER(vp)]),
     "whir_server_run": (ctypes.c_int, [vp, ctypes.POINTER(JobC), ctypes.c_int, ctypes.c_int,
@@ -599,3 +601,18 @@ def serve_simulate(arrival_s, need_bytes, duration_s, workers, budget_bytes):
     _check(lib().whir_serve_simulate(A, N, D, n, workers, budget_bytes, S, E,
                                      Wk.ctypes.data_as(i32p), St.ctypes.data_as(i32p)))
     return np.array(S[:n]), np.array(E[:n]), Wk[:n], St[:n]
+
+
+def verify(params, poly_k, groups, proof):
+    """Whir::verify on the host: returns (result, checkpoint); result 0 means
+    accepted (see whir_verify for the rejection codes)."""
+    p = params if isinstance(params, Params) else Params(*params)
+    ks = (ctypes.c_int32 * len(poly_k))(*poly_k)
+    gn = (ctypes.c_int32 * max(1, len(groups)))(*[len(g) for g in groups])
+    flat = [i for g in groups for i in g]
+    gi = (ctypes.c_int32 * max(1, len(flat)))(*flat)
+    res = ctypes.c_int32()
+    cp = np.zeros(1, np.uint32)
+    _check(lib().whir_verify(ctypes.byref(p), ks, len(poly_k), gn, len(groups), gi, bytes(proof),
+                             len(proof), ctypes.byref(res), cp.ctypes.data_as(u32p)))
+    return res.value, int(cp[0])

@@ -16,6 +16,7 @@
 #include "poseidon2_host.h"
 #include "batch.h"
 #include "prover.h"
+#include "verifier.h"
 #include "transcript.h"
 
 using whir::Context;
@@ -681,6 +682,26 @@ int whir_serve_simulate(const double *arrival_s, const uint64_t *need_b, const d
     worker[i] = js[i].worker;
     status[i] = js[i].status == 0 ? WHIR_OK : js[i].status == -4 ? WHIR_ERR_CAPACITY : WHIR_ERR_INTERNAL;
   }
+  API_END
+}
+
+int whir_verify(const whir_params *params, const int32_t *poly_k, int n_polys,
+                const int32_t *group_n, int n_groups, const int32_t *group_ids,
+                const uint8_t *proof, size_t len, int32_t *result, uint32_t *checkpoint) {
+  API_BEGIN
+  need(result != nullptr, "null result");
+  std::vector<int> ks = ks_in(poly_k, n_polys);
+  need(n_groups >= 0 && (group_n || !n_groups), "bad claim groups");
+  std::vector<std::vector<int>> groups;
+  size_t off = 0;
+  for (int g = 0; g < n_groups; g++) {
+    need(group_n[g] > 0 && group_ids, "empty claim group");
+    groups.emplace_back(group_ids + off, group_ids + off + group_n[g]);
+    off += group_n[g];
+  }
+  uint32_t cp = 0;
+  *result = (int32_t)whir::verify(params_in(params), ks, groups, proof, len, &cp);
+  if (checkpoint) *checkpoint = *result == 0 ? cp : 0;
   API_END
 }
 

@@ -1,5 +1,6 @@
 // GPU WHIR prover host orchestration (see prover.h).
 #include "prover.h"
+#include "host_math.h"
 
 #include <math.h>
 #include <string.h>
@@ -190,56 +191,7 @@ void Context::count_copy(size_t bytes, int kind) {
   if (kind == cudaMemcpyDeviceToHost) d2h_bytes_ += bytes;
 }
 
-// ---------------- host helpers ----------------
-static E4 e_inv2() { return e_from(inv(from_canonical(2))); }
-static void lagrange012(const E4 &r, E4 w[3]) {
-  E4 it = e_inv2(), one = e_one(), two = e_dbl(e_one());
-  w[0] = e_mul(e_mul(e_sub(r, one), e_sub(r, two)), it);
-  w[1] = e_mul(r, e_sub(two, r));
-  w[2] = e_mul(e_mul(r, e_sub(r, one)), it);
-}
-static E4 extrapolate012(const E4 &e0, const E4 &e1, const E4 &e2, const E4 &r) {
-  E4 w[3];
-  lagrange012(r, w);
-  return e_add(e_add(e_mul(e0, w[0]), e_mul(e1, w[1])), e_mul(e2, w[2]));
-}
-static void eq_host(const E4 *z, int k, const E4 &scale, E4 *out) {
-  out[0] = scale;
-  for (int i = 0; i < k; i++) {
-    size_t h = (size_t)1 << i;
-    for (size_t j = 0; j < h; j++) {
-      E4 hi = e_mul(out[j], z[i]);
-      out[j + h] = hi;
-      out[j] = e_sub(out[j], hi);
-    }
-  }
-}
-static E4 eval_eq_xy(const E4 *x, const E4 *y, int n) {
-  E4 acc = e_one();
-  for (int i = 0; i < n; i++) {
-    E4 t = e_sub(e_sub(e_dbl(e_mul(y[i], x[i])), x[i]), y[i]);
-    acc = e_mul(acc, e_add(t, e_one()));
-  }
-  return acc;
-}
-static E4 horner(const E4 *c, size_t n, const E4 &x) {
-  E4 acc = e_zero();
-  for (size_t i = n; i-- > 0;) acc = e_add(e_mul(acc, x), c[i]);
-  return acc;
-}
-static void expand(E4 *out, int k, E4 v) {
-  for (int i = 0; i < k; i++) {
-    out[i] = v;
-    v = e_sq(v);
-  }
-}
-static E4 eval_ext_small(const E4 *poly, int k, const E4 *z) {
-  std::vector<E4> eq((size_t)1 << k);
-  eq_host(z, k, e_one(), eq.data());
-  E4 acc = e_zero();
-  for (size_t i = 0; i < eq.size(); i++) acc = e_add(acc, e_mul(eq[i], poly[i]));
-  return acc;
-}
+// ---------------- host helpers (host_math.h) ----------------
 static size_t ipow3(int r) {
   size_t v = 1;
   while (r--) v *= 3;
@@ -320,14 +272,44 @@ class PinnedBuffer {
   size_t bytes_ = 0;
 };
 
-struct LayEntry {
-  int nbits;
-  uint8_t bits[32];
-  int poly;
-  size_t index;
-};
+
 
 }  // namespace
+
+// ProverStack::layout (crates/whir/src/sumcheck/prover.rs:92-124): polys
+// placed largest first, each at an aligned offset; entries sorted by their
+// selector bits as BTreeMap<Selector, _> orders them (Vec<bool>
+// lexicographic).  Shared by the prover and the verifier.
+std::vector<LayEntry> stack_layout(const std::vector<int> &pk, int k_expect, int folding) {
+  int n = (int)pk.size();
+  std::vector<int> order(n);
+  for (int i = 0; i < n; i++) order[i] = i;
+  std::stable_sort(order.begin(), order.end(), [&](int a, int b) { return pk[a] < pk[b]; });
+  size_t total = 0;
+  for (int i = 0; i < n; i++) total += (size_t)1 << pk[i];
+  int k = 0;
+  while (((size_t)1 << k) < total) k++;
+  if (k != k_expect) throw WhirError(-1, "stacked layout size does not match params.k");
+  if (k < folding) throw WhirError(-1, "k smaller than folding");
+  std::vector<LayEntry> lay(n);
+  size_t off = 0;
+  for (int t = 0; t < n; t++) {
+    int id = order[n - 1 - t];
+    LayEntry &e = lay[t];
+    e.poly = id;
+    e.nbits = k - pk[id];
+    e.index = off >> pk[id];
+    for (int b = 0; b < e.nbits; b++) e.bits[b] = (e.index >> b) & 1;
+    off += (size_t)1 << pk[id];
+  }
+  std::sort(lay.begin(), lay.end(), [](const LayEntry &a, const LayEntry &b) {
+    int m = std::min(a.nbits, b.nbits);
+    for (int i = 0; i < m; i++)
+      if (a.bits[i] != b.bits[i]) return a.bits[i] < b.bits[i];
+    return a.nbits < b.nbits;
+  });
+  return lay;
+}
 
 // crates/whir/src/whir.rs:150-166: the domain, folding and rates of round r
 void round_params(const Params &p, int round, int *kfd, int *this_rate, int *prev_rate) {
@@ -523,33 +505,7 @@ struct Prover::Impl {
 
   // ---- layout (ProverStack::layout, prover.rs:92-124) ----
   void make_layout() {
-    std::vector<int> order(n_polys);
-    for (int i = 0; i < n_polys; i++) order[i] = i;
-    std::stable_sort(order.begin(), order.end(), [&](int a, int b) { return pk[a] < pk[b]; });
-    size_t total = 0;
-    for (int i = 0; i < n_polys; i++) total += (size_t)1 << pk[i];
-    int k = 0;
-    while (((size_t)1 << k) < total) k++;
-    if (k != p.k) throw WhirError(-1, "stacked layout size does not match params.k");
-    if (k < ks) throw WhirError(-1, "k smaller than folding");
-    lay.assign(n_polys, LayEntry{});
-    size_t off = 0;
-    for (int t = 0; t < n_polys; t++) {
-      int id = order[n_polys - 1 - t];
-      LayEntry &e = lay[t];
-      e.poly = id;
-      e.nbits = k - pk[id];
-      e.index = off >> pk[id];
-      for (int b = 0; b < e.nbits; b++) e.bits[b] = (e.index >> b) & 1;
-      off += (size_t)1 << pk[id];
-    }
-    // BTreeMap<Selector, _> order: Vec<bool> compared lexicographically
-    std::sort(lay.begin(), lay.end(), [](const LayEntry &a, const LayEntry &b) {
-      int n = std::min(a.nbits, b.nbits);
-      for (int i = 0; i < n; i++)
-        if (a.bits[i] != b.bits[i]) return a.bits[i] < b.bits[i];
-      return a.nbits < b.nbits;
-    });
+    lay = stack_layout(pk, p.k, ks);
     poly_off.assign(n_polys, 0);
     for (auto &e : lay) poly_off[e.poly] = e.index << pk[e.poly];
   }

@@ -34,6 +34,15 @@ constexpr int EXT_BITS = 124;  // bits of |BinomialExtensionField<KoalaBear, 4>|
 
 uint32_t two_adic_generator(int bits);  // Montgomery form
 
+// one entry of the stacked layout: poly id, selector bits, aligned index
+struct LayEntry {
+  int nbits = 0;
+  uint8_t bits[32] = {};
+  int poly = 0;
+  size_t index = 0;
+};
+std::vector<LayEntry> stack_layout(const std::vector<int> &pk, int k_expect, int folding);
+
 // domain bits, folded-domain bits and rates of WHIR round `round`
 void round_params(const Params &p, int round, int *kfd, int *this_rate, int *prev_rate);
 

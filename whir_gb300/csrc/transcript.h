@@ -69,4 +69,60 @@ class Transcript {
   Challenger ch_;
 };
 
+// The verifier's side (crates/transcript/src/poseidon.rs:13-87): the proof
+// bytes are read back in order; read_* observes what write_* observed,
+// hint_* reads hints without observing.  A read past the end, or a word
+// that is not a canonical field element, sets the error flag and yields 0.
+class TranscriptReader {
+ public:
+  TranscriptReader(const uint8_t *bytes, size_t len) : p_(bytes), n_(len) {}
+  uint32_t read_fe() {
+    uint32_t v = take();
+    ch_.observe(v);
+    return v;
+  }
+  kb::E4 read_ext() {
+    kb::E4 e;
+    for (int i = 0; i < 4; i++) e.c[i] = read_fe();
+    return e;
+  }
+  void read_digest(uint32_t *d) {
+    for (int i = 0; i < 8; i++) d[i] = read_fe();
+  }
+  uint32_t hint_fe() { return take(); }
+  void hint_digest(uint32_t *d) {
+    for (int i = 0; i < 8; i++) d[i] = take();
+  }
+  kb::E4 draw_ext() {
+    kb::E4 e;
+    for (int i = 0; i < 4; i++) e.c[i] = ch_.sample();
+    return e;
+  }
+  uint32_t draw_fe() { return ch_.sample(); }
+  size_t draw_bits(int bits) { return ch_.sample_bits(bits); }
+  bool failed() const { return err_; }
+  size_t remaining() const { return n_ - off_; }
+
+ private:
+  uint32_t take() {
+    if (off_ + 4 > n_) {
+      err_ = true;
+      off_ = n_;
+      return 0;
+    }
+    uint32_t v = (uint32_t)p_[off_] | ((uint32_t)p_[off_ + 1] << 8) |
+                 ((uint32_t)p_[off_ + 2] << 16) | ((uint32_t)p_[off_ + 3] << 24);
+    off_ += 4;
+    if (v >= kb::P) {
+      err_ = true;
+      return 0;
+    }
+    return v;
+  }
+  const uint8_t *p_;
+  size_t n_, off_ = 0;
+  bool err_ = false;
+  Challenger ch_;
+};
+
 }  // namespace whir

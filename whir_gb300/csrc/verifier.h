@@ -1,0 +1,31 @@
+// WHIR verifier on the host: Whir::verify (crates/whir/src/whir.rs:361-522)
+// with SumcheckVerifier (crates/whir/src/sumcheck/verifier.rs), over the same
+// transcript (PoseidonWriter reading side) and Merkle hashing as the prover.
+#pragma once
+#include <stddef.h>
+#include <stdint.h>
+
+#include <vector>
+
+#include "prover.h"
+
+namespace whir {
+
+// Why a proof was rejected (0: accepted).
+enum VerifyResult {
+  V_OK = 0,
+  V_TRANSCRIPT = 1,  // proof bytes ran out or held a non-canonical word
+  V_MERKLE = 2,      // an opening did not hash to its commitment
+  V_STIR = 3,        // a final-round opening disagrees with the final polynomial
+  V_SUMCHECK = 4,    // the sumcheck's final claim does not match
+  V_SHAPE = 5,       // the proof's round structure does not match the parameters
+};
+
+// Checks a proof made by Prover::prove with the same parameters, polynomial
+// sizes and claim groups.  On acceptance *checkpoint is the base element the
+// harness draws after the proof (test.rs:236).  Argument errors throw.
+VerifyResult verify(const Params &p, const std::vector<int> &poly_k,
+                    const std::vector<std::vector<int>> &groups, const uint8_t *proof, size_t len,
+                    uint32_t *checkpoint);
+
+}  // namespace whir
