@@ -142,7 +142,27 @@ __global__ void __launch_bounds__(CH_T) compress_hi_kernel(const uint32_t *__res
   for (size_t hh = blockIdx.x; hh < n_hi; hh += gridDim.x) {
     const uint32_t *base = poly + hh * block_words;
     E4 inner = kb::e_zero();
-    for (size_t e = tid; e < block_words; e += CH_T)
+    size_t e = tid;
+    // four products of canonical words per 64-bit sum (4 p^2 < 2p 2^32), one
+    // Montgomery reduction per four: the sum of Montgomery words' products
+    // reduces to the Montgomery word of the sum of products
+    for (; e + 3 * CH_T < block_words; e += 4 * CH_T) {
+      uint32_t x[4];
+#pragma unroll
+      for (int q = 0; q < 4; q++) x[q] = __ldg(base + e + q * CH_T);
+      unsigned long long s4[4] = {0, 0, 0, 0};
+#pragma unroll
+      for (int q = 0; q < 4; q++) {
+        const E4 l = lo[(e + q * CH_T) >> ks];
+#pragma unroll
+        for (int c = 0; c < 4; c++) s4[c] += (unsigned long long)l.c[c] * x[q];
+      }
+      E4 part4;
+#pragma unroll
+      for (int c = 0; c < 4; c++) part4.c[c] = kb::reduce_wide(s4[c]);
+      inner = kb::e_add(inner, part4);
+    }
+    for (; e < block_words; e += CH_T)
       inner = kb::e_add(inner, kb::e_scale(lo[e >> ks], __ldg(base + e)));
     outer = kb::e_add(outer, kb::e_mul(inner, eq_hi[hh]));
   }
