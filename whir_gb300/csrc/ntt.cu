@@ -337,6 +337,137 @@ __global__ void __launch_bounds__(256) dft_tile_v(const uint32_t *__restrict__ i
   }
 }
 
+// ---- vectorised tile with the first and last radix steps on global memory ----
+// The same transform as dft_tile_v, but the first radix step reads its rows
+// straight from global memory (zero padding and the coset pre-twiddle on the
+// fly) and the last step writes its rows straight to their bit-reversed
+// output rows (four-step post-twiddle on the fly): two shared-memory passes
+// and two barriers fewer per tile.  Needs S >= 4 (at least two steps).
+template <int C, int R>
+__device__ __forceinline__ void dif_first_v(uint4 *tile, const uint32_t *twl, int rows_log, int S,
+                                            const uint4 *__restrict__ in4, uint32_t o0,
+                                            uint32_t wv, uint32_t v0, uint32_t rows_valid,
+                                            uint32_t a_in, uint32_t b_in, int pre_log) {
+  constexpr int T = 1 << R, V = C / 4, LV = V == 2 ? 1 : 0;
+  const int lh = S - 1, lq = lh - (R - 1);
+  const int q = 1 << lq, H = 1 << lh, n = 1 << S;
+  const uint32_t pmask = (1u << pre_log) - 1u;
+  const int tasks = (1 << (rows_log - R)) << LV;
+  for (int task = threadIdx.x; task < tasks; task += blockDim.x) {
+    const int c = task & (V - 1), rest = task >> LV;
+    const int j = rest & (q - 1), blk = rest >> lq;
+    const int base = blk * 2 * H + j;
+    uint4 v[T];
+#pragma unroll
+    for (int t = 0; t < T; t++) {
+      const int r = base + t * q;
+      const uint32_t o = o0 + (uint32_t)(r >> S), i = (uint32_t)(r & (n - 1));
+      const uint32_t row = o * a_in + i * b_in;
+      v[t] = make_uint4(0, 0, 0, 0);
+      if (row < rows_valid) {
+        v[t] = __ldg(in4 + row * wv + v0 + c);
+        if (pre_log) v[t] = mul4(v[t], root_pow(((o * i) & pmask) << (24 - pre_log)));
+      }
+    }
+#pragma unroll
+    for (int st = 0; st < R; st++) {
+      const int span = T >> (st + 1);
+      const int hh = H >> st;
+#pragma unroll
+      for (int t = 0; t < T; t++) {
+        if (t & span) continue;
+        const int tl = t & (span - 1);
+        uint4 a = v[t], b = v[t + span];
+        v[t] = add4(a, b);
+        v[t + span] = submul4(a, b, twl[hh + j + tl * q]);
+      }
+    }
+#pragma unroll
+    for (int t = 0; t < T; t++) tile[vrow<C>(base + t * q) * V + c] = v[t];
+  }
+}
+
+// the final radix-8 step (block stride 1, first half-size 4), written to the
+// output rows
+template <int C>
+__device__ __forceinline__ void dif_last_v(const uint4 *tile, const uint32_t *twl, int rows_log,
+                                           int S, uint4 *__restrict__ out4, uint32_t o0,
+                                           uint32_t wv, uint32_t v0, uint32_t a_out,
+                                           uint32_t b_out, int tw_log) {
+  constexpr int R = 3, T = 8, V = C / 4, LV = V == 2 ? 1 : 0;
+  const int n = 1 << S;
+  const uint32_t tmask = (1u << tw_log) - 1u;
+  const int tasks = (1 << (rows_log - R)) << LV;
+  for (int task = threadIdx.x; task < tasks; task += blockDim.x) {
+    const int c = task & (V - 1), blk = task >> LV;
+    const int base = blk * T;
+    uint4 v[T];
+#pragma unroll
+    for (int t = 0; t < T; t++) v[t] = tile[vrow<C>(base + t) * V + c];
+#pragma unroll
+    for (int st = 0; st < R; st++) {
+      const int span = T >> (st + 1);
+      const int hh = 4 >> st;
+#pragma unroll
+      for (int t = 0; t < T; t++) {
+        if (t & span) continue;
+        const int tl = t & (span - 1);
+        uint4 a = v[t], b = v[t + span];
+        v[t] = add4(a, b);
+        if (tl == 0) v[t + span] = sub4(a, b);  // w^0 = 1
+        else v[t + span] = submul4(a, b, twl[hh + tl]);
+      }
+    }
+#pragma unroll
+    for (int t = 0; t < T; t++) {
+      const int r = base + t;
+      const uint32_t o = o0 + (uint32_t)(r >> S);
+      const uint32_t k = brev((uint32_t)(r & (n - 1)), S);
+      uint4 x = v[t];
+      if (tw_log) x = mul4(x, root_pow(((o * k) & tmask) << (24 - tw_log)));
+      out4[(o * a_out + k * b_out) * wv + v0 + c] = x;
+    }
+  }
+}
+
+template <int C>
+__global__ void __launch_bounds__(256) dft_tile_v2(const uint32_t *__restrict__ in,
+                                                   uint32_t *__restrict__ out, int S, int lg,
+                                                   uint32_t width, uint32_t rows_valid,
+                                                   uint32_t a_in, uint32_t b_in, uint32_t a_out,
+                                                   uint32_t b_out, int pre_log, int tw_log) {
+  constexpr int V = C / 4;
+  extern __shared__ uint4 smv[];
+  const int n = 1 << S, rows = n << lg;
+  uint4 *tile = smv;
+  uint32_t *aux = reinterpret_cast<uint32_t *>(smv + rows * V);  // DIF twiddles only
+  const uint32_t o0 = blockIdx.y << lg;
+  const uint32_t v0 = blockIdx.x * V;
+  const uint32_t wv = width / 4;
+  const uint4 *in4 = reinterpret_cast<const uint4 *>(in);
+  uint4 *out4 = reinterpret_cast<uint4 *>(out);
+  for (int x = threadIdx.x + 1; x < n; x += blockDim.x) {
+    int lh = 31 - __clz(x);
+    uint32_t pos = (uint32_t)(x - (1 << lh));
+    aux[x] = root_pow(pos << (24 - 1 - lh));  // w_{2^(lh+1)}^pos
+  }
+  __syncthreads();
+  const int rows_log = S + lg;
+  const int r0 = S % 3 == 0 ? 3 : S % 3;
+  if (r0 == 1)
+    dif_first_v<C, 1>(tile, aux, rows_log, S, in4, o0, wv, v0, rows_valid, a_in, b_in, pre_log);
+  else if (r0 == 2)
+    dif_first_v<C, 2>(tile, aux, rows_log, S, in4, o0, wv, v0, rows_valid, a_in, b_in, pre_log);
+  else
+    dif_first_v<C, 3>(tile, aux, rows_log, S, in4, o0, wv, v0, rows_valid, a_in, b_in, pre_log);
+  __syncthreads();
+  for (int lh = S - 1 - r0; lh >= 5; lh -= 3) {
+    dif_step_v<C, 3, false>(tile, aux, rows_log, lh);
+    __syncthreads();
+  }
+  dif_last_v<C>(tile, aux, rows_log, S, out4, o0, wv, v0, a_out, b_out, tw_log);
+}
+
 template <int C>
 static cudaError_t launch_tile_v(const uint32_t *in, uint32_t *out, int S, size_t width,
                                  size_t rows_valid, size_t n_outer, size_t a_in, size_t b_in,
@@ -349,9 +480,15 @@ static cudaError_t launch_tile_v(const uint32_t *in, uint32_t *out, int S, size_
   int threads = (int)(rows * (C / 4) / 8);
   threads = threads < 32 ? 32 : (threads > 256 ? 256 : threads);
   dim3 grid((unsigned)(width / C), (unsigned)(n_outer >> lg));
-  dft_tile_v<C><<<grid, threads, smem, st>>>(in, out, S, lg, (uint32_t)width,
-                                             (uint32_t)rows_valid, (uint32_t)a_in, (uint32_t)b_in,
-                                             (uint32_t)a_out, (uint32_t)b_out, pre_log, tw_log);
+  if (S >= 4)
+    dft_tile_v2<C><<<grid, threads, smem, st>>>(in, out, S, lg, (uint32_t)width,
+                                                (uint32_t)rows_valid, (uint32_t)a_in,
+                                                (uint32_t)b_in, (uint32_t)a_out, (uint32_t)b_out,
+                                                pre_log, tw_log);
+  else
+    dft_tile_v<C><<<grid, threads, smem, st>>>(in, out, S, lg, (uint32_t)width,
+                                               (uint32_t)rows_valid, (uint32_t)a_in, (uint32_t)b_in,
+                                               (uint32_t)a_out, (uint32_t)b_out, pre_log, tw_log);
   count_launches(1);
   return cudaGetLastError();
 }
@@ -444,6 +581,8 @@ cudaError_t init_device_tables() {
   if (e == cudaSuccess) e = cudaFuncSetAttribute(dft_tile<1>, cudaFuncAttributeMaxDynamicSharedMemorySize, tile_smem_max(1));
   if (e == cudaSuccess) e = cudaFuncSetAttribute(dft_tile_v<8>, cudaFuncAttributeMaxDynamicSharedMemorySize, tile_smem_max(8));
   if (e == cudaSuccess) e = cudaFuncSetAttribute(dft_tile_v<4>, cudaFuncAttributeMaxDynamicSharedMemorySize, tile_smem_max(4));
+  if (e == cudaSuccess) e = cudaFuncSetAttribute(dft_tile_v2<8>, cudaFuncAttributeMaxDynamicSharedMemorySize, tile_smem_max(8));
+  if (e == cudaSuccess) e = cudaFuncSetAttribute(dft_tile_v2<4>, cudaFuncAttributeMaxDynamicSharedMemorySize, tile_smem_max(4));
   if (e == cudaSuccess) done[dev] = true;
   return e;
 }
