@@ -231,7 +231,7 @@ def run_batched(W, args, device):
     compared with the plain loop's proof of the same job.
     """
     import torch
-    workers = args.workers or max(2, min(12, (os.cpu_count() or 4) - 2))
+    workers = args.workers or max(2, min(16, os.cpu_count() or 4))
     rng = np.random.default_rng(WORKLOAD["seed"] + 17)
     pool = {}
     for k in range(14, 25):

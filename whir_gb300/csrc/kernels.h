@@ -20,6 +20,10 @@ struct Publish {
   unsigned int *counter = nullptr;
   unsigned long long *host = nullptr;
   int words = 0;
+  // optional: after the results, the last CTA stores seq to *flag (pinned
+  // host memory), so the host can wait on that word instead of the stream
+  unsigned int *flag = nullptr;
+  unsigned int seq = 0;
 };
 
 // ---- kernel launches issued by this library (all contexts), for reporting ----
@@ -42,8 +46,10 @@ cudaError_t hash_rows(const uint32_t *rows, size_t n_rows, int row_len, uint32_t
                       cudaStream_t st);
 // all levels above the leaves: level l+1 node i = C(level l node i, node i + n/2)
 // nodes: level 0 (2^log_h digests) first, then each level in turn
-// host_root (optional, device-writable host memory): the root is also written there
-cudaError_t build_tree(uint32_t *nodes, int log_h, cudaStream_t st, uint32_t *host_root = nullptr);
+// host_root (optional, device-writable host memory): the root is also written
+// there, and then seq to *flag (when flag is set)
+cudaError_t build_tree(uint32_t *nodes, int log_h, cudaStream_t st, uint32_t *host_root = nullptr,
+                       unsigned int *flag = nullptr, unsigned int seq = 0);
 // per query: the leaf row then log_h sibling digests bottom-up
 cudaError_t gather_openings(const uint32_t *rows, int row_len, const uint32_t *nodes, int log_h,
                             const uint32_t *idx, int n, uint32_t *out, cudaStream_t st);

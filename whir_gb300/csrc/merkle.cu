@@ -172,7 +172,8 @@ __device__ __forceinline__ void p2q_permute(uint32_t (&x)[4], int l, const uint3
 // CTA, G = 1, to the root), and each node is compressed by a quad of lanes.
 // Threads: 4 per node of the first level made (at most 1024).
 __global__ void __launch_bounds__(1024) tree_subtrees(uint32_t *__restrict__ nodes, int log_h,
-                                                     int l0, int steps, uint32_t *host_root) {
+                                                     int l0, int steps, uint32_t *host_root,
+                                                     unsigned int *flag, unsigned int seq) {
   extern __shared__ uint4 sm[];  // 2 uint4 per node of this CTA's share
   __shared__ uint32_t kc[8 * 16 + 20];
   for (int i = threadIdx.x; i < 8 * 16 + 20; i += blockDim.x) kc[i] = c_p2_16[i];
@@ -211,6 +212,11 @@ __global__ void __launch_bounds__(1024) tree_subtrees(uint32_t *__restrict__ nod
     __syncthreads();
     n = half;
   }
+  if (flag && host_root && gridDim.x == 1) {  // the root is written: raise the flag
+    __threadfence_system();
+    __syncthreads();
+    if (threadIdx.x == 0) *reinterpret_cast<volatile unsigned int *>(flag) = seq;
+  }
 }
 
 // Levels whose step makes at least 2^WIDE_LOG nodes run one thread per node
@@ -219,18 +225,19 @@ __global__ void __launch_bounds__(1024) tree_subtrees(uint32_t *__restrict__ nod
 constexpr int WIDE_LOG = 15;
 
 static cudaError_t launch_subtrees(uint32_t *nodes, int log_h, int l0, int log_g, cudaStream_t st,
-                                   uint32_t *host_root) {
+                                   uint32_t *host_root, unsigned int *flag, unsigned int seq) {
   int steps = log_h - l0 - log_g;
   if (steps <= 0) return cudaSuccess;
   int n = 1 << steps;  // nodes per CTA at level l0
   int threads = 2 * n < 32 ? 32 : 2 * n;  // a quad per node made at the first step
   tree_subtrees<<<1u << log_g, threads, (size_t)n * 32, st>>>(nodes, log_h, l0, steps,
-                                                              host_root);
+                                                              host_root, flag, seq);
   count_launches(1);
   return cudaGetLastError();
 }
 
-cudaError_t build_tree(uint32_t *nodes, int log_h, cudaStream_t st, uint32_t *host_root) {
+cudaError_t build_tree(uint32_t *nodes, int log_h, cudaStream_t st, uint32_t *host_root,
+                       unsigned int *flag, unsigned int seq) {
   const int T = 128;
   int l = 0;
   for (; l < log_h && ((size_t)1 << (log_h - l)) / 2 >= ((size_t)1 << WIDE_LOG); l++) {
@@ -242,9 +249,10 @@ cudaError_t build_tree(uint32_t *nodes, int log_h, cudaStream_t st, uint32_t *ho
   // remaining S = log_h - l steps (S <= WIDE_LOG): G = 2^(S/2) subtrees, then the top
   int S = log_h - l;
   int log_g = S / 2;
-  cudaError_t e = launch_subtrees(nodes, log_h, l, log_g, st, host_root);
+  // only the last launch (one CTA, G = 1) reaches the root
+  cudaError_t e = launch_subtrees(nodes, log_h, l, log_g, st, host_root, flag, seq);
   if (e != cudaSuccess) return e;
-  return launch_subtrees(nodes, log_h, log_h - log_g, 0, st, host_root);
+  return launch_subtrees(nodes, log_h, log_h - log_g, 0, st, host_root, flag, seq);
 }
 
 __global__ void gather_openings_kernel(const uint32_t *__restrict__ rows, int row_len,

@@ -90,6 +90,8 @@ Context::Context(int device) : device_(device) {
   cuda_check(cudaSetDevice(device), "cudaSetDevice");
   cuda_check(cudaStreamCreateWithFlags(&stream_, cudaStreamNonBlocking), "cudaStreamCreate");
   cuda_check(gpu::init_device_tables(), "device tables");
+  cuda_check(cudaMallocHost(&flag_, 64), "cudaMallocHost");
+  *flag_ = 0;
 }
 Context::~Context() {
   cudaSetDevice(device_);
@@ -98,6 +100,8 @@ Context::~Context() {
     cudaEventDestroy(e.b);
   }
   for (auto e : free_events_) cudaEventDestroy(e);
+  if (block_ev_) cudaEventDestroy(block_ev_);
+  if (flag_) cudaFreeHost(flag_);
   if (pinned_) cudaFreeHost(pinned_);
   if (stream_) cudaStreamDestroy(stream_);
 }
@@ -117,14 +121,43 @@ void Context::wait_stream() {
     cuda_check(cudaStreamSynchronize(stream_), "stream sync");
     return;
   }
-  // poll, giving the core to other runnable threads between polls
+  // poll briefly, giving the core to other runnable threads between polls;
+  // then sleep on a blocking-sync event so a waiting worker holds no core
+  auto t0 = std::chrono::steady_clock::now();
   for (;;) {
     cudaError_t e = cudaStreamQuery(stream_);
     if (e == cudaSuccess) return;
     if (e != cudaErrorNotReady) cuda_check(e, "stream sync");
+    if (std::chrono::steady_clock::now() - t0 > std::chrono::microseconds(20)) break;
     std::this_thread::yield();
   }
+  if (!block_ev_)
+    cuda_check(cudaEventCreateWithFlags(&block_ev_, cudaEventBlockingSync | cudaEventDisableTiming),
+               "cudaEventCreate");
+  cuda_check(cudaEventRecord(block_ev_, stream_), "cudaEventRecord");
+  cuda_check(cudaEventSynchronize(block_ev_), "stream sync");
 }
+void Context::wait_flag(unsigned int seq) {
+  auto t0 = std::chrono::steady_clock::now();
+  unsigned long spins = 0;
+  while (__atomic_load_n(flag_, __ATOMIC_ACQUIRE) != seq) {
+    // now and then make sure the stream is alive: a failed launch never
+    // raises the flag, and a finished stream must have raised it
+    if ((++spins & 4095) == 0) {
+      cudaError_t e = cudaStreamQuery(stream_);
+      if (e != cudaSuccess && e != cudaErrorNotReady) cuda_check(e, "stream");
+      if (e == cudaSuccess && __atomic_load_n(flag_, __ATOMIC_ACQUIRE) != seq)
+        throw WhirError(-5, "stream finished without raising the result flag");
+    }
+    if (yield_) std::this_thread::yield();
+  }
+  if (prof_) {
+    acc_ms_[K_SYNC] +=
+        std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t0).count();
+    acc_n_[K_SYNC] += 1;
+  }
+}
+
 void Context::sync() {
   if (!prof_) {
     wait_stream();
@@ -218,12 +251,16 @@ void encode_commit(Context &ctx, const uint32_t *src, int k, int rate, int foldi
   ctx.prof_end(Context::K_LEAF, 4.0 * (double)(rows * width + rows * 8));
   // the last tree launch writes the root straight into pinned host memory
   uint32_t *h = (uint32_t *)ctx.pinned(64);
+  unsigned int seq = ctx.next_seq();
   ctx.prof_begin(Context::K_TREE);
-  cuda_check(gpu::build_tree(nodes, log_h, st, h), "build_tree");
+  cuda_check(gpu::build_tree(nodes, log_h, st, h, ctx.flag(), seq), "build_tree");
   ctx.prof_end(Context::K_TREE, 32.0 * (double)(2 * rows - 2 + rows - 1));
-  if (log_h == 0)  // a single leaf is the root; no tree launch ran
+  if (log_h == 0) {  // a single leaf is the root; no tree launch ran
     cuda_check(copy_async(ctx, h, nodes, 32, cudaMemcpyDeviceToHost), "root copy");
-  ctx.sync();
+    ctx.sync();
+  } else {
+    ctx.wait_flag(seq);  // the last tree launch raised it after writing the root
+  }
   out->rows = codeword;
   out->nodes = nodes;
   out->log_h = log_h;
@@ -446,7 +483,19 @@ struct Prover::Impl {
     p.host = published();
     p.words = words;
     if ((size_t)words > PUB_WORDS) throw WhirError(-5, "reduction too wide to publish");
+    p.flag = ctx->flag();
+    p.seq = pub_seq = ctx->next_seq();
+    args_mark = args_off;
     return p;
+  }
+  // waits for the last publish (its flag) instead of the stream; everything
+  // queued before that launch has completed, so the argument space is free
+  // again unless arguments were queued after it
+  unsigned int pub_seq = 0;
+  size_t args_mark = 0;
+  void wait_published() {
+    ctx->wait_flag(pub_seq);
+    if (args_off == args_mark) args_off = 0;
   }
   unsigned long long *published() { return (unsigned long long *)ctx->pinned(8 * PUB_WORDS); }
   // pinned argument space for host->device copies issued before the next sync
@@ -551,7 +600,7 @@ struct Prover::Impl {
                "compress_hi");
     ctx->prof_end(Context::K_SUMCHECK, 4.0 * (double)((size_t)1 << kp));
     const unsigned long long *h = published();
-    sync();
+    wait_published();
     size_t n = (size_t)1 << ks;
     c.compressed.resize(n);
     for (size_t j = 0; j < n; j++) c.compressed[j] = reduce_acc(h + 4 * j);
@@ -690,7 +739,7 @@ struct Prover::Impl {
   }
   void coeffs_end(E4 *c0, E4 *c2, E4 *extra = nullptr) {
     const unsigned long long *h = published();
-    sync();
+    wait_published();
     *c0 = reduce_acc(h);
     *c2 = reduce_acc(h + 4);
     if (extra) *extra = reduce_acc(h + 8);
@@ -1130,7 +1179,7 @@ struct Prover::Impl {
     unsigned long long *a = acc.as<unsigned long long>();
     cuda_check(gpu::eval_ext(P(), k, lo, s_lo, hi, a, st(), publish(4)), "eval_ext");
     const unsigned long long *h = published();
-    sync();
+    wait_published();
     return reduce_acc(h);
   }
 };

@@ -88,9 +88,15 @@ class Context {
   void *pinned(size_t bytes);  // staging for D2H results and H2D arguments
   void sync();
   // Waiting for the stream: a blocking synchronise (lowest latency, keeps a
-  // core busy), or polling with a yield between polls so that many worker
-  // threads can share the host cores.
+  // core busy), or a short poll with yields followed by a sleep on a
+  // blocking-sync event, so that many worker threads can share the host cores.
   void set_yield_wait(bool on) { yield_ = on; }
+  // A word of pinned host memory that kernels raise to a sequence number
+  // after writing their results there (gpu::Publish): waiting on it costs no
+  // driver call.  next_seq() hands out the number for the next such launch.
+  unsigned int *flag() const { return flag_; }
+  unsigned int next_seq() { return seq_ = seq_ + 1 ? seq_ + 1 : 1; }
+  void wait_flag(unsigned int seq);
   // per-kernel-class CUDA-event timing on this stream
   // kernel classes timed with events, and K_SYNC: host time blocked in sync()
   enum Klass { K_DFT = 0, K_LEAF = 1, K_TREE = 2, K_SUMCHECK = 3, K_SYNC = 4, K_NCLASS = 5 };
@@ -108,6 +114,9 @@ class Context {
   void wait_stream();
   int device_;
   bool yield_ = false;
+  cudaEvent_t block_ev_ = nullptr;
+  unsigned int *flag_ = nullptr;
+  unsigned int seq_ = 0;
   cudaStream_t stream_ = nullptr;
   void *pinned_ = nullptr;
   size_t pinned_bytes_ = 0;

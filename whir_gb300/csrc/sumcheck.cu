@@ -36,6 +36,11 @@ __device__ __forceinline__ void publish_if_last(unsigned long long *acc, const P
   __threadfence();
   for (int i = threadIdx.x; i < pub.words; i += blockDim.x) pub.host[i] = atomicExch(acc + i, 0ull);
   if (threadIdx.x == 0) atomicExch(pub.counter, 0u);
+  if (pub.flag) {
+    __threadfence_system();  // the results reach host memory before the flag
+    __syncthreads();
+    if (threadIdx.x == 0) *reinterpret_cast<volatile unsigned int *>(pub.flag) = pub.seq;
+  }
 }
 
 __global__ void eq_entries(Point z, int off, int nv, E4 scale, E4 *out) {
