@@ -590,7 +590,7 @@ struct Prover::Impl {
     c.k = kp;
     c.point.assign(point, point + kp);
     int nz = kp - ks;
-    int s_lo = std::min(10, nz);
+    int s_lo = std::min(8, nz);  // 2^(nz-8) CTAs: enough loads in flight
     E4 *lo = eqbuf.as<E4>(), *hi = lo + ((size_t)1 << s_lo);
     make_eq_tables({point + ks}, nz, {e_one()}, s_lo, lo);
     size_t na = (size_t)4 << ks;
