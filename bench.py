@@ -92,6 +92,22 @@ def dist_env():
     return world, rank, local
 
 
+def max_over_ranks(x, world, device):
+    """The largest x over all ranks (the slowest replica's time); x on one rank."""
+    if world <= 1:
+        return x
+    import torch
+    t = torch.tensor([x], dtype=torch.float64, device=device)
+    torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+    return float(t.item())
+
+
+def replica_throughput(world, steps, slowest_s):
+    """Whole-job proofs/s of N independent replicas: every rank proves
+    `steps` proofs, the job ends with the slowest rank (weak scaling)."""
+    return world * steps / slowest_s
+
+
 def workload_config(k):
     return {
         "workload": f"WHIR commit+open, 2^{k} KoalaBear evaluations, rate 1/4, folding 4, "
@@ -383,11 +399,8 @@ def run_gb300(args):
                          "share": sync_ms / total_ms if total_ms else None,
                          "note": "host time blocked on the stream (transcript round trips)"}
     prof["wall_ms_per_step"] = wall_ms / args.steps
-    if world > 1:
-        t = torch.tensor([total_ms], dtype=torch.float64, device=f"cuda:{local}")
-        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
-        total_ms = float(t.item())
-    value = world * args.steps / (total_ms * 1e-3)
+    total_ms = max_over_ranks(total_ms, world, f"cuda:{local}")
+    value = replica_throughput(world, args.steps, total_ms * 1e-3)
 
     # ---- e2e: pinned host input through the C ABI ----
     host_t = torch.empty(1 << k, dtype=torch.int32, pin_memory=True)
@@ -413,10 +426,7 @@ def run_gb300(args):
     e2e_s = time.perf_counter() - t0
     _, h2d1, d2h1 = ctx.counters()
     barrier()
-    if world > 1:
-        t = torch.tensor([e2e_s], dtype=torch.float64, device=f"cuda:{local}")
-        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
-        e2e_s = float(t.item())
+    e2e_s = max_over_ranks(e2e_s, world, f"cuda:{local}")
 
     if rank != 0:
         return
@@ -442,7 +452,7 @@ def run_gb300(args):
         "data": "synthetic (seeded Poly::rand, as the reference harness)",
         "config": workload_config(k),
         "latency_ms": {"p50": float(np.percentile(lat, 50)), "p99": float(np.percentile(lat, 99))},
-        "e2e": {"value": world * args.steps / e2e_s, "unit": UNIT,
+        "e2e": {"value": replica_throughput(world, args.steps, e2e_s), "unit": UNIT,
                 "h2d_bytes_per_step": (h2d1 - h2d0) / args.steps,
                 "d2h_bytes_per_step": (d2h1 - d2h0) / args.steps,
                 "latency_ms": {"p50": 1e3 * float(np.percentile(e2e_lat, 50)),
