@@ -360,6 +360,9 @@ def run_gb300(args):
         t.draw_base()
         return t
 
+    # launch splits of this device for the workload's tree heights and DFT
+    # sizes (untimed; outputs do not depend on them)
+    tune_report = W.autotune(ctx, 10, k + WORKLOAD["rate"] - WORKLOAD["folding"])
     for _ in range(args.warmup):
         first = prove_dev()
     gpu_proof = first.finalize()
@@ -472,6 +475,7 @@ def run_gb300(args):
                     "(profiles/hash_rows_fixed_leaf_hash.md)"},
         "kernels": prof,
         "gpu_launches": int(launches1 - launches0),
+        "autotune": tune_report.splitlines(),
         "clocks": clk,
     }
     if not args.no_batched:

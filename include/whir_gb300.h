@@ -258,6 +258,22 @@ WHIR_API int whir_serve_simulate(const double *arrival_s, const uint64_t *need,
 WHIR_API int whir_compress_hi_noalloc(void *cuda_stream, const uint32_t *poly, int k,
                                       const uint32_t *point, int kz, uint32_t *out);
 
+/* ---- launch-split autotuning (no counterpart in the reference).  How a
+ * Merkle tree of height log_h and a two-pass DFT of 2^log_h rows are split
+ * into launches is chosen per size; every choice gives the same result.
+ * whir_autotune times the candidates for log_h in [lo, hi] on the context's
+ * stream (a few hundred ms, up to ~1.5 GB of temporary device memory),
+ * installs the fastest process-wide and writes a text report (one line per
+ * size) into report.  whir_tune_tree / whir_tune_dft set one choice (tree:
+ * levels making >= 2^wide_log nodes run one thread per node, the rest as
+ * 2^((S + split) / 2) subtrees, split in -1..1; DFT: first pass of 2^L1
+ * rows, L1 = (log_h + 1) / 2 + l1_bias); whir_tune_reset restores the
+ * defaults. ---- */
+WHIR_API int whir_autotune(whir_ctx *ctx, int log_h_lo, int log_h_hi, char *report, size_t cap);
+WHIR_API int whir_tune_tree(int log_h, int wide_log, int split);
+WHIR_API int whir_tune_dft(int log_h, size_t width, int l1_bias);
+WHIR_API int whir_tune_reset(void);
+
 /* ---- per-kernel-class timing with CUDA events on the context stream:
  * klass 0 DFT, 1 leaf hash, 2 tree, 3 sumcheck passes; klass 4 is host time
  * blocked waiting for the stream (ms and number of waits).  read returns and

@@ -105,6 +105,11 @@ _SIGS = {
                                         ctypes.c_int, ctypes.c_uint64, ctypes.POINTER(RunStatsC)]),
     "whir_serve": (ctypes.c_int, [ctypes.c_int, ctypes.POINTER(JobC), ctypes.c_int,
                                   ctypes.c_int, ctypes.c_uint64, ctypes.POINTER(RunStatsC)]),
+    "whir_autotune": (ctypes.c_int, [vp, ctypes.c_int, ctypes.c_int, ctypes.c_char_p,
+                                     ctypes.c_size_t]),
+    "whir_tune_tree": (ctypes.c_int, [ctypes.c_int, ctypes.c_int, ctypes.c_int]),
+    "whir_tune_dft": (ctypes.c_int, [ctypes.c_int, ctypes.c_size_t, ctypes.c_int]),
+    "whir_tune_reset": (ctypes.c_int, []),
     "whir_verify": (ctypes.c_int, [ctypes.POINTER(Params), i32p, ctypes.c_int, i32p, ctypes.c_int,
                                    i32p, ctypes.c_char_p, ctypes.c_size_t, i32p, u32p]),
     "whir_server_new": (ctypes.c_int, [ctypes.c_int, ctypes.c_int, ctypes.c_uint64,
@@ -616,3 +621,23 @@ def verify(params, poly_k, groups, proof):
     _check(lib().whir_verify(ctypes.byref(p), ks, len(poly_k), gn, len(groups), gi, bytes(proof),
                              len(proof), ctypes.byref(res), cp.ctypes.data_as(u32p)))
     return res.value, int(cp[0])
+
+
+def autotune(ctx, log_h_lo, log_h_hi):
+    """Pick the fastest tree / DFT launch splits for these sizes (process-wide);
+    returns the text report."""
+    buf = ctypes.create_string_buffer(1 << 16)
+    _check(lib().whir_autotune(ctx.h, log_h_lo, log_h_hi, buf, len(buf)))
+    return buf.value.decode()
+
+
+def tune_tree(log_h, wide_log, split):
+    _check(lib().whir_tune_tree(log_h, wide_log, split))
+
+
+def tune_dft(log_h, width, l1_bias):
+    _check(lib().whir_tune_dft(log_h, width, l1_bias))
+
+
+def tune_reset():
+    _check(lib().whir_tune_reset())

@@ -16,6 +16,7 @@
 #include "poseidon2_host.h"
 #include "batch.h"
 #include "prover.h"
+#include "tune.h"
 #include "verifier.h"
 #include "transcript.h"
 
@@ -702,6 +703,40 @@ int whir_verify(const whir_params *params, const int32_t *poly_k, int n_polys,
   uint32_t cp = 0;
   *result = (int32_t)whir::verify(params_in(params), ks, groups, proof, len, &cp);
   if (checkpoint) *checkpoint = *result == 0 ? cp : 0;
+  API_END
+}
+
+int whir_autotune(whir_ctx *ctx, int log_h_lo, int log_h_hi, char *report, size_t cap) {
+  API_BEGIN
+  need(ctx != nullptr, "null context");
+  std::string r = whir::autotune(ctx->ctx, log_h_lo, log_h_hi);
+  if (report && cap) {
+    size_t n = std::min(cap - 1, r.size());
+    memcpy(report, r.data(), n);
+    report[n] = 0;
+  }
+  API_END
+}
+int whir_tune_tree(int log_h, int wide_log, int split) {
+  API_BEGIN
+  whir::gpu::TreeTune t;
+  t.wide_log = wide_log;
+  t.split = split;
+  need(whir::gpu::tree_tune_valid(log_h, t), "tree split out of range");
+  whir::gpu::set_tree_tune(log_h, t);
+  API_END
+}
+int whir_tune_dft(int log_h, size_t width, int l1_bias) {
+  API_BEGIN
+  whir::gpu::DftTune t;
+  t.l1_bias = l1_bias;
+  need(log_h >= 0 && log_h <= 24 && whir::gpu::dft_tune_valid(log_h, t), "DFT split out of range");
+  whir::gpu::set_dft_tune(log_h, width, t);
+  API_END
+}
+int whir_tune_reset(void) {
+  API_BEGIN
+  whir::tune_reset();
   API_END
 }
 

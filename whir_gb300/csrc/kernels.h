@@ -26,6 +26,27 @@ struct Publish {
   unsigned int seq = 0;
 };
 
+// ---- per-size scheduling choices ----
+// How a tree or a DFT of a given size is split into launches.  Every choice
+// computes the same result; whir::autotune picks them by measurement.
+// Tree: levels that make >= 2^wide_log nodes run one thread per node; the
+// remaining S levels run as 2^((S + split) / 2) strided subtrees, then one
+// CTA to the root.  DFT (two-pass sizes): the first pass transforms columns
+// of 2^L1 rows, L1 = (log_h + 1) / 2 + l1_bias.
+struct TreeTune {
+  int wide_log = 15;
+  int split = 0;
+};
+struct DftTune {
+  int l1_bias = 0;
+};
+TreeTune tree_tune(int log_h);
+void set_tree_tune(int log_h, TreeTune t);
+DftTune dft_tune(int log_h, size_t width);
+void set_dft_tune(int log_h, size_t width, DftTune t);
+bool tree_tune_valid(int log_h, TreeTune t);
+bool dft_tune_valid(int log_h, DftTune t);
+
 // ---- kernel launches issued by this library (all contexts), for reporting ----
 unsigned long long launch_count();
 void count_launches(unsigned n);

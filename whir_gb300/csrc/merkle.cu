@@ -3,6 +3,7 @@
 // opening gather.  Tree shape and hashing follow
 // crates/merkle/src/poseidon_packed.rs:98-143,269-304,344-384 and
 // crates/merkle/src/poseidon.rs:33-74.
+#include <algorithm>
 #include <atomic>
 
 #include "kernels.h"
@@ -219,10 +220,33 @@ __global__ void __launch_bounds__(1024) tree_subtrees(uint32_t *__restrict__ nod
   }
 }
 
-// Levels whose step makes at least 2^WIDE_LOG nodes run one thread per node
-// over the whole GPU; the rest (at most 2^(WIDE_LOG+1) nodes at the first
-// narrow level) go through tree_subtrees.
-constexpr int WIDE_LOG = 15;
+// Default: levels whose step makes at least 2^15 nodes run one thread per
+// node over the whole GPU; the rest (at most 2^16 nodes at the first narrow
+// level) go through tree_subtrees.  Per-size overrides in tree_tune().
+static std::atomic<int> g_tree_tune[41];  // 0: default, else (wide_log << 4) | (split + 2)
+
+TreeTune tree_tune(int log_h) {
+  TreeTune t;
+  if (log_h < 0 || log_h > 40) return t;
+  int v = g_tree_tune[log_h].load(std::memory_order_relaxed);
+  if (v) {
+    t.wide_log = v >> 4;
+    t.split = (v & 15) - 2;
+  }
+  return t;
+}
+bool tree_tune_valid(int log_h, TreeTune t) {
+  if (t.wide_log < 10 || t.wide_log > 18 || t.split < -1 || t.split > 1) return false;
+  // the narrow part has S <= wide_log levels; both subtree launches hold at
+  // most 512 nodes per CTA (1024 threads)
+  int S = std::min(log_h, t.wide_log);
+  int log_g = std::max(0, std::min(S, (S + t.split) / 2));
+  return S - log_g <= 9 && log_g <= 9;
+}
+void set_tree_tune(int log_h, TreeTune t) {
+  if (log_h < 0 || log_h > 40 || !tree_tune_valid(log_h, t)) return;
+  g_tree_tune[log_h].store((t.wide_log << 4) | (t.split + 2), std::memory_order_relaxed);
+}
 
 static cudaError_t launch_subtrees(uint32_t *nodes, int log_h, int l0, int log_g, cudaStream_t st,
                                    uint32_t *host_root, unsigned int *flag, unsigned int seq) {
@@ -239,16 +263,19 @@ static cudaError_t launch_subtrees(uint32_t *nodes, int log_h, int l0, int log_g
 cudaError_t build_tree(uint32_t *nodes, int log_h, cudaStream_t st, uint32_t *host_root,
                        unsigned int *flag, unsigned int seq) {
   const int T = 128;
+  TreeTune tune = tree_tune(log_h);
+  if (!tree_tune_valid(log_h, tune)) tune = TreeTune();
   int l = 0;
-  for (; l < log_h && ((size_t)1 << (log_h - l)) / 2 >= ((size_t)1 << WIDE_LOG); l++) {
+  for (; l < log_h && ((size_t)1 << (log_h - l)) / 2 >= ((size_t)1 << tune.wide_log); l++) {
     size_t half = ((size_t)1 << (log_h - l)) / 2;
     compress_level<<<(unsigned)((half + T - 1) / T), T, 0, st>>>(
         nodes + level_offset_words(log_h, l), nodes + level_offset_words(log_h, l + 1), half);
     count_launches(1);
   }
-  // remaining S = log_h - l steps (S <= WIDE_LOG): G = 2^(S/2) subtrees, then the top
+  // remaining S = log_h - l steps (S <= wide_log): G = 2^((S + split)/2)
+  // subtrees, then the top
   int S = log_h - l;
-  int log_g = S / 2;
+  int log_g = std::max(0, std::min(S, (S + tune.split) / 2));
   // only the last launch (one CTA, G = 1) reaches the root
   cudaError_t e = launch_subtrees(nodes, log_h, l, log_g, st, host_root, flag, seq);
   if (e != cudaSuccess) return e;

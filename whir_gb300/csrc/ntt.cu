@@ -17,6 +17,7 @@
 // Each pass reads and writes the matrix once with full 32-byte sectors (a
 // CTA owns 8 columns = 32 bytes of every row it touches).  Zero padding is
 // never materialised: rows >= h_in are read as zero in pass 1.
+#include <atomic>
 #include <mutex>
 
 #include "kernels.h"
@@ -536,6 +537,25 @@ static cudaError_t tile_any(const uint32_t *in, uint32_t *out, int S, size_t wid
                         pre_log, tw_log, st);
 }
 
+// per-size overrides of the two-pass split (0: default), by log_h and width class
+static std::atomic<int> g_dft_tune[25][2];
+static int width_class(size_t width) { return width > 16 ? 1 : 0; }
+DftTune dft_tune(int log_h, size_t width) {
+  DftTune t;
+  if (log_h < 0 || log_h > 24) return t;
+  int v = g_dft_tune[log_h][width_class(width)].load(std::memory_order_relaxed);
+  if (v) t.l1_bias = v - 8;
+  return t;
+}
+bool dft_tune_valid(int log_h, DftTune t) {
+  int L1 = (log_h + 1) / 2 + t.l1_bias, L2 = log_h - L1;
+  return t.l1_bias >= -2 && t.l1_bias <= 2 && L1 >= 4 && L2 >= 4 && L1 <= 11 && L2 <= 11;
+}
+void set_dft_tune(int log_h, size_t width, DftTune t) {
+  if (log_h < 0 || log_h > 24 || !dft_tune_valid(log_h, t)) return;
+  g_dft_tune[log_h][width_class(width)].store(t.l1_bias + 8, std::memory_order_relaxed);
+}
+
 cudaError_t dft_batch(const uint32_t *in, size_t h_in, size_t width, int log_h, uint32_t *out,
                       uint32_t *scratch, cudaStream_t st) {
   if (log_h < 0 || log_h > 24 || width == 0) return cudaErrorInvalidValue;
@@ -554,8 +574,10 @@ cudaError_t dft_batch(const uint32_t *in, size_t h_in, size_t width, int log_h, 
     size_t M1 = h >> L0;
     return tile_any(in, out, L0, width, h_in, M1, 0, 1, 1, M1, log_h, 0, st);
   }
-  int L1 = (log_h + 1) / 2, L2 = log_h - L1;
-  if (L1 > MAX_TILE_LOG) return cudaErrorInvalidValue;
+  DftTune tune = dft_tune(log_h, width);
+  if (!dft_tune_valid(log_h, tune)) tune = DftTune();
+  int L1 = (log_h + 1) / 2 + tune.l1_bias, L2 = log_h - L1;
+  if (L1 > MAX_TILE_LOG || L2 > MAX_TILE_LOG) return cudaErrorInvalidValue;
   size_t M1 = (size_t)1 << L1, M2 = (size_t)1 << L2;
   cudaError_t e = tile_any(in, scratch, L1, width, h_in, M2, 1, M2, 1, M2, 0, log_h, st);
   if (e != cudaSuccess) return e;
