@@ -432,7 +432,7 @@ __device__ __forceinline__ void dif_last_v(const uint4 *tile, const uint32_t *tw
 }
 
 template <int C>
-__global__ void __launch_bounds__(256) dft_tile_v2(const uint32_t *__restrict__ in,
+__global__ void __launch_bounds__(256, 4) dft_tile_v2(const uint32_t *__restrict__ in,
                                                    uint32_t *__restrict__ out, int S, int lg,
                                                    uint32_t width, uint32_t rows_valid,
                                                    uint32_t a_in, uint32_t b_in, uint32_t a_out,
@@ -474,8 +474,9 @@ static cudaError_t launch_tile_v(const uint32_t *in, uint32_t *out, int S, size_
                                  size_t rows_valid, size_t n_outer, size_t a_in, size_t b_in,
                                  size_t a_out, size_t b_out, int pre_log, int tw_log,
                                  cudaStream_t st) {
+  // pack small sub-transforms so that a CTA holds at least 2^10 rows
   int lg = 0;
-  while (S + lg < 11 && ((size_t)2 << lg) <= n_outer) lg++;
+  while (S + lg < 10 && ((size_t)2 << lg) <= n_outer) lg++;
   size_t rows = (size_t)1 << (S + lg);
   size_t smem = (rows * C + rows) * 4;
   int threads = (int)(rows * (C / 4) / 8);
