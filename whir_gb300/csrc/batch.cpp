@@ -196,6 +196,8 @@ RunStats Server::run(std::vector<Job> &jobs, bool honor_arrival) {
   auto exec = [device](void *state, Job &job) -> size_t {
     cuda_check(cudaSetDevice(device), "cudaSetDevice");
     auto *w = static_cast<GpuWorker *>(state);
+    // large jobs set the tail latency: their blocks go first on the device
+    w->ctx->set_high_priority(job.params.k >= Server::kPriorityK);
     if (!w->prover) w->prover.reset(new Prover(w->ctx.get(), job.params));
     else w->prover->set_params(job.params);
     Transcript ts;

@@ -98,6 +98,8 @@ class Server {
   Server &operator=(const Server &) = delete;
   RunStats run(std::vector<Job> &jobs, bool honor_arrival);
   int workers() const { return (int)states_.size(); }
+  // jobs of at least 2^kPriorityK evaluations run on high-priority streams
+  static constexpr int kPriorityK = 22;
 
  private:
   int device_;

@@ -88,7 +88,13 @@ void DeviceBuffer::reserve(size_t bytes) {
 
 Context::Context(int device) : device_(device) {
   cuda_check(cudaSetDevice(device), "cudaSetDevice");
-  cuda_check(cudaStreamCreateWithFlags(&stream_, cudaStreamNonBlocking), "cudaStreamCreate");
+  int least = 0, greatest = 0;
+  cuda_check(cudaDeviceGetStreamPriorityRange(&least, &greatest), "stream priorities");
+  cuda_check(cudaStreamCreateWithPriority(&streams_[0], cudaStreamNonBlocking, least),
+             "cudaStreamCreate");
+  cuda_check(cudaStreamCreateWithPriority(&streams_[1], cudaStreamNonBlocking, greatest),
+             "cudaStreamCreate");
+  stream_ = streams_[0];
   cuda_check(gpu::init_device_tables(), "device tables");
   cuda_check(cudaMallocHost(&flag_, 64), "cudaMallocHost");
   *flag_ = 0;
@@ -103,7 +109,8 @@ Context::~Context() {
   if (block_ev_) cudaEventDestroy(block_ev_);
   if (flag_) cudaFreeHost(flag_);
   if (pinned_) cudaFreeHost(pinned_);
-  if (stream_) cudaStreamDestroy(stream_);
+  for (auto s : streams_)
+    if (s) cudaStreamDestroy(s);
 }
 void *Context::pinned(size_t bytes) {
   if (bytes > pinned_bytes_) {
@@ -137,6 +144,13 @@ void Context::wait_stream() {
   cuda_check(cudaEventRecord(block_ev_, stream_), "cudaEventRecord");
   cuda_check(cudaEventSynchronize(block_ev_), "stream sync");
 }
+void Context::set_high_priority(bool on) {
+  cudaStream_t want = streams_[on ? 1 : 0];
+  if (want == stream_) return;
+  cuda_check(cudaStreamSynchronize(stream_), "stream sync");
+  stream_ = want;
+}
+
 void Context::wait_flag(unsigned int seq) {
   auto t0 = std::chrono::steady_clock::now();
   unsigned long spins = 0;

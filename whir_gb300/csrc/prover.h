@@ -85,6 +85,10 @@ class Context {
   ~Context();
   int device() const { return device_; }
   cudaStream_t stream() const { return stream_; }
+  // Runs the following work on a high-priority stream (the device schedules
+  // its blocks first) or back on the normal one; waits for the current
+  // stream first.
+  void set_high_priority(bool on);
   void *pinned(size_t bytes);  // staging for D2H results and H2D arguments
   void sync();
   // Waiting for the stream: a blocking synchronise (lowest latency, keeps a
@@ -118,6 +122,7 @@ class Context {
   unsigned int *flag_ = nullptr;
   unsigned int seq_ = 0;
   cudaStream_t stream_ = nullptr;
+  cudaStream_t streams_[2] = {nullptr, nullptr};  // normal, high priority
   void *pinned_ = nullptr;
   size_t pinned_bytes_ = 0;
   bool prof_ = false;
