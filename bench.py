@@ -48,6 +48,12 @@ UNIT = "proofs/s"
 # command and the per-launch figures are in profiles/hash_rows_fixed_leaf_hash.md.
 NCU_TRAFFIC_BYTES = {"leaf_hash": 294.6e6}
 NCU_TRAFFIC_K = 24
+# Thread instructions per width-24 permutation of the leaf hash
+# (smsp__inst_executed.sum * 32 / permutations, same ncu capture file).  With
+# one warp instruction issued per cycle on each of the 4 sub-partitions of
+# each SM, the issue-bound rate is SMs * 4 * 32 * clock / this.
+LEAF_INSTR_PER_PERM24 = 8735
+GB300_SMS = 152
 
 
 def leaf_permutations(k, folding, rate, initial_reduction):
@@ -106,6 +112,24 @@ def replica_throughput(world, steps, slowest_s):
     """Whole-job proofs/s of N independent replicas: every rank proves
     `steps` proofs, the job ends with the slowest rank (weak scaling)."""
     return world * steps / slowest_s
+
+
+def integer_roofline(k, prof, clk):
+    """The leaf hash against the integer issue rate: achieved width-24
+    permutations/s over SMs * 4 * 32 * SM clock / instructions per permutation."""
+    ms = prof["leaf_hash"]["ms_per_step"]
+    if not ms:
+        return None
+    perms = leaf_permutations(k, WORKLOAD["folding"], WORKLOAD["rate"],
+                              WORKLOAD["initial_reduction"])
+    achieved = perms / (ms * 1e-3)
+    mhz = clk.get("sm_mhz") or 2070.0
+    peak = GB300_SMS * 4 * 32 * mhz * 1e6 / LEAF_INSTR_PER_PERM24
+    return {"kernel": "leaf_hash", "bound": "integer issue", "unit": "perm24/s",
+            "achieved": achieved, "peak": peak, "frac": achieved / peak,
+            "peak_source": f"{LEAF_INSTR_PER_PERM24} instructions per permutation (ncu) at "
+                           f"{mhz:.0f} MHz, 152 SMs x 4 issue slots",
+            "note": "profiles/hash_rows_fixed_leaf_hash.md"}
 
 
 def workload_config(k):
@@ -465,14 +489,7 @@ def run_gb300(args):
                      "peak_source": peak_src, "traffic": traffic,
                      "per_launch_ms": per_launch_ms,
                      "note": "Poseidon2 hashing is integer-pipe bound; frac is against HBM"},
-        "integer_pipe": {
-            "kernel": "leaf_hash",
-            "perm24_per_s": leaf_permutations(k, WORKLOAD["folding"], WORKLOAD["rate"],
-                                              WORKLOAD["initial_reduction"]) /
-                            (prof["leaf_hash"]["ms_per_step"] * 1e-3)
-                            if prof["leaf_hash"]["ms_per_step"] else None,
-            "note": "issue ~68% and FMA-heavy/ALU pipes ~70% busy under ncu "
-                    "(profiles/hash_rows_fixed_leaf_hash.md)"},
+        "integer_pipe": integer_roofline(k, prof, clk),
         "kernels": prof,
         "gpu_launches": int(launches1 - launches0),
         "autotune": tune_report.splitlines(),
