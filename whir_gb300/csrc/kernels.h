@@ -74,6 +74,14 @@ cudaError_t build_tree(uint32_t *nodes, int log_h, cudaStream_t st, uint32_t *ho
 // per query: the leaf row then log_h sibling digests bottom-up
 cudaError_t gather_openings(const uint32_t *rows, int row_len, const uint32_t *nodes, int log_h,
                             const uint32_t *idx, int n, uint32_t *out, cudaStream_t st);
+// the same with at most IdxArgs::N indexes passed by value
+struct IdxArgs {
+  static constexpr int N = 2048;
+  uint32_t idx[N];
+};
+cudaError_t gather_openings_val(const uint32_t *rows, int row_len, const uint32_t *nodes,
+                                int log_h, const IdxArgs &a, int n, uint32_t *out,
+                                cudaStream_t st);
 KB_HD size_t tree_words(int log_h) { return (((size_t)2 << log_h) - 1) * 8; }
 KB_HD size_t level_offset_words(int log_h, int level) {
   return (((size_t)2 << log_h) - ((size_t)2 << (log_h - level))) * 8;
@@ -94,6 +102,14 @@ cudaError_t eq_split(const Point &z, int s, kb::E4 scale, kb::E4 *lo, kb::E4 *hi
 // rest times scales[t]
 cudaError_t eq_tables(const kb::E4 *pts, const kb::E4 *scales, int n, int k, int s, kb::E4 *out,
                       cudaStream_t st);
+// eq_tables with at most EqArgs::N points of at most EqArgs::K coordinates
+// passed by value (no device copy of the points)
+struct EqArgs {
+  static constexpr int N = 8, K = 32;
+  kb::E4 z[N * K];  // point t at z[t * K]
+  kb::E4 scale[N];
+};
+cudaError_t eq_tables_val(const EqArgs &a, int n, int k, int s, kb::E4 *out, cudaStream_t st);
 // full table eq(z) * scale of 2^k entries (k <= 24)
 cudaError_t eq_full(const Point &z, kb::E4 scale, kb::E4 *out, kb::E4 *tmp, cudaStream_t st);
 

@@ -282,13 +282,9 @@ cudaError_t build_tree(uint32_t *nodes, int log_h, cudaStream_t st, uint32_t *ho
   return launch_subtrees(nodes, log_h, log_h - log_g, 0, st, host_root, flag, seq);
 }
 
-__global__ void gather_openings_kernel(const uint32_t *__restrict__ rows, int row_len,
-                                       const uint32_t *__restrict__ nodes, int log_h,
-                                       const uint32_t *__restrict__ idx, int n,
-                                       uint32_t *__restrict__ out) {
-  int q = blockIdx.x;
-  if (q >= n) return;
-  size_t index = idx[q];
+__device__ __forceinline__ void gather_one(const uint32_t *__restrict__ rows, int row_len,
+                                           const uint32_t *__restrict__ nodes, int log_h,
+                                           size_t index, int q, uint32_t *__restrict__ out) {
   size_t per = (size_t)row_len + 8 * (size_t)log_h;
   uint32_t *o = out + q * per;
   for (int j = threadIdx.x; j < row_len; j += blockDim.x) o[j] = rows[index * row_len + j];
@@ -300,6 +296,34 @@ __global__ void gather_openings_kernel(const uint32_t *__restrict__ rows, int ro
     size_t sib = (index & mask) ^ mid;
     o[row_len + t] = nodes[level_offset_words(log_h, l) + sib * 8 + w];
   }
+}
+
+__global__ void gather_openings_kernel(const uint32_t *__restrict__ rows, int row_len,
+                                       const uint32_t *__restrict__ nodes, int log_h,
+                                       const uint32_t *__restrict__ idx, int n,
+                                       uint32_t *__restrict__ out) {
+  int q = blockIdx.x;
+  if (q >= n) return;
+  gather_one(rows, row_len, nodes, log_h, idx[q], q, out);
+}
+// the same with the indexes passed by value
+__global__ void gather_openings_val_kernel(const uint32_t *__restrict__ rows, int row_len,
+                                           const uint32_t *__restrict__ nodes, int log_h,
+                                           const __grid_constant__ IdxArgs a, int n,
+                                           uint32_t *__restrict__ out) {
+  int q = blockIdx.x;
+  if (q >= n) return;
+  gather_one(rows, row_len, nodes, log_h, a.idx[q], q, out);
+}
+
+cudaError_t gather_openings_val(const uint32_t *rows, int row_len, const uint32_t *nodes,
+                                int log_h, const IdxArgs &a, int n, uint32_t *out,
+                                cudaStream_t st) {
+  if (n == 0) return cudaSuccess;
+  if (n > IdxArgs::N) return cudaErrorInvalidValue;
+  gather_openings_val_kernel<<<n, 128, 0, st>>>(rows, row_len, nodes, log_h, a, n, out);
+  count_launches(1);
+  return cudaGetLastError();
 }
 
 cudaError_t gather_openings(const uint32_t *rows, int row_len, const uint32_t *nodes, int log_h,

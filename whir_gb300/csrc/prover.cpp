@@ -535,6 +535,15 @@ struct Prover::Impl {
                       int s, E4 *out) {
     size_t n = pts.size();
     if (n == 0) return;
+    if (n <= (size_t)gpu::EqArgs::N && k <= gpu::EqArgs::K) {  // by value: no upload
+      gpu::EqArgs a;
+      for (size_t t = 0; t < n; t++) {
+        std::copy(pts[t], pts[t] + k, a.z + t * gpu::EqArgs::K);
+        a.scale[t] = scales[t];
+      }
+      cuda_check(gpu::eq_tables_val(a, (int)n, k, s, out, st()), "eq_tables");
+      return;
+    }
     std::vector<E4> host(n * k + n);
     for (size_t t = 0; t < n; t++) {
       std::copy(pts[t], pts[t] + k, host.begin() + t * k);
@@ -941,20 +950,28 @@ struct Prover::Impl {
     int n = (int)idx.size();
     if (n == 0) return 0;
     size_t per = (size_t)t.row_len + 8 * (size_t)t.log_h;
-    size_t need = 4 * (size_t)n + 16;
-    if (need > gather.bytes()) {
-      sync();  // an earlier gather may still be in flight
-      gather.reserve(2 * need);
-    }
-    std::vector<uint32_t> hidx(n);
-    for (int i = 0; i < n; i++) hidx[i] = (uint32_t)idx[i];
-    uint32_t *didx = gather.as<uint32_t>();
-    upload(didx, hidx.data(), 4 * (size_t)n);
     // the gather writes the hint words straight into the deferred pinned area
     size_t off = defer_alloc(per * n, ts);
-    cuda_check(gpu::gather_openings(t.rows, t.row_len, t.nodes, t.log_h, didx, n, defer_ptr(off),
-                                    st()),
-               "gather");
+    if (n <= gpu::IdxArgs::N) {  // indexes by value: no upload
+      static thread_local gpu::IdxArgs a;
+      for (int i = 0; i < n; i++) a.idx[i] = (uint32_t)idx[i];
+      cuda_check(gpu::gather_openings_val(t.rows, t.row_len, t.nodes, t.log_h, a, n,
+                                          defer_ptr(off), st()),
+                 "gather");
+    } else {
+      size_t need = 4 * (size_t)n + 16;
+      if (need > gather.bytes()) {
+        sync();  // an earlier gather may still be in flight
+        gather.reserve(2 * need);
+      }
+      std::vector<uint32_t> hidx(n);
+      for (int i = 0; i < n; i++) hidx[i] = (uint32_t)idx[i];
+      uint32_t *didx = gather.as<uint32_t>();
+      upload(didx, hidx.data(), 4 * (size_t)n);
+      cuda_check(gpu::gather_openings(t.rows, t.row_len, t.nodes, t.log_h, didx, n,
+                                      defer_ptr(off), st()),
+                 "gather");
+    }
     ctx->count_copy(4 * per * n, cudaMemcpyDeviceToHost);
     for (int i = 0; i < n; i++)
       pending_hints.push_back(PendingHint{ts.hint_reserve(per), off + per * i, per});

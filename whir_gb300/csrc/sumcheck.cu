@@ -90,6 +90,40 @@ cudaError_t eq_tables(const E4 *pts, const E4 *scales, int n, int k, int s, E4 *
   return cudaGetLastError();
 }
 
+// the same tables with the points passed by value in the kernel parameters
+// (no upload on the stream)
+__global__ void eq_tables_val_kernel(const __grid_constant__ EqArgs a, int k, int s,
+                                     E4 *__restrict__ out) {
+  const int t = blockIdx.y;
+  const size_t nlo = (size_t)1 << s, per = nlo + ((size_t)1 << (k - s));
+  size_t x = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (x >= per) return;
+  const E4 *z = a.z + t * EqArgs::K;
+  E4 acc;
+  int off, nv;
+  size_t b;
+  if (x < nlo) {
+    acc = kb::e_one(); off = 0; nv = s; b = x;
+  } else {
+    acc = a.scale[t]; off = s; nv = k - s; b = x - nlo;
+  }
+  for (int i = 0; i < nv; i++) {
+    E4 zi = z[off + i];
+    acc = kb::e_mul(acc, ((b >> i) & 1) ? zi : kb::e_sub(kb::e_one(), zi));
+  }
+  out[(size_t)t * per + x] = acc;
+}
+
+cudaError_t eq_tables_val(const EqArgs &a, int n, int k, int s, E4 *out, cudaStream_t st) {
+  if (n == 0) return cudaSuccess;
+  if (n > EqArgs::N || k > EqArgs::K || s < 0 || s > k) return cudaErrorInvalidValue;
+  size_t per = ((size_t)1 << s) + ((size_t)1 << (k - s));
+  dim3 grid((unsigned)((per + 127) / 128), (unsigned)n);
+  eq_tables_val_kernel<<<grid, 128, 0, st>>>(a, k, s, out);
+  count_launches(1);
+  return cudaGetLastError();
+}
+
 static cudaError_t eq_part(const Point &z, int off, int nv, E4 scale, E4 *out, cudaStream_t st) {
   size_t n = (size_t)1 << nv;
   unsigned T = 256, G = (unsigned)((n + T - 1) / T);
