@@ -82,6 +82,8 @@ def parse():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--cpu-seconds", type=float, default=12.0,
                     help="time budget of the bounded CPU baseline sample")
+    ap.add_argument("--no-autotune", action="store_true",
+                    help="keep the default launch splits (profiling runs)")
     ap.add_argument("--no-batched", action="store_true",
                     help="skip the batched / served workloads")
     ap.add_argument("--workers", type=int, default=0,
@@ -386,7 +388,8 @@ def run_gb300(args):
 
     # launch splits of this device for the workload's tree heights and DFT
     # sizes (untimed; outputs do not depend on them)
-    tune_report = W.autotune(ctx, 10, k + WORKLOAD["rate"] - WORKLOAD["folding"])
+    tune_report = "" if args.no_autotune else W.autotune(
+        ctx, 10, k + WORKLOAD["rate"] - WORKLOAD["folding"])
     for _ in range(args.warmup):
         first = prove_dev()
     gpu_proof = first.finalize()

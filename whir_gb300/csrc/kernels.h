@@ -131,6 +131,14 @@ cudaError_t add_eq(kb::E4 *w, int k, const kb::E4 *tables, int n_tables, cudaStr
 size_t add_pows_scratch_words(int k, int n);
 cudaError_t add_pows(kb::E4 *w, int k, const uint32_t *vars, const kb::E4 *scales, int n,
                      uint32_t *tab, cudaStream_t st);
+// add_pows with at most PowArgs::N variables and scales passed by value
+struct PowArgs {
+  static constexpr int N = 256;
+  uint32_t vars[N];
+  kb::E4 scales[N];
+};
+cudaError_t add_pows_val(kb::E4 *w, int k, const PowArgs &a, int n, uint32_t *tab,
+                         cudaStream_t st);
 // one sumcheck round (expr.rs:14-27, poly.rs:131-142): optionally fold both
 // arrays by r into (p_out, w_out), then add (c0, c2) of the result into acc
 // (u64[8], unreduced canonical) when coeffs != 0.

@@ -836,6 +836,16 @@ struct Prover::Impl {
   // space, so no sync is needed here
   void add_pows(const std::vector<uint32_t> &vars, const std::vector<E4> &scales) {
     if (vars.empty()) return;
+    if (vars.size() <= (size_t)gpu::PowArgs::N) {  // by value: no upload
+      static thread_local gpu::PowArgs a;
+      std::copy(vars.begin(), vars.end(), a.vars);
+      std::copy(scales.begin(), scales.end(), a.scales);
+      size_t tw = gpu::add_pows_scratch_words(kc, (int)vars.size());
+      if (4 * tw > eqbuf.bytes()) eqbuf.reserve(4 * tw);
+      cuda_check(gpu::add_pows_val(W(), kc, a, (int)vars.size(), eqbuf.as<uint32_t>(), st()),
+                 "add_pows");
+      return;
+    }
     size_t bytes = vars.size() * 4 + scales.size() * 16;
     std::vector<uint8_t> h(bytes);
     memcpy(h.data(), scales.data(), scales.size() * 16);

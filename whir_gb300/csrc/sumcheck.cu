@@ -315,6 +315,45 @@ __global__ void add_pows_kernel(E4 *__restrict__ w, size_t n_out, int s, int n,
   w[i] = acc;
 }
 
+// the same two passes with the variables and scales passed by value
+__global__ void pow_tables_val_kernel(const __grid_constant__ PowArgs a, int n, int s, int k,
+                                      uint32_t *__restrict__ tab) {
+  const size_t nlo = (size_t)1 << s, per = nlo + ((size_t)1 << (k - s));
+  size_t x = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (x >= (size_t)n * per) return;
+  size_t t = x / per, j = x % per;
+  uint64_t e = j < nlo ? j : (uint64_t)(j - nlo) << s;
+  tab[x] = kb::pow(a.vars[t], e);
+}
+__global__ void add_pows_val_kernel(E4 *__restrict__ w, size_t n_out, int s, int n,
+                                    const uint32_t *__restrict__ tab,
+                                    const __grid_constant__ PowArgs a) {
+  size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n_out) return;
+  const size_t nlo = (size_t)1 << s, per = nlo + (n_out >> s);
+  const size_t il = i & (nlo - 1), ih = nlo + (i >> s);
+  E4 acc = w[i];
+  for (int t = 0; t < n; t++) {
+    const uint32_t *tb = tab + (size_t)t * per;
+    uint32_t pw = kb::mul(__ldg(tb + il), __ldg(tb + ih));
+    acc = kb::e_add(acc, kb::e_scale(a.scales[t], pw));
+  }
+  w[i] = acc;
+}
+
+cudaError_t add_pows_val(E4 *w, int k, const PowArgs &a, int n, uint32_t *tab, cudaStream_t st) {
+  if (n == 0) return cudaSuccess;
+  if (n > PowArgs::N) return cudaErrorInvalidValue;
+  int s = k / 2;
+  size_t words = add_pows_scratch_words(k, n);
+  pow_tables_val_kernel<<<(unsigned)((words + 255) / 256), 256, 0, st>>>(a, n, s, k, tab);
+  count_launches(1);
+  size_t N = (size_t)1 << k;
+  add_pows_val_kernel<<<(unsigned)((N + 255) / 256), 256, 0, st>>>(w, N, s, n, tab, a);
+  count_launches(1);
+  return cudaGetLastError();
+}
+
 size_t add_pows_scratch_words(int k, int n) {
   int s = k / 2;
   return (size_t)n * (((size_t)1 << s) + ((size_t)1 << (k - s)));
