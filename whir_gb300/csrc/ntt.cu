@@ -28,6 +28,9 @@ namespace gpu {
 // powers of the 2^24-th root of unity: w^e = lo[e & 4095] * hi[e >> 12]
 __device__ uint32_t g_tw_lo[4096];
 __device__ uint32_t g_tw_hi[4096];
+// DIF twiddles: g_dif[h + pos] = w_{2h}^pos for h = 1, 2, .., 2048 and pos < h
+// (the entry depends on the index alone, so one table serves every size)
+__device__ uint32_t g_dif[4096];
 
 static const uint32_t ROOT24 = 0x6ac49f88u;  // two_adic_generator(24), canonical
 
@@ -42,8 +45,17 @@ static cudaError_t upload_device_tables() {
     lo[i] = kb::mul(lo[i - 1], w);
     hi[i] = kb::mul(hi[i - 1], w4096);
   }
+  static uint32_t dif[4096];
+  dif[0] = 0;
+  for (int x = 1; x < 4096; x++) {
+    int lh = 31 - __builtin_clz((unsigned)x);
+    uint32_t pos = (uint32_t)(x - (1 << lh));
+    uint32_t e = pos << (24 - 1 - lh);  // w_{2^(lh+1)}^pos = w_24^(pos 2^(23-lh))
+    dif[x] = kb::mul(lo[e & 4095], hi[e >> 12]);
+  }
   cudaError_t e = cudaMemcpyToSymbol(g_tw_lo, lo, sizeof lo);
   if (e == cudaSuccess) e = cudaMemcpyToSymbol(g_tw_hi, hi, sizeof hi);
+  if (e == cudaSuccess) e = cudaMemcpyToSymbol(g_dif, dif, sizeof dif);
   if (e == cudaSuccess) e = init_poseidon2_tables();
   return e;
 }
@@ -441,18 +453,13 @@ __global__ void __launch_bounds__(256, 4) dft_tile_v2(const uint32_t *__restrict
   extern __shared__ uint4 smv[];
   const int n = 1 << S, rows = n << lg;
   uint4 *tile = smv;
-  uint32_t *aux = reinterpret_cast<uint32_t *>(smv + rows * V);  // DIF twiddles only
+  const uint32_t *aux = g_dif;  // DIF twiddles (global, read through the L1)
   const uint32_t o0 = blockIdx.y << lg;
   const uint32_t v0 = blockIdx.x * V;
   const uint32_t wv = width / 4;
   const uint4 *in4 = reinterpret_cast<const uint4 *>(in);
   uint4 *out4 = reinterpret_cast<uint4 *>(out);
-  for (int x = threadIdx.x + 1; x < n; x += blockDim.x) {
-    int lh = 31 - __clz(x);
-    uint32_t pos = (uint32_t)(x - (1 << lh));
-    aux[x] = root_pow(pos << (24 - 1 - lh));  // w_{2^(lh+1)}^pos
-  }
-  __syncthreads();
+  (void)n;
   const int rows_log = S + lg;
   const int r0 = S % 3 == 0 ? 3 : S % 3;
   if (r0 == 1)
@@ -483,7 +490,7 @@ static cudaError_t launch_tile_v(const uint32_t *in, uint32_t *out, int S, size_
   threads = threads < 32 ? 32 : (threads > 256 ? 256 : threads);
   dim3 grid((unsigned)(width / C), (unsigned)(n_outer >> lg));
   if (S >= 4)
-    dft_tile_v2<C><<<grid, threads, smem, st>>>(in, out, S, lg, (uint32_t)width,
+    dft_tile_v2<C><<<grid, threads, rows * C * 4, st>>>(in, out, S, lg, (uint32_t)width,
                                                 (uint32_t)rows_valid, (uint32_t)a_in,
                                                 (uint32_t)b_in, (uint32_t)a_out, (uint32_t)b_out,
                                                 pre_log, tw_log);
