@@ -31,6 +31,8 @@ __device__ uint32_t g_tw_hi[4096];
 // DIF twiddles: g_dif[h + pos] = w_{2h}^pos for h = 1, 2, .., 2048 and pos < h
 // (the entry depends on the index alone, so one table serves every size)
 __device__ uint32_t g_dif[4096];
+// the same twiddles for Shoup products: {plain value w, floor(w 2^32 / p)}
+__device__ uint2 g_dif2[4096];
 
 static const uint32_t ROOT24 = 0x6ac49f88u;  // two_adic_generator(24), canonical
 
@@ -56,6 +58,12 @@ static cudaError_t upload_device_tables() {
   cudaError_t e = cudaMemcpyToSymbol(g_tw_lo, lo, sizeof lo);
   if (e == cudaSuccess) e = cudaMemcpyToSymbol(g_tw_hi, hi, sizeof hi);
   if (e == cudaSuccess) e = cudaMemcpyToSymbol(g_dif, dif, sizeof dif);
+  static uint2 dif2[4096];
+  for (int x = 0; x < 4096; x++) {
+    uint32_t w = kb::to_canonical(dif[x]);
+    dif2[x] = make_uint2(w, (uint32_t)(((uint64_t)w << 32) / kb::P));
+  }
+  if (e == cudaSuccess) e = cudaMemcpyToSymbol(g_dif2, dif2, sizeof dif2);
   if (e == cudaSuccess) e = init_poseidon2_tables();
   return e;
 }
@@ -235,11 +243,35 @@ __device__ __forceinline__ uint4 mul4(uint4 a, uint32_t w) {
   return make_uint4(kb::mul(a.x, w), kb::mul(a.y, w), kb::mul(a.z, w), kb::mul(a.w, w));
 }
 
+// Twiddle sources for the vectorised steps.  TwMont: Montgomery words (a
+// shared table); TwShoup: the plain value w and floor(w 2^32 / p) (a global
+// table), so (a - b) w mod p is one high and two low products and one
+// correction (Shoup's method); both give the same field element.
+struct TwMont {
+  const uint32_t *t;
+  __device__ __forceinline__ uint4 submul(uint4 a, uint4 b, int i) const {
+    return submul4(a, b, t[i]);
+  }
+};
+__device__ __forceinline__ uint32_t shoup_mul(uint32_t d, uint2 w) {  // d < 2^32
+  uint32_t q = __umulhi(d, w.y);
+  uint32_t r = d * w.x - q * kb::P;  // in [0, 2p)
+  return kb::umin(r, r - kb::P);
+}
+struct TwShoup {
+  const uint2 *t;
+  __device__ __forceinline__ uint4 submul(uint4 a, uint4 b, int i) const {
+    uint2 w = t[i];
+    return make_uint4(shoup_mul(a.x - b.x + kb::P, w), shoup_mul(a.y - b.y + kb::P, w),
+                      shoup_mul(a.z - b.z + kb::P, w), shoup_mul(a.w - b.w + kb::P, w));
+  }
+};
+
 // R radix-2 DIF stages in registers (see dif_step).  LAST: the final step of
 // the transform, where the block stride q is 1, the first half-size is
 // 2^(R-1) and position 0 of every stage has twiddle 1.
-template <int C, int R, bool LAST>
-__device__ __forceinline__ void dif_step_v(uint4 *tile, const uint32_t *twl, int rows_log, int lh) {
+template <int C, int R, bool LAST, class TW>
+__device__ __forceinline__ void dif_step_v(uint4 *tile, const TW &tw, int rows_log, int lh) {
   constexpr int T = 1 << R, V = C / 4, LV = V == 2 ? 1 : 0;
   const int lq = LAST ? 0 : lh - (R - 1);
   const int q = 1 << lq;
@@ -263,7 +295,7 @@ __device__ __forceinline__ void dif_step_v(uint4 *tile, const uint32_t *twl, int
         uint4 a = v[t], b = v[t + span];
         v[t] = add4(a, b);
         if (LAST && tl == 0) v[t + span] = sub4(a, b);  // w^0 = 1
-        else v[t + span] = submul4(a, b, twl[hh + j + tl * q]);
+        else v[t + span] = tw.submul(a, b, hh + j + tl * q);
       }
     }
 #pragma unroll
@@ -273,8 +305,9 @@ __device__ __forceinline__ void dif_step_v(uint4 *tile, const uint32_t *twl, int
 
 template <int C, int R>
 __device__ __forceinline__ void dif_run_v(uint4 *tile, const uint32_t *twl, int rows_log, int lh) {
-  if (lh == R - 1) dif_step_v<C, R, true>(tile, twl, rows_log, lh);
-  else dif_step_v<C, R, false>(tile, twl, rows_log, lh);
+  TwMont tw{twl};
+  if (lh == R - 1) dif_step_v<C, R, true>(tile, tw, rows_log, lh);
+  else dif_step_v<C, R, false>(tile, tw, rows_log, lh);
   __syncthreads();
 }
 
@@ -356,8 +389,8 @@ __global__ void __launch_bounds__(256) dft_tile_v(const uint32_t *__restrict__ i
 // fly) and the last step writes its rows straight to their bit-reversed
 // output rows (four-step post-twiddle on the fly): two shared-memory passes
 // and two barriers fewer per tile.  Needs S >= 4 (at least two steps).
-template <int C, int R>
-__device__ __forceinline__ void dif_first_v(uint4 *tile, const uint32_t *twl, int rows_log, int S,
+template <int C, int R, class TW>
+__device__ __forceinline__ void dif_first_v(uint4 *tile, const TW &tw, int rows_log, int S,
                                             const uint4 *__restrict__ in4, uint32_t o0,
                                             uint32_t wv, uint32_t v0, uint32_t rows_valid,
                                             uint32_t a_in, uint32_t b_in, int pre_log) {
@@ -392,7 +425,7 @@ __device__ __forceinline__ void dif_first_v(uint4 *tile, const uint32_t *twl, in
         const int tl = t & (span - 1);
         uint4 a = v[t], b = v[t + span];
         v[t] = add4(a, b);
-        v[t + span] = submul4(a, b, twl[hh + j + tl * q]);
+        v[t + span] = tw.submul(a, b, hh + j + tl * q);
       }
     }
 #pragma unroll
@@ -402,8 +435,8 @@ __device__ __forceinline__ void dif_first_v(uint4 *tile, const uint32_t *twl, in
 
 // the final radix-8 step (block stride 1, first half-size 4), written to the
 // output rows
-template <int C>
-__device__ __forceinline__ void dif_last_v(const uint4 *tile, const uint32_t *twl, int rows_log,
+template <int C, class TW>
+__device__ __forceinline__ void dif_last_v(const uint4 *tile, const TW &tw, int rows_log,
                                            int S, uint4 *__restrict__ out4, uint32_t o0,
                                            uint32_t wv, uint32_t v0, uint32_t a_out,
                                            uint32_t b_out, int tw_log) {
@@ -428,7 +461,7 @@ __device__ __forceinline__ void dif_last_v(const uint4 *tile, const uint32_t *tw
         uint4 a = v[t], b = v[t + span];
         v[t] = add4(a, b);
         if (tl == 0) v[t + span] = sub4(a, b);  // w^0 = 1
-        else v[t + span] = submul4(a, b, twl[hh + tl]);
+        else v[t + span] = tw.submul(a, b, hh + tl);
       }
     }
 #pragma unroll
@@ -453,7 +486,7 @@ __global__ void __launch_bounds__(256, 4) dft_tile_v2(const uint32_t *__restrict
   extern __shared__ uint4 smv[];
   const int n = 1 << S, rows = n << lg;
   uint4 *tile = smv;
-  const uint32_t *aux = g_dif;  // DIF twiddles (global, read through the L1)
+  const TwShoup aux{g_dif2};  // DIF twiddles (global, read through the L1)
   const uint32_t o0 = blockIdx.y << lg;
   const uint32_t v0 = blockIdx.x * V;
   const uint32_t wv = width / 4;
