@@ -91,18 +91,12 @@ __host__ __device__ constexpr DiagEntry diag_entry24(int i) {
   return v[i];
 }
 
-// x * num / 2^log_den mod p on a canonical word (Montgomery form is linear,
-// so scaling the word scales the element).  Division by 2^e (e <= 24): with
-// m = -x mod 2^e, x + m p is divisible by 2^e because p = 127 * 2^24 + 1, and
-// (x + m p) / 2^e = (x + m) / 2^e + m * 127 * 2^(24-e) < p.
-template <int NUM, int LOGD>
+// x * num mod p for num in 1..4 on a canonical word (Montgomery form is
+// linear, so scaling the word scales the element)
+template <int NUM>
 __device__ __forceinline__ uint32_t mul_small(uint32_t x) {
   using namespace kb;
-  if constexpr (LOGD > 0) {
-    static_assert(NUM == 1 && LOGD <= 24, "only 2^-e");
-    uint32_t m = (0u - x) & ((1u << LOGD) - 1u);
-    return ((x + m) >> LOGD) + m * (127u << (24 - LOGD));
-  } else if constexpr (NUM == 1) {
+  if constexpr (NUM == 1) {
     return x;
   } else if constexpr (NUM == 2) {
     return dbl(x);
@@ -114,16 +108,65 @@ __device__ __forceinline__ uint32_t mul_small(uint32_t x) {
   }
 }
 
+// Lanes with a diagonal entry +-2^-e.
+//  e < 7: x 2^-e = (x + m p) / 2^e with m = -x mod 2^e (x + m p is divisible
+//         by 2^e because p = 127 * 2^24 + 1), = (x + m) / 2^e + m K with
+//         K = 127 * 2^(24-e); below p for a canonical x.  Then one modular
+//         add or subtract.
+//  e >= 7: write x = q 2^e + lo (lo < 2^e); since 2^-e = -K (mod p),
+//         x 2^-e = q - lo K with q < 2^(31-e) <= 2^24 and lo K < p, for any
+//         lane word x < 2^31.
+//    +2^-e: (sum + p) + q - lo K lies in [1, 2^32 - 2^24]; one conditional
+//         subtraction leaves it in [0, 2^31), congruent but not always
+//         canonical ("loose"; the lane sum and this same update accept such a
+//         word, and the permutation reduces it after the internal rounds).
+//    -2^-e: reduce(sum + lo K) - q lies in (-2^24, p); one conditional
+//         addition makes it canonical.
+// (On GB300 the e >= 7 forms are 2% faster over a leaf-hash launch; the same
+// forms for e < 7 were slower than the ones above.)
+// Entries 1, 2, 3, 4 (up to sign) are sums of canonical words.
 template <int W, int I>
-__device__ __forceinline__ void p2_internal_lane(uint32_t (&s)[W], uint32_t sum) {
+__device__ __forceinline__ constexpr bool p2_loose_lane() {
   constexpr DiagEntry d = W == 16 ? diag_entry16(I) : diag_entry24(I);
-  uint32_t y = mul_small<d.num, d.log_den>(s[I]);
-  s[I] = d.sign > 0 ? kb::add(sum, y) : kb::sub(sum, y);
+  return d.log_den >= 7 && d.sign > 0;
+}
+template <int W, int I>
+__device__ __forceinline__ void p2_internal_lane(uint32_t (&s)[W], uint32_t sum, uint32_t sum_p) {
+  using namespace kb;
+  constexpr DiagEntry d = W == 16 ? diag_entry16(I) : diag_entry24(I);
+  constexpr int E = d.log_den;
+  const uint32_t x = s[I];
+  if constexpr (E >= 7) {
+    constexpr uint32_t MASK = (1u << E) - 1u, K = 127u << (24 - E);
+    if constexpr (d.sign > 0) {
+      uint32_t r = sum_p + (x >> E) - (x & MASK) * K;
+      s[I] = kb::umin(r, r - P);
+    } else {
+      uint32_t t = sum + (x & MASK) * K;
+      t = kb::umin(t, t - P);
+      uint32_t r = t - (x >> E);
+      s[I] = kb::umin(r, r + P);
+    }
+  } else if constexpr (E > 0) {
+    constexpr uint32_t MASK = (1u << E) - 1u, K = 127u << (24 - E);
+    uint32_t m = (0u - x) & MASK;
+    uint32_t y = ((x + m) >> E) + m * K;
+    s[I] = d.sign > 0 ? add(sum, y) : sub(sum, y);
+  } else {
+    uint32_t y = mul_small<d.num>(x);
+    s[I] = d.sign > 0 ? add(sum, y) : sub(sum, y);
+  }
 }
 template <int W, int... I>
 __device__ __forceinline__ void p2_internal_all(uint32_t (&s)[W], uint32_t sum,
                                                 std::integer_sequence<int, I...>) {
-  (p2_internal_lane<W, I>(s, sum), ...);
+  const uint32_t sum_p = sum + kb::P;
+  (p2_internal_lane<W, I>(s, sum, sum_p), ...);
+}
+// canonical form of the loose lanes, after the last internal round
+template <int W, int... I>
+__device__ __forceinline__ void p2_reduce_loose(uint32_t (&s)[W], std::integer_sequence<int, I...>) {
+  ((p2_loose_lane<W, I>() ? (void)(s[I] = kb::umin(s[I], s[I] - kb::P)) : (void)0), ...);
 }
 
 // Signed Montgomery product of int32 words with |a * b| < p * 2^31: with t
@@ -150,9 +193,9 @@ template <int W>
 __device__ __forceinline__ void p2_internal_round(uint32_t (&s)[W], uint32_t rc) {
   using namespace kb;
   s[0] = sbox((int32_t)(s[0] + rc));
-  // sum of the W canonical lanes in 64 bits (< W p < 2^36): pairs of lanes
-  // add without overflow in 32 bits (2p < 2^32), then one reduction:
-  // 2^31 = 2^24 - 1 (mod p) folds the high part, leaving < 2p
+  // sum of the W lanes in 64 bits: every lane is below 2^31 (canonical or
+  // loose), so pairs add without overflow in 32 bits; then one reduction: 2^31 = 2^24 - 1 (mod p) folds the high
+  // part, leaving < 2p
   uint64_t wide = 0;
 #pragma unroll
   for (int i = 0; i < W; i += 2) wide += (uint32_t)(s[i] + s[i + 1]);
@@ -176,6 +219,7 @@ __device__ __forceinline__ void p2_permute(uint32_t (&s)[W]) {
     if (r == 4) {
 #pragma unroll 1
       for (int q = 0; q < RP; q++) p2_internal_round<W>(s, I[q]);
+      p2_reduce_loose<W>(s, std::make_integer_sequence<int, W>{});
     }
     p2_external_round<W>(s, C + r * W);
   }
