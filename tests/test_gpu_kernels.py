@@ -22,7 +22,10 @@ def rand(oracle, seed, n):
     (0, 16, 1), (1, 16, 1), (3, 2, 4), (5, 4, 8), (8, 16, 64), (11, 16, 1024), (11, 64, 512),
     (12, 16, 1024), (13, 8, 8192), (16, 64, 8192), (17, 16, 65536), (20, 16, 262144),
     (21, 64, 65536), (22, 16, 1 << 20), (4, 8, 16), (6, 4, 40), (9, 16, 300), (14, 8, 100),
-    (15, 32, 1000)])
+    (15, 32, 1000),
+    # two passes over a zero-padded input (pass 1 skips the zero stages):
+    # ragged h_in, 4-column tiles, and a padding too deep for the short form
+    (18, 8, 70000), (19, 4, 40000), (14, 16, 4097), (20, 8, 4000), (17, 8, 10000)])
 def test_dft_batch(ctx, oracle, log_h, width, h_in):
     x = rand(oracle, 7 + log_h, h_in * width)
     want = oracle.dft_batch(x, h_in, width, log_h)

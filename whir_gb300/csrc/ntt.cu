@@ -79,6 +79,19 @@ __device__ __forceinline__ uint32_t brev(uint32_t i, int bits) {
 
 constexpr int MAX_TILE_LOG = 12;
 
+// Index maps of the vectorised tile beyond the linear ones: sub-transform o
+// reads input row (o & in_mask) * a_in + i * b_in, its pre-twiddle exponent
+// is (o >> pre_shift) * i, and its post-twiddle exponent is
+// (o & post_mask) * ((o >> post_shift) + (k << post_kshift)).  The identity
+// map (all-ones masks, shifts 0, 31, 0) gives o * i and o * k.
+struct TileIdx {
+  uint32_t in_mask = 0xffffffffu;
+  int pre_shift = 0;
+  uint32_t post_mask = 0xffffffffu;
+  int post_shift = 31;
+  int post_kshift = 0;
+};
+
 // Shared-memory tile index of (row, column): rows are permuted inside each
 // aligned group of 4 by XOR with bits 3..4 of the row, so that the 4 rows a
 // warp touches at once (consecutive rows, or rows 8 apart in the last radix
@@ -393,7 +406,8 @@ template <int C, int R, class TW>
 __device__ __forceinline__ void dif_first_v(uint4 *tile, const TW &tw, int rows_log, int S,
                                             const uint4 *__restrict__ in4, uint32_t o0,
                                             uint32_t wv, uint32_t v0, uint32_t rows_valid,
-                                            uint32_t a_in, uint32_t b_in, int pre_log) {
+                                            uint32_t a_in, uint32_t b_in, int pre_log,
+                                            const TileIdx &ix) {
   constexpr int T = 1 << R, V = C / 4, LV = V == 2 ? 1 : 0;
   const int lh = S - 1, lq = lh - (R - 1);
   const int q = 1 << lq, H = 1 << lh, n = 1 << S;
@@ -408,11 +422,18 @@ __device__ __forceinline__ void dif_first_v(uint4 *tile, const TW &tw, int rows_
     for (int t = 0; t < T; t++) {
       const int r = base + t * q;
       const uint32_t o = o0 + (uint32_t)(r >> S), i = (uint32_t)(r & (n - 1));
-      const uint32_t row = o * a_in + i * b_in;
+      const uint32_t row = (o & ix.in_mask) * a_in + i * b_in;
       v[t] = make_uint4(0, 0, 0, 0);
       if (row < rows_valid) {
-        v[t] = __ldg(in4 + row * wv + v0 + c);
-        if (pre_log) v[t] = mul4(v[t], root_pow(((o * i) & pmask) << (24 - pre_log)));
+        // rows read once bypass the L1 (it keeps the twiddles); coset
+        // transforms (pre_log > 0) read every input row once per coset, so
+        // theirs stay cached
+        if (pre_log) {
+          v[t] = __ldg(in4 + row * wv + v0 + c);
+          v[t] = mul4(v[t], root_pow((((o >> ix.pre_shift) * i) & pmask) << (24 - pre_log)));
+        } else {
+          v[t] = __ldcg(in4 + row * wv + v0 + c);
+        }
       }
     }
 #pragma unroll
@@ -439,7 +460,7 @@ template <int C, class TW>
 __device__ __forceinline__ void dif_last_v(const uint4 *tile, const TW &tw, int rows_log,
                                            int S, uint4 *__restrict__ out4, uint32_t o0,
                                            uint32_t wv, uint32_t v0, uint32_t a_out,
-                                           uint32_t b_out, int tw_log) {
+                                           uint32_t b_out, int tw_log, const TileIdx &ix) {
   constexpr int R = 3, T = 8, V = C / 4, LV = V == 2 ? 1 : 0;
   const int n = 1 << S;
   const uint32_t tmask = (1u << tw_log) - 1u;
@@ -470,7 +491,10 @@ __device__ __forceinline__ void dif_last_v(const uint4 *tile, const TW &tw, int 
       const uint32_t o = o0 + (uint32_t)(r >> S);
       const uint32_t k = brev((uint32_t)(r & (n - 1)), S);
       uint4 x = v[t];
-      if (tw_log) x = mul4(x, root_pow(((o * k) & tmask) << (24 - tw_log)));
+      if (tw_log) {
+        const uint32_t e = (o & ix.post_mask) * ((o >> ix.post_shift) + (k << ix.post_kshift));
+        x = mul4(x, root_pow((e & tmask) << (24 - tw_log)));
+      }
       out4[(o * a_out + k * b_out) * wv + v0 + c] = x;
     }
   }
@@ -481,7 +505,8 @@ __global__ void __launch_bounds__(256, 4) dft_tile_v2(const uint32_t *__restrict
                                                    uint32_t *__restrict__ out, int S, int lg,
                                                    uint32_t width, uint32_t rows_valid,
                                                    uint32_t a_in, uint32_t b_in, uint32_t a_out,
-                                                   uint32_t b_out, int pre_log, int tw_log) {
+                                                   uint32_t b_out, int pre_log, int tw_log,
+                                                   const TileIdx ix) {
   constexpr int V = C / 4;
   extern __shared__ uint4 smv[];
   const int n = 1 << S, rows = n << lg;
@@ -496,24 +521,27 @@ __global__ void __launch_bounds__(256, 4) dft_tile_v2(const uint32_t *__restrict
   const int rows_log = S + lg;
   const int r0 = S % 3 == 0 ? 3 : S % 3;
   if (r0 == 1)
-    dif_first_v<C, 1>(tile, aux, rows_log, S, in4, o0, wv, v0, rows_valid, a_in, b_in, pre_log);
+    dif_first_v<C, 1>(tile, aux, rows_log, S, in4, o0, wv, v0, rows_valid, a_in, b_in, pre_log,
+                         ix);
   else if (r0 == 2)
-    dif_first_v<C, 2>(tile, aux, rows_log, S, in4, o0, wv, v0, rows_valid, a_in, b_in, pre_log);
+    dif_first_v<C, 2>(tile, aux, rows_log, S, in4, o0, wv, v0, rows_valid, a_in, b_in, pre_log,
+                         ix);
   else
-    dif_first_v<C, 3>(tile, aux, rows_log, S, in4, o0, wv, v0, rows_valid, a_in, b_in, pre_log);
+    dif_first_v<C, 3>(tile, aux, rows_log, S, in4, o0, wv, v0, rows_valid, a_in, b_in, pre_log,
+                         ix);
   __syncthreads();
   for (int lh = S - 1 - r0; lh >= 5; lh -= 3) {
     dif_step_v<C, 3, false>(tile, aux, rows_log, lh);
     __syncthreads();
   }
-  dif_last_v<C>(tile, aux, rows_log, S, out4, o0, wv, v0, a_out, b_out, tw_log);
+  dif_last_v<C>(tile, aux, rows_log, S, out4, o0, wv, v0, a_out, b_out, tw_log, ix);
 }
 
 template <int C>
 static cudaError_t launch_tile_v(const uint32_t *in, uint32_t *out, int S, size_t width,
                                  size_t rows_valid, size_t n_outer, size_t a_in, size_t b_in,
                                  size_t a_out, size_t b_out, int pre_log, int tw_log,
-                                 cudaStream_t st) {
+                                 cudaStream_t st, const TileIdx &ix = TileIdx()) {
   // pack small sub-transforms so that a CTA holds at least 2^10 rows
   int lg = 0;
   while (S + lg < 10 && ((size_t)2 << lg) <= n_outer) lg++;
@@ -526,7 +554,7 @@ static cudaError_t launch_tile_v(const uint32_t *in, uint32_t *out, int S, size_
     dft_tile_v2<C><<<grid, threads, rows * C * 4, st>>>(in, out, S, lg, (uint32_t)width,
                                                 (uint32_t)rows_valid, (uint32_t)a_in,
                                                 (uint32_t)b_in, (uint32_t)a_out, (uint32_t)b_out,
-                                                pre_log, tw_log);
+                                                pre_log, tw_log, ix);
   else
     dft_tile_v<C><<<grid, threads, smem, st>>>(in, out, S, lg, (uint32_t)width,
                                                (uint32_t)rows_valid, (uint32_t)a_in, (uint32_t)b_in,
@@ -620,7 +648,34 @@ cudaError_t dft_batch(const uint32_t *in, size_t h_in, size_t width, int log_h, 
   int L1 = (log_h + 1) / 2 + tune.l1_bias, L2 = log_h - L1;
   if (L1 > MAX_TILE_LOG || L2 > MAX_TILE_LOG) return cudaErrorInvalidValue;
   size_t M1 = (size_t)1 << L1, M2 = (size_t)1 << L2;
-  cudaError_t e = tile_any(in, scratch, L1, width, h_in, M2, 1, M2, 1, M2, 0, log_h, st);
+  cudaError_t e;
+  // Pass 1 of a zero-padded input: column n2 has nonzero entries only at
+  // n1 < N' = 2^S' with S' = L0 - L2, so with k = k1 + rho k2 (rho = M1 / N')
+  // its size-M1 DFT is rho DFTs of size N' of x[M2 n1 + n2] w_{M1}^(n1 k1),
+  // the zero butterfly stages skipped.  Sub-transform o = n2 + M2 k1 reads
+  // rows (o & (M2-1)) + M2 n1, writes row o + M2 rho k2 = n2 + M2 k, and
+  // applies the four-step twiddle w_M^(n2 k).  Used from rho = 8 up: at
+  // rho = 4 the pre-twiddle costs about what the two skipped stages save
+  // (measured on GB300).
+  const int lr = log_h - L0, S1 = L1 - lr;
+  const bool aligned = (((uintptr_t)in | (uintptr_t)scratch) & 15) == 0;
+  if (lr >= 3 && S1 >= 4 && aligned && width % 4 == 0) {
+    TileIdx ix;
+    ix.in_mask = (uint32_t)(M2 - 1);
+    ix.pre_shift = L2;
+    ix.post_mask = (uint32_t)(M2 - 1);
+    ix.post_shift = L2;
+    ix.post_kshift = lr;
+    const size_t n_outer = M2 << lr;
+    if (width % 8 == 0)
+      e = launch_tile_v<8>(in, scratch, S1, width, h_in, n_outer, 1, M2, 1, n_outer, L1, log_h,
+                           st, ix);
+    else
+      e = launch_tile_v<4>(in, scratch, S1, width, h_in, n_outer, 1, M2, 1, n_outer, L1, log_h,
+                           st, ix);
+  } else {
+    e = tile_any(in, scratch, L1, width, h_in, M2, 1, M2, 1, M2, 0, log_h, st);
+  }
   if (e != cudaSuccess) return e;
   return tile_any(scratch, out, L2, width, h, M1, M2, 1, 1, M1, 0, 0, st);
 }
