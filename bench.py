@@ -49,10 +49,11 @@ UNIT = "proofs/s"
 NCU_TRAFFIC_BYTES = {"leaf_hash": 294.6e6}
 NCU_TRAFFIC_K = 24
 # Thread instructions per width-24 permutation of the leaf hash
-# (smsp__inst_executed.sum * 32 / permutations, same ncu capture file).  With
-# one warp instruction issued per cycle on each of the 4 sub-partitions of
-# each SM, the issue-bound rate is SMs * 4 * 32 * clock / this.
-LEAF_INSTR_PER_PERM24 = 8735
+# (smsp__inst_executed.sum * 32 / permutations of hash_rows_fixed<16> on a
+# k = 22 proof, profiles/hash_rows_fixed_leaf_hash.md).  With one warp
+# instruction issued per cycle on each of the 4 sub-partitions of each SM,
+# the issue-bound rate is SMs * 4 * 32 * clock / this.
+LEAF_INSTR_PER_PERM24 = 8576
 GB300_SMS = 152
 
 
