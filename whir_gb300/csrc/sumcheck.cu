@@ -160,13 +160,34 @@ cudaError_t eq_full(const Point &z, E4 scale, E4 *out, E4 *tmp, cudaStream_t st)
 // walks whole h_hi blocks (2^s_lo contiguous rows); thread t always sees
 // column j = t mod W, so it keeps one inner sum (over h_lo, weighted by
 // eq_lo) and folds it into its outer sum with eq_hi[h_hi] once per block.
+// Four CTAs per SM, each walking several blocks, so that the fixed cost of a
+// CTA (the eq_lo copy, the reduction of its sums) is paid a few hundred
+// times per launch, not once per block.
 constexpr int CH_T = 256;
-__global__ void __launch_bounds__(CH_T) compress_hi_kernel(const uint32_t *__restrict__ poly,
-                                                           int k, int ks,
-                                                           const E4 *__restrict__ eq_lo, int s_lo,
-                                                           const E4 *__restrict__ eq_hi,
-                                                           unsigned long long *acc,
-                                                           Publish pub) {
+__device__ __forceinline__ void ch_accumulate4(E4 &inner, const E4 *lo, int ks, size_t e,
+                                               const uint32_t (&x)[4]) {
+  // four products of canonical words per 64-bit sum (4 p^2 < 2p 2^32), one
+  // Montgomery reduction per four: the sum of Montgomery words' products
+  // reduces to the Montgomery word of the sum of products
+  unsigned long long s4[4] = {0, 0, 0, 0};
+#pragma unroll
+  for (int q = 0; q < 4; q++) {
+    const E4 l = lo[(e + q * CH_T) >> ks];
+#pragma unroll
+    for (int c = 0; c < 4; c++) s4[c] += (unsigned long long)l.c[c] * x[q];
+  }
+  E4 part4;
+#pragma unroll
+  for (int c = 0; c < 4; c++) part4.c[c] = kb::reduce_wide(s4[c]);
+  inner = kb::e_add(inner, part4);
+}
+__global__ void __launch_bounds__(CH_T, 4) compress_hi_kernel(const uint32_t *__restrict__ poly,
+                                                              int k, int ks,
+                                                              const E4 *__restrict__ eq_lo,
+                                                              int s_lo,
+                                                              const E4 *__restrict__ eq_hi,
+                                                              unsigned long long *acc,
+                                                              Publish pub) {
   extern __shared__ unsigned char smraw[];
   E4 *lo = reinterpret_cast<E4 *>(smraw);
   unsigned long long *part = reinterpret_cast<unsigned long long *>(lo + ((size_t)1 << s_lo));
@@ -182,30 +203,35 @@ __global__ void __launch_bounds__(CH_T) compress_hi_kernel(const uint32_t *__res
     const uint32_t *base = poly + hh * block_words;
     E4 inner = kb::e_zero();
     size_t e = tid;
-    // four products of canonical words per 64-bit sum (4 p^2 < 2p 2^32), one
-    // Montgomery reduction per four: the sum of Montgomery words' products
-    // reduces to the Montgomery word of the sum of products
+    // sixteen streaming loads in flight per thread
+    for (; e + 15 * CH_T < block_words; e += 16 * CH_T) {
+      uint32_t x[4][4];
+#pragma unroll
+      for (int g = 0; g < 4; g++)
+#pragma unroll
+        for (int q = 0; q < 4; q++) x[g][q] = __ldcs(base + e + (4 * g + q) * CH_T);
+#pragma unroll
+      for (int g = 0; g < 4; g++) ch_accumulate4(inner, lo, ks, e + 4 * g * CH_T, x[g]);
+    }
     for (; e + 3 * CH_T < block_words; e += 4 * CH_T) {
       uint32_t x[4];
 #pragma unroll
-      for (int q = 0; q < 4; q++) x[q] = __ldg(base + e + q * CH_T);
-      unsigned long long s4[4] = {0, 0, 0, 0};
-#pragma unroll
-      for (int q = 0; q < 4; q++) {
-        const E4 l = lo[(e + q * CH_T) >> ks];
-#pragma unroll
-        for (int c = 0; c < 4; c++) s4[c] += (unsigned long long)l.c[c] * x[q];
-      }
-      E4 part4;
-#pragma unroll
-      for (int c = 0; c < 4; c++) part4.c[c] = kb::reduce_wide(s4[c]);
-      inner = kb::e_add(inner, part4);
+      for (int q = 0; q < 4; q++) x[q] = __ldcs(base + e + q * CH_T);
+      ch_accumulate4(inner, lo, ks, e, x);
     }
     for (; e < block_words; e += CH_T)
       inner = kb::e_add(inner, kb::e_scale(lo[e >> ks], __ldg(base + e)));
     outer = kb::e_add(outer, kb::e_mul(inner, eq_hi[hh]));
   }
-  {
+  // lanes of a warp that share a column add their sums by shuffles first
+  // (modular adds of canonical words), so the shared atomics below see one
+  // value per column and warp
+  const int lane = tid & 31;
+  for (int off = W; off < 32; off <<= 1)
+#pragma unroll
+    for (int c = 0; c < 4; c++)
+      outer.c[c] = kb::add(outer.c[c], __shfl_xor_sync(0xffffffffu, outer.c[c], off));
+  if (W >= 32 || lane < W) {
     const int j = tid & (W - 1);
 #pragma unroll
     for (int c = 0; c < 4; c++) atomicAdd(part + j * 4 + c, (unsigned long long)outer.c[c]);
@@ -220,7 +246,7 @@ cudaError_t compress_hi(const uint32_t *poly, int k, int ks, const E4 *eq_lo, in
                         const Publish &pub) {
   if ((1 << ks) > CH_T || k < ks + s_lo) return cudaErrorInvalidValue;
   size_t n_hi = (size_t)1 << (k - ks - s_lo);
-  unsigned grid = (unsigned)(n_hi < 152 * 8 ? n_hi : 152 * 8);
+  unsigned grid = (unsigned)(n_hi < 152 * 4 ? n_hi : 152 * 4);
   size_t smem = ((size_t)1 << s_lo) * sizeof(E4) + ((size_t)4 << ks) * 8;
   compress_hi_kernel<<<grid, CH_T, smem, st>>>(poly, k, ks, eq_lo, s_lo, eq_hi, acc, pub);
   count_launches(1);
