@@ -58,15 +58,8 @@ cudaError_t init_device_tables();
 // out[i][c] = sum_{r < h_in} in[r][c] * w^(r i), w = two_adic_generator(log_h),
 // rows of `width` words, natural order; rows >= h_in are zero.  `scratch`
 // holds 2^log_h * width words when log_h > 11 (two passes), else unused.
-//
-// tee (optional): `in` is host memory mapped into the device address space
-// (pinned); the launch that reads the input reads each row once and also
-// stores it at the same offset of `tee` (device memory), so the input crosses
-// the host link once and no separate copy is needed.  Only for shapes where
-// dft_tee_supported() holds.
 cudaError_t dft_batch(const uint32_t *in, size_t h_in, size_t width, int log_h, uint32_t *out,
-                      uint32_t *scratch, cudaStream_t st, uint32_t *tee = nullptr);
-bool dft_tee_supported(const void *in, const void *tee, size_t h_in, size_t width, int log_h);
+                      uint32_t *scratch, cudaStream_t st);
 
 // ---- Merkle (crates/merkle/src/poseidon_packed.rs) ----
 // leaf digests: PaddingFreeSponge<P24, 24, 16, 8> over each row of row_len words

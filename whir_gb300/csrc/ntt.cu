@@ -90,7 +90,6 @@ struct TileIdx {
   uint32_t post_mask = 0xffffffffu;
   int post_shift = 31;
   int post_kshift = 0;
-  uint4 *tee = nullptr;  // also store every input row read (see dft_batch)
 };
 
 // Shared-memory tile index of (row, column): rows are permuted inside each
@@ -403,7 +402,7 @@ __global__ void __launch_bounds__(256) dft_tile_v(const uint32_t *__restrict__ i
 // fly) and the last step writes its rows straight to their bit-reversed
 // output rows (four-step post-twiddle on the fly): two shared-memory passes
 // and two barriers fewer per tile.  Needs S >= 4 (at least two steps).
-template <int C, int R, bool TEE, class TW>
+template <int C, int R, class TW>
 __device__ __forceinline__ void dif_first_v(uint4 *tile, const TW &tw, int rows_log, int S,
                                             const uint4 *__restrict__ in4, uint32_t o0,
                                             uint32_t wv, uint32_t v0, uint32_t rows_valid,
@@ -432,25 +431,9 @@ __device__ __forceinline__ void dif_first_v(uint4 *tile, const TW &tw, int rows_
         if (pre_log) {
           v[t] = __ldg(in4 + row * wv + v0 + c);
           v[t] = mul4(v[t], root_pow((((o >> ix.pre_shift) * i) & pmask) << (24 - pre_log)));
-        } else if (TEE) {
-          // host memory over the link: ask the L2 for the whole 256-byte
-          // span, which the neighbouring column slices and rows read next
-          const uint4 *src = in4 + row * wv + v0 + c;
-          asm volatile("ld.global.cg.L2::256B.v4.u32 {%0, %1, %2, %3}, [%4];"
-                       : "=r"(v[t].x), "=r"(v[t].y), "=r"(v[t].z), "=r"(v[t].w)
-                       : "l"(src));
         } else {
           v[t] = __ldcg(in4 + row * wv + v0 + c);
         }
-      }
-    }
-    if (TEE) {  // after every load of the task is in flight
-#pragma unroll
-      for (int t = 0; t < T; t++) {
-        const int r = base + t * q;
-        const uint32_t o = o0 + (uint32_t)(r >> S), i = (uint32_t)(r & (n - 1));
-        const uint32_t row = (o & ix.in_mask) * a_in + i * b_in;
-        if (row < rows_valid) ix.tee[row * wv + v0 + c] = v[t];
       }
     }
 #pragma unroll
@@ -517,7 +500,7 @@ __device__ __forceinline__ void dif_last_v(const uint4 *tile, const TW &tw, int 
   }
 }
 
-template <int C, bool TEE>
+template <int C>
 __global__ void __launch_bounds__(256, 4) dft_tile_v2(const uint32_t *__restrict__ in,
                                                    uint32_t *__restrict__ out, int S, int lg,
                                                    uint32_t width, uint32_t rows_valid,
@@ -538,16 +521,13 @@ __global__ void __launch_bounds__(256, 4) dft_tile_v2(const uint32_t *__restrict
   const int rows_log = S + lg;
   const int r0 = S % 3 == 0 ? 3 : S % 3;
   if (r0 == 1)
-    dif_first_v<C, 1, TEE>(tile, aux, rows_log, S, in4, o0, wv, v0, rows_valid, a_in, b_in,
-                               pre_log,
+    dif_first_v<C, 1>(tile, aux, rows_log, S, in4, o0, wv, v0, rows_valid, a_in, b_in, pre_log,
                          ix);
   else if (r0 == 2)
-    dif_first_v<C, 2, TEE>(tile, aux, rows_log, S, in4, o0, wv, v0, rows_valid, a_in, b_in,
-                               pre_log,
+    dif_first_v<C, 2>(tile, aux, rows_log, S, in4, o0, wv, v0, rows_valid, a_in, b_in, pre_log,
                          ix);
   else
-    dif_first_v<C, 3, TEE>(tile, aux, rows_log, S, in4, o0, wv, v0, rows_valid, a_in, b_in,
-                               pre_log,
+    dif_first_v<C, 3>(tile, aux, rows_log, S, in4, o0, wv, v0, rows_valid, a_in, b_in, pre_log,
                          ix);
   __syncthreads();
   for (int lh = S - 1 - r0; lh >= 5; lh -= 3) {
@@ -570,14 +550,11 @@ static cudaError_t launch_tile_v(const uint32_t *in, uint32_t *out, int S, size_
   int threads = (int)(rows * (C / 4) / 8);
   threads = threads < 32 ? 32 : (threads > 256 ? 256 : threads);
   dim3 grid((unsigned)(width / C), (unsigned)(n_outer >> lg));
-  if (S >= 4 && ix.tee)
-    dft_tile_v2<C, true><<<grid, threads, rows * C * 4, st>>>(
-        in, out, S, lg, (uint32_t)width, (uint32_t)rows_valid, (uint32_t)a_in, (uint32_t)b_in,
-        (uint32_t)a_out, (uint32_t)b_out, pre_log, tw_log, ix);
-  else if (S >= 4)
-    dft_tile_v2<C, false><<<grid, threads, rows * C * 4, st>>>(
-        in, out, S, lg, (uint32_t)width, (uint32_t)rows_valid, (uint32_t)a_in, (uint32_t)b_in,
-        (uint32_t)a_out, (uint32_t)b_out, pre_log, tw_log, ix);
+  if (S >= 4)
+    dft_tile_v2<C><<<grid, threads, rows * C * 4, st>>>(in, out, S, lg, (uint32_t)width,
+                                                (uint32_t)rows_valid, (uint32_t)a_in,
+                                                (uint32_t)b_in, (uint32_t)a_out, (uint32_t)b_out,
+                                                pre_log, tw_log, ix);
   else
     dft_tile_v<C><<<grid, threads, smem, st>>>(in, out, S, lg, (uint32_t)width,
                                                (uint32_t)rows_valid, (uint32_t)a_in, (uint32_t)b_in,
@@ -648,87 +625,41 @@ void set_dft_tune(int log_h, size_t width, DftTune t) {
   g_dft_tune[log_h][width_class(width)].store(t.l1_bias + 8, std::memory_order_relaxed);
 }
 
-// The shape decisions of dft_batch.
-enum class DftPath { ONE_PASS, COSET, TWO_PASS_SHORT, TWO_PASS };
-struct DftPlan {
-  DftPath path;
-  int L0, L1, L2, lr, S1;
-};
-static DftPlan dft_plan(size_t h_in, size_t width, int log_h, bool aligned) {
-  DftPlan pl{};
-  while (((size_t)1 << pl.L0) < h_in) pl.L0++;
-  if (log_h <= 11) {
-    pl.path = DftPath::ONE_PASS;
-    return pl;
-  }
-  if (pl.L0 <= 11 && log_h - pl.L0 <= 15) {
-    pl.path = DftPath::COSET;
-    return pl;
-  }
-  DftTune tune = dft_tune(log_h, width);
-  if (!dft_tune_valid(log_h, tune)) tune = DftTune();
-  pl.L1 = (log_h + 1) / 2 + tune.l1_bias;
-  pl.L2 = log_h - pl.L1;
-  pl.lr = log_h - pl.L0;
-  pl.S1 = pl.L1 - pl.lr;
-  pl.path = pl.lr >= 3 && pl.S1 >= 4 && aligned && width % 4 == 0 ? DftPath::TWO_PASS_SHORT
-                                                                   : DftPath::TWO_PASS;
-  return pl;
-}
-
-bool dft_tee_supported(const void *in, const void *tee, size_t h_in, size_t width, int log_h) {
-  if (log_h < 0 || log_h > 24 || width == 0 || width % 4 || !in || !tee) return false;
-  if ((((uintptr_t)in | (uintptr_t)tee) & 15) != 0) return false;
-  if (width >= (1u << 16) || (((size_t)width) << log_h) >= ((size_t)1 << 32)) return false;
-  DftPlan pl = dft_plan(h_in, width, log_h, true);
-  // the vectorised tile with its first step on global memory (size >= 2^4),
-  // reading every input row exactly once
-  if (pl.path == DftPath::ONE_PASS) return log_h >= 4;
-  return pl.path == DftPath::TWO_PASS && pl.L1 >= 4;
-}
-
 cudaError_t dft_batch(const uint32_t *in, size_t h_in, size_t width, int log_h, uint32_t *out,
-                      uint32_t *scratch, cudaStream_t st, uint32_t *tee) {
+                      uint32_t *scratch, cudaStream_t st) {
   if (log_h < 0 || log_h > 24 || width == 0) return cudaErrorInvalidValue;
   size_t h = (size_t)1 << log_h;
   if (h_in > h) return cudaErrorInvalidValue;
   // the kernel indexes words with 32-bit arithmetic
   if (width >= (1u << 16) || (h * width) >= ((size_t)1 << 32)) return cudaErrorInvalidValue;
-  const DftPlan pl = dft_plan(h_in, width, log_h, (((uintptr_t)in | (uintptr_t)scratch) & 15) == 0);
-  TileIdx tix;
-  if (tee) {
-    const void *dst = pl.path == DftPath::ONE_PASS ? (const void *)out : (const void *)scratch;
-    if (!dft_tee_supported(in, tee, h_in, width, log_h) || ((uintptr_t)dst & 15))
-      return cudaErrorNotSupported;
-    tix.tee = reinterpret_cast<uint4 *>(tee);
-  }
-  if (pl.path == DftPath::ONE_PASS) {
-    if (tee)
-      return width % 8 == 0
-                 ? launch_tile_v<8>(in, out, log_h, width, h_in, 1, 0, 1, 0, 1, 0, 0, st, tix)
-                 : launch_tile_v<4>(in, out, log_h, width, h_in, 1, 0, 1, 0, 1, 0, 0, st, tix);
+  if (log_h <= 11)
     return tile_any(in, out, log_h, width, h_in, 1, 0, 1, 0, 1, 0, 0, st);
-  }
-  if (pl.path == DftPath::COSET) {
+  int L0 = 0;
+  while (((size_t)1 << L0) < h_in) L0++;
+  if (L0 <= 11 && log_h - L0 <= 15) {
     // coset form: with N0 = 2^L0 >= h_in and M1 = 2^(log_h - L0),
     // out[k1 + M1 k2] = sum_{n < N0} (x[n] w^(n k1)) w_{N0}^(n k2): M1 transforms
     // of size N0 of the pre-twiddled input, one pass, no scratch
-    size_t M1 = h >> pl.L0;
-    return tile_any(in, out, pl.L0, width, h_in, M1, 0, 1, 1, M1, log_h, 0, st);
+    size_t M1 = h >> L0;
+    return tile_any(in, out, L0, width, h_in, M1, 0, 1, 1, M1, log_h, 0, st);
   }
-  const int L1 = pl.L1, L2 = pl.L2, lr = pl.lr, S1 = pl.S1;
+  DftTune tune = dft_tune(log_h, width);
+  if (!dft_tune_valid(log_h, tune)) tune = DftTune();
+  int L1 = (log_h + 1) / 2 + tune.l1_bias, L2 = log_h - L1;
   if (L1 > MAX_TILE_LOG || L2 > MAX_TILE_LOG) return cudaErrorInvalidValue;
   size_t M1 = (size_t)1 << L1, M2 = (size_t)1 << L2;
   cudaError_t e;
-  if (pl.path == DftPath::TWO_PASS_SHORT) {
-    // Pass 1 of a zero-padded input: column n2 has nonzero entries only at
-    // n1 < N' = 2^S' with S' = L0 - L2, so with k = k1 + rho k2 (rho = M1 / N')
-    // its size-M1 DFT is rho DFTs of size N' of x[M2 n1 + n2] w_{M1}^(n1 k1),
-    // the zero butterfly stages skipped.  Sub-transform o = n2 + M2 k1 reads
-    // rows (o & (M2-1)) + M2 n1, writes row o + M2 rho k2 = n2 + M2 k, and
-    // applies the four-step twiddle w_M^(n2 k).  Used from rho = 8 up: at
-    // rho = 4 the pre-twiddle costs about what the two skipped stages save
-    // (measured on GB300).
+  // Pass 1 of a zero-padded input: column n2 has nonzero entries only at
+  // n1 < N' = 2^S' with S' = L0 - L2, so with k = k1 + rho k2 (rho = M1 / N')
+  // its size-M1 DFT is rho DFTs of size N' of x[M2 n1 + n2] w_{M1}^(n1 k1),
+  // the zero butterfly stages skipped.  Sub-transform o = n2 + M2 k1 reads
+  // rows (o & (M2-1)) + M2 n1, writes row o + M2 rho k2 = n2 + M2 k, and
+  // applies the four-step twiddle w_M^(n2 k).  Used from rho = 8 up: at
+  // rho = 4 the pre-twiddle costs about what the two skipped stages save
+  // (measured on GB300).
+  const int lr = log_h - L0, S1 = L1 - lr;
+  const bool aligned = (((uintptr_t)in | (uintptr_t)scratch) & 15) == 0;
+  if (lr >= 3 && S1 >= 4 && aligned && width % 4 == 0) {
     TileIdx ix;
     ix.in_mask = (uint32_t)(M2 - 1);
     ix.pre_shift = L2;
@@ -742,10 +673,6 @@ cudaError_t dft_batch(const uint32_t *in, size_t h_in, size_t width, int log_h, 
     else
       e = launch_tile_v<4>(in, scratch, S1, width, h_in, n_outer, 1, M2, 1, n_outer, L1, log_h,
                            st, ix);
-  } else if (tee) {
-    e = width % 8 == 0
-            ? launch_tile_v<8>(in, scratch, L1, width, h_in, M2, 1, M2, 1, M2, 0, log_h, st, tix)
-            : launch_tile_v<4>(in, scratch, L1, width, h_in, M2, 1, M2, 1, M2, 0, log_h, st, tix);
   } else {
     e = tile_any(in, scratch, L1, width, h_in, M2, 1, M2, 1, M2, 0, log_h, st);
   }
@@ -772,10 +699,8 @@ cudaError_t init_device_tables() {
   if (e == cudaSuccess) e = cudaFuncSetAttribute(dft_tile<1>, cudaFuncAttributeMaxDynamicSharedMemorySize, tile_smem_max(1));
   if (e == cudaSuccess) e = cudaFuncSetAttribute(dft_tile_v<8>, cudaFuncAttributeMaxDynamicSharedMemorySize, tile_smem_max(8));
   if (e == cudaSuccess) e = cudaFuncSetAttribute(dft_tile_v<4>, cudaFuncAttributeMaxDynamicSharedMemorySize, tile_smem_max(4));
-  for (auto f : {dft_tile_v2<8, false>, dft_tile_v2<8, true>})
-    if (e == cudaSuccess) e = cudaFuncSetAttribute(f, cudaFuncAttributeMaxDynamicSharedMemorySize, tile_smem_max(8));
-  for (auto f : {dft_tile_v2<4, false>, dft_tile_v2<4, true>})
-    if (e == cudaSuccess) e = cudaFuncSetAttribute(f, cudaFuncAttributeMaxDynamicSharedMemorySize, tile_smem_max(4));
+  if (e == cudaSuccess) e = cudaFuncSetAttribute(dft_tile_v2<8>, cudaFuncAttributeMaxDynamicSharedMemorySize, tile_smem_max(8));
+  if (e == cudaSuccess) e = cudaFuncSetAttribute(dft_tile_v2<4>, cudaFuncAttributeMaxDynamicSharedMemorySize, tile_smem_max(4));
   if (e == cudaSuccess) done[dev] = true;
   return e;
 }

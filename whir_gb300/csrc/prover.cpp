@@ -252,14 +252,13 @@ static E4 reduce_acc(const unsigned long long *a) {
 
 // ---------------- encode + commit ----------------
 void encode_commit(Context &ctx, const uint32_t *src, int k, int rate, int folding, int dim,
-                   uint32_t *codeword, uint32_t *scratch, uint32_t *nodes, DeviceTree *out,
-                   uint32_t *tee) {
+                   uint32_t *codeword, uint32_t *scratch, uint32_t *nodes, DeviceTree *out) {
   cudaStream_t st = ctx.stream();
   int log_h = k + rate - folding;
   size_t width = (size_t)dim << folding, h_in = (size_t)1 << (k - folding);
   size_t rows = (size_t)1 << log_h;
   ctx.prof_begin(Context::K_DFT);
-  cuda_check(gpu::dft_batch(src, h_in, width, log_h, codeword, scratch, st, tee), "dft_batch");
+  cuda_check(gpu::dft_batch(src, h_in, width, log_h, codeword, scratch, st), "dft_batch");
   ctx.prof_end(Context::K_DFT, 4.0 * (double)(h_in * width + rows * width));
   ctx.prof_begin(Context::K_LEAF);
   cuda_check(gpu::hash_rows(codeword, rows, (int)width, nodes, st), "hash_rows");
@@ -1280,38 +1279,16 @@ void Prover::commit(Transcript &ts, const uint32_t *polys, bool on_device,
   size_t total = (size_t)1 << p_.k;
   uint32_t *stk = m.stacked.as<uint32_t>();
   if (m.n_polys > 1) cuda_check(cudaMemsetAsync(stk, 0, 4 * total, st), "memset");
-  // One polynomial in pinned host memory: the encoding reads it over the
-  // host link directly and leaves the device copy the later passes read
-  // (the input crosses the link once, overlapped with the first DFT pass,
-  // instead of a copy ahead of it).  Otherwise copy, then encode.
-  const uint32_t *mapped = nullptr;
-  if (m.n_polys == 1 && poly_k[0] == p_.k && m.poly_off[0] == 0 && !on_device) {
-    cudaPointerAttributes at{};
-    if (cudaPointerGetAttributes(&at, polys) == cudaSuccess && at.type == cudaMemoryTypeHost &&
-        at.devicePointer) {
-      const uint32_t *d = static_cast<const uint32_t *>(at.devicePointer);
-      if (gpu::dft_tee_supported(d, stk, (size_t)1 << (p_.k - p_.folding),
-                                 (size_t)1 << p_.folding, p_.k + p_.rate - p_.folding))
-        mapped = d;
-    }
-    cudaGetLastError();  // an unregistered pointer is not an error here
+  size_t src_off = 0;
+  for (int id = 0; id < m.n_polys; id++) {
+    size_t n = (size_t)1 << poly_k[id];
+    cuda_check(copy_async(*ctx_, stk + m.poly_off[id], polys + src_off, 4 * n,
+                          on_device ? cudaMemcpyDeviceToDevice : cudaMemcpyHostToDevice),
+               "poly copy");
+    src_off += n;
   }
-  if (mapped) {
-    ctx_->count_copy(4 * total, cudaMemcpyHostToDevice);
-    encode_commit(*ctx_, mapped, p_.k, p_.rate, p_.folding, 1, m.cw0.as<uint32_t>(),
-                  m.scratch.as<uint32_t>(), m.tree0.as<uint32_t>(), &m.t0, stk);
-  } else {
-    size_t src_off = 0;
-    for (int id = 0; id < m.n_polys; id++) {
-      size_t n = (size_t)1 << poly_k[id];
-      cuda_check(copy_async(*ctx_, stk + m.poly_off[id], polys + src_off, 4 * n,
-                            on_device ? cudaMemcpyDeviceToDevice : cudaMemcpyHostToDevice),
-                 "poly copy");
-      src_off += n;
-    }
-    encode_commit(*ctx_, stk, p_.k, p_.rate, p_.folding, 1, m.cw0.as<uint32_t>(),
-                  m.scratch.as<uint32_t>(), m.tree0.as<uint32_t>(), &m.t0);
-  }
+  encode_commit(*ctx_, stk, p_.k, p_.rate, p_.folding, 1, m.cw0.as<uint32_t>(),
+                m.scratch.as<uint32_t>(), m.tree0.as<uint32_t>(), &m.t0);
   ts.write_digest(m.t0.root);
 }
 

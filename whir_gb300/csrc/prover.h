@@ -154,13 +154,9 @@ struct DeviceTree {
   uint32_t root[8];
 };
 
-// Reed-Solomon encode + Merkle commit of `src` (2^k rows... see commit_rows).
-// tee: `src` is pinned host memory (its device address) and the encoding also
-// leaves a device copy of it at `tee` (gpu::dft_batch); needs
-// gpu::dft_tee_supported for the shape.
+// Reed-Solomon encode + Merkle commit of `src` (2^k rows... see commit_rows)
 void encode_commit(Context &ctx, const uint32_t *src, int k, int rate, int folding, int dim,
-                   uint32_t *codeword, uint32_t *scratch, uint32_t *nodes, DeviceTree *out,
-                   uint32_t *tee = nullptr);
+                   uint32_t *codeword, uint32_t *scratch, uint32_t *nodes, DeviceTree *out);
 
 class Prover {
  public:
