@@ -93,3 +93,21 @@ def test_max_sizes_verify(ctx, oracle, k, rate):
     assert rc == 0 and vcp == cp
     again, cp2 = W.prove_harness(ctx, params, [poly], [k], [[0]] * 2)
     assert again == proof and cp2 == cp
+
+
+@pytest.mark.parametrize("k,f,rate", [(12, 4, 2), (18, 4, 2), (9, 1, 1)])
+def test_pinned_host_input(ctx, oracle, k, f, rate):
+    # the bench's end-to-end input: a polynomial in pinned host memory
+    torch = pytest.importorskip("torch")
+    poly = oracle.rand_fe(21 + k, 1 << k)
+    pinned = torch.empty(1 << k, dtype=torch.int32, pin_memory=True)
+    host = pinned.numpy().view(np.uint32)
+    host[:] = poly
+    params = (k, f, rate, 1, 1, 100 if f == 4 else 32)
+    _, h2d0, _ = ctx.counters()
+    proof, cp = W.prove_harness(ctx, params, host, [k], [[0], [0]])
+    _, h2d1, _ = ctx.counters()
+    assert h2d1 - h2d0 >= 4 << k  # the polynomial crossed the host link, counted
+    want, wcp = oracle.prove(params, [poly], [k], [[0], [0]])
+    assert proof == want and cp == wcp
+    assert np.array_equal(host, poly)  # the input is only read
