@@ -114,7 +114,8 @@ def test_combine_eqs(ctx, oracle, k, n):
     assert np.array_equal(dw.download(4 << k), oracle.combine_eqs(w, k, pts, n, alpha))
 
 
-@pytest.mark.parametrize("k,n,shift", [(2, 1, 0), (5, 2, 11), (9, 10, 3), (9, 11, 11), (16, 52, 2)])
+@pytest.mark.parametrize("k,n,shift", [(2, 1, 0), (5, 2, 11), (9, 10, 3), (9, 11, 11), (16, 52, 2),
+                                         (17, 108, 0), (18, 1, 5), (18, 300, 1)])
 def test_combine_pows(ctx, oracle, k, n, shift):
     w = rand(oracle, 23, 4 << k)
     vars_ = rand(oracle, 24, n)

@@ -326,19 +326,79 @@ __global__ void pow_tables_kernel(const uint32_t *__restrict__ vars, int n, int 
 }
 
 // w[i] += sum_t scale_t * var_t^i, one thread per i
-__global__ void add_pows_kernel(E4 *__restrict__ w, size_t n_out, int s, int n,
-                                const uint32_t *__restrict__ tab, const E4 *__restrict__ scales) {
-  size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
-  if (i >= n_out) return;
+// w[i] += sum_t scale_t * lo_t[i mod 2^s] * hi_t[i >> s] (per-point power
+// tables from pow_tables).  When 2^s >= the CTA size every thread of a CTA
+// shares hi_t, so the CTA first forms S_t = scale_t * hi_t in shared memory
+// and each thread then adds S_t * lo_t: four 64-bit products per point,
+// folded every three points (2^32 = 2^32 - 2p mod p keeps the sum below
+// 2^58) and reduced once.  Otherwise every thread forms the products itself.
+constexpr int AP_T = 256;
+constexpr uint32_t FOLD_2_32 = (uint32_t)((1ull << 32) % kb::P);
+__device__ __forceinline__ unsigned long long fold_2_32(unsigned long long x) {
+  return (unsigned long long)(uint32_t)(x >> 32) * FOLD_2_32 + (uint32_t)x;  // < 2^57 + 2^32
+}
+template <class SCALE>
+__device__ __forceinline__ void add_pows_body(E4 *__restrict__ w, size_t n_out, int s, int n,
+                                              const uint32_t *__restrict__ tab,
+                                              const SCALE &scale) {
+  extern __shared__ E4 sh[];
   const size_t nlo = (size_t)1 << s, per = nlo + (n_out >> s);
+  const size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (nlo >= blockDim.x) {  // one hi index per CTA
+    const size_t ih = nlo + (((size_t)blockIdx.x * blockDim.x) >> s);
+    for (int t = threadIdx.x; t < n; t += blockDim.x)
+      sh[t] = kb::e_scale(scale(t), __ldg(tab + (size_t)t * per + ih));
+    __syncthreads();
+    if (i >= n_out) return;
+    const uint32_t *tb = tab + (i & (nlo - 1));
+    unsigned long long a[4] = {0, 0, 0, 0};
+    int t = 0;
+    for (; t + 2 < n; t += 3) {
+      uint32_t x[3];
+#pragma unroll
+      for (int u = 0; u < 3; u++) x[u] = __ldg(tb + (size_t)(t + u) * per);
+#pragma unroll
+      for (int u = 0; u < 3; u++) {
+        const E4 sc = sh[t + u];
+#pragma unroll
+        for (int c = 0; c < 4; c++) a[c] += (unsigned long long)sc.c[c] * x[u];
+      }
+#pragma unroll
+      for (int c = 0; c < 4; c++) a[c] = fold_2_32(a[c]);
+    }
+    for (; t < n; t++) {
+      const uint32_t x = __ldg(tb + (size_t)t * per);
+      const E4 sc = sh[t];
+#pragma unroll
+      for (int c = 0; c < 4; c++) a[c] = fold_2_32(a[c] + (unsigned long long)sc.c[c] * x);
+    }
+    E4 add;
+#pragma unroll
+    for (int c = 0; c < 4; c++) add.c[c] = kb::reduce_wide(a[c]);
+    w[i] = kb::e_add(w[i], add);
+    return;
+  }
+  if (i >= n_out) return;
   const size_t il = i & (nlo - 1), ih = nlo + (i >> s);
   E4 acc = w[i];
   for (int t = 0; t < n; t++) {
     const uint32_t *tb = tab + (size_t)t * per;
     uint32_t pw = kb::mul(__ldg(tb + il), __ldg(tb + ih));
-    acc = kb::e_add(acc, kb::e_scale(scales[t], pw));
+    acc = kb::e_add(acc, kb::e_scale(scale(t), pw));
   }
   w[i] = acc;
+}
+struct ScalePtr {
+  const E4 *p;
+  __device__ __forceinline__ E4 operator()(int t) const { return p[t]; }
+};
+struct ScaleVal {
+  const PowArgs *a;
+  __device__ __forceinline__ E4 operator()(int t) const { return a->scales[t]; }
+};
+__global__ void add_pows_kernel(E4 *__restrict__ w, size_t n_out, int s, int n,
+                                const uint32_t *__restrict__ tab, const E4 *__restrict__ scales) {
+  add_pows_body(w, n_out, s, n, tab, ScalePtr{scales});
 }
 
 // the same two passes with the variables and scales passed by value
@@ -354,17 +414,13 @@ __global__ void pow_tables_val_kernel(const __grid_constant__ PowArgs a, int n, 
 __global__ void add_pows_val_kernel(E4 *__restrict__ w, size_t n_out, int s, int n,
                                     const uint32_t *__restrict__ tab,
                                     const __grid_constant__ PowArgs a) {
-  size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
-  if (i >= n_out) return;
-  const size_t nlo = (size_t)1 << s, per = nlo + (n_out >> s);
-  const size_t il = i & (nlo - 1), ih = nlo + (i >> s);
-  E4 acc = w[i];
-  for (int t = 0; t < n; t++) {
-    const uint32_t *tb = tab + (size_t)t * per;
-    uint32_t pw = kb::mul(__ldg(tb + il), __ldg(tb + ih));
-    acc = kb::e_add(acc, kb::e_scale(a.scales[t], pw));
-  }
-  w[i] = acc;
+  add_pows_body(w, n_out, s, n, tab, ScaleVal{&a});
+}
+
+// shared memory of add_pows_body: the S_t of one CTA (none without them)
+static size_t add_pows_smem(int k, int n) {
+  int s = k / 2;
+  return ((size_t)1 << s) >= (size_t)AP_T ? (size_t)n * sizeof(E4) : 0;
 }
 
 cudaError_t add_pows_val(E4 *w, int k, const PowArgs &a, int n, uint32_t *tab, cudaStream_t st) {
@@ -375,7 +431,8 @@ cudaError_t add_pows_val(E4 *w, int k, const PowArgs &a, int n, uint32_t *tab, c
   pow_tables_val_kernel<<<(unsigned)((words + 255) / 256), 256, 0, st>>>(a, n, s, k, tab);
   count_launches(1);
   size_t N = (size_t)1 << k;
-  add_pows_val_kernel<<<(unsigned)((N + 255) / 256), 256, 0, st>>>(w, N, s, n, tab, a);
+  add_pows_val_kernel<<<(unsigned)((N + AP_T - 1) / AP_T), AP_T, add_pows_smem(k, n), st>>>(
+      w, N, s, n, tab, a);
   count_launches(1);
   return cudaGetLastError();
 }
@@ -393,7 +450,9 @@ cudaError_t add_pows(E4 *w, int k, const uint32_t *vars, const E4 *scales, int n
   pow_tables_kernel<<<(unsigned)((words + 255) / 256), 256, 0, st>>>(vars, n, s, k, tab);
   count_launches(1);
   size_t N = (size_t)1 << k;
-  add_pows_kernel<<<(unsigned)((N + 255) / 256), 256, 0, st>>>(w, N, s, n, tab, scales);
+  const size_t smem = add_pows_smem(k, n);
+  if (smem > 48 * 1024) return cudaErrorInvalidValue;  // more than 3072 points
+  add_pows_kernel<<<(unsigned)((N + AP_T - 1) / AP_T), AP_T, smem, st>>>(w, N, s, n, tab, scales);
   count_launches(1);
   return cudaGetLastError();
 }
