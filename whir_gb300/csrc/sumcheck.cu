@@ -27,15 +27,21 @@ __device__ __forceinline__ void acc_add(unsigned long long *a, const E4 &v) {
 // calls it.
 __device__ __forceinline__ void publish_if_last(unsigned long long *acc, const Publish &pub) {
   if (!pub.host) return;
-  __shared__ bool last;
-  __threadfence();  // this CTA's atomics are visible before its ticket
-  __syncthreads();
-  if (threadIdx.x == 0) last = atomicAdd(pub.counter, 1u) == gridDim.x - 1;
-  __syncthreads();
-  if (!last) return;
-  __threadfence();
+  if (gridDim.x == 1) {
+    // the only CTA is the last: its atomics on acc precede the exchanges
+    // below in the same memory location's order, no ticket or fence needed
+    __syncthreads();
+  } else {
+    __shared__ bool last;
+    __threadfence();  // this CTA's atomics are visible before its ticket
+    __syncthreads();
+    if (threadIdx.x == 0) last = atomicAdd(pub.counter, 1u) == gridDim.x - 1;
+    __syncthreads();
+    if (!last) return;
+    __threadfence();
+  }
   for (int i = threadIdx.x; i < pub.words; i += blockDim.x) pub.host[i] = atomicExch(acc + i, 0ull);
-  if (threadIdx.x == 0) atomicExch(pub.counter, 0u);
+  if (threadIdx.x == 0 && gridDim.x > 1) atomicExch(pub.counter, 0u);
   if (pub.flag) {
     __threadfence_system();  // the results reach host memory before the flag
     __syncthreads();
