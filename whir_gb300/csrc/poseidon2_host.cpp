@@ -92,6 +92,7 @@ void build(Poseidon2Constants &c, int width) {
   for (int i = 0; i < width; i++) {
     const int *v = width == 16 ? v16[i] : v24[i];
     c.diag[i] = diag_value(v[0], (uint32_t)v[1], v[2]);
+    c.diag_plain[i] = kb::to_canonical(c.diag[i]);
   }
   ChaCha12 rng(1000);
   for (int r = 0; r < 8; r++)
@@ -99,22 +100,36 @@ void build(Poseidon2Constants &c, int width) {
   for (int r = 0; r < c.rounds_p; r++) c.int_rc[r] = rng.next_field();
 }
 
-void mat4(uint32_t *x) {
-  using namespace kb;
-  uint32_t t01 = add(x[0], x[1]), t23 = add(x[2], x[3]);
-  uint32_t t0123 = add(t01, t23);
-  uint32_t t01123 = add(t0123, x[1]), t01233 = add(t0123, x[3]);
-  uint32_t y3 = add(t01233, dbl(x[0]));
-  uint32_t y1 = add(t01123, dbl(x[2]));
-  uint32_t y0 = add(t01123, t01);
-  uint32_t y2 = add(t01233, t23);
+// The linear layers in 64-bit lanes with one reduction per output word (the
+// compiler turns % p into a multiply-high and a subtract).
+inline void mat4_wide(uint64_t *x) {
+  uint64_t t01 = x[0] + x[1], t23 = x[2] + x[3];
+  uint64_t t0123 = t01 + t23;
+  uint64_t t01123 = t0123 + x[1], t01233 = t0123 + x[3];
+  uint64_t y3 = t01233 + 2 * x[0];
+  uint64_t y1 = t01123 + 2 * x[2];
+  uint64_t y0 = t01123 + t01;
+  uint64_t y2 = t01233 + t23;
   x[0] = y0; x[1] = y1; x[2] = y2; x[3] = y3;
 }
+// light MDS of canonical words: every output below 49 p before its reduction
 void mds_light(uint32_t *s, int w) {
-  for (int i = 0; i < w; i += 4) mat4(s + i);
-  uint32_t sums[4] = {0, 0, 0, 0};
-  for (int i = 0; i < w; i++) sums[i & 3] = kb::add(sums[i & 3], s[i]);
-  for (int i = 0; i < w; i++) s[i] = kb::add(s[i], sums[i & 3]);
+  uint64_t x[24];
+  for (int i = 0; i < w; i++) x[i] = s[i];
+  for (int i = 0; i < w; i += 4) mat4_wide(x + i);
+  uint64_t sums[4] = {0, 0, 0, 0};
+  for (int i = 0; i < w; i++) sums[i & 3] += x[i];
+  for (int i = 0; i < w; i++) s[i] = (uint32_t)((x[i] + sums[i & 3]) % kb::P);
+}
+// s_i <- sum + d_i s_i: the Montgomery word times the plain residue d_i is
+// the Montgomery word of the product (below p 2^31 before its reduction)
+void internal_layer(const Poseidon2Constants &c, uint32_t *s) {
+  const int w = c.width;
+  uint64_t total = 0;
+  for (int i = 0; i < w; i++) total += s[i];
+  const uint64_t sum = total % kb::P;
+  for (int i = 0; i < w; i++)
+    s[i] = (uint32_t)((sum + (uint64_t)s[i] * c.diag_plain[i]) % kb::P);
 }
 
 }  // namespace
@@ -139,9 +154,7 @@ void poseidon2_permute_host(const Poseidon2Constants &c, uint32_t *s) {
   }
   for (int r = 0; r < c.rounds_p; r++) {
     s[0] = cube(add(s[0], c.int_rc[r]));
-    uint32_t sum = 0;
-    for (int i = 0; i < w; i++) sum = add(sum, s[i]);
-    for (int i = 0; i < w; i++) s[i] = add(sum, mul(c.diag[i], s[i]));
+    internal_layer(c, s);
   }
   for (int r = 4; r < 8; r++) {
     for (int i = 0; i < w; i++) s[i] = cube(add(s[i], c.ext_rc[r][i]));
