@@ -487,6 +487,25 @@ __device__ __forceinline__ void block_acc(const E4 (&v)[NV], unsigned long long 
 
 // One round: new[i] = a[2i] + r (a[2i+1] - a[2i]) for poly and weights (when
 // folding), then c0 += w[2m] p[2m], c2 += (2 w[2m+1] - w[2m]) (2 p[2m+1] - p[2m]).
+// Extension elements through 16-byte accesses when the arrays are 16-byte
+// aligned (VEC; E4 itself only promises 4), word by word otherwise.
+template <bool VEC>
+__device__ __forceinline__ E4 ld_e4(const E4 *p) {
+  if constexpr (VEC) {
+    const uint4 v = __ldg(reinterpret_cast<const uint4 *>(p));
+    return E4{{v.x, v.y, v.z, v.w}};
+  } else {
+    return *p;
+  }
+}
+template <bool VEC>
+__device__ __forceinline__ void st_e4(E4 *p, const E4 &a) {
+  if constexpr (VEC) *reinterpret_cast<uint4 *>(p) = make_uint4(a.c[0], a.c[1], a.c[2], a.c[3]);
+  else *p = a;
+}
+__host__ __forceinline__ bool aligned16(const void *p) { return ((uintptr_t)p & 15) == 0; }
+
+template <bool VEC>
 __global__ void __launch_bounds__(256) round_kernel(const E4 *__restrict__ p_in,
                                                     const E4 *__restrict__ w_in, size_t n_in,
                                                     int fold, E4 r, E4 *__restrict__ p_out,
@@ -500,19 +519,27 @@ __global__ void __launch_bounds__(256) round_kernel(const E4 *__restrict__ p_in,
     E4 p0, p1 = kb::e_zero(), w0, w1 = kb::e_zero();
     if (fold) {
       const E4 *pp = p_in + 4 * m, *ww = w_in + 4 * m;
-      p0 = kb::e_add(pp[0], kb::e_mul(r, kb::e_sub(pp[1], pp[0])));
-      w0 = kb::e_add(ww[0], kb::e_mul(r, kb::e_sub(ww[1], ww[0])));
-      p_out[2 * m] = p0;
-      w_out[2 * m] = w0;
-      if (2 * m + 1 < n) {
-        p1 = kb::e_add(pp[2], kb::e_mul(r, kb::e_sub(pp[3], pp[2])));
-        w1 = kb::e_add(ww[2], kb::e_mul(r, kb::e_sub(ww[3], ww[2])));
-        p_out[2 * m + 1] = p1;
-        w_out[2 * m + 1] = w1;
+      const bool two = 2 * m + 1 < n;
+      const E4 a0 = ld_e4<VEC>(pp), a1 = ld_e4<VEC>(pp + 1);
+      const E4 b0 = ld_e4<VEC>(ww), b1 = ld_e4<VEC>(ww + 1);
+      E4 a2 = kb::e_zero(), a3 = kb::e_zero(), b2 = kb::e_zero(), b3 = kb::e_zero();
+      if (two) {
+        a2 = ld_e4<VEC>(pp + 2); a3 = ld_e4<VEC>(pp + 3);
+        b2 = ld_e4<VEC>(ww + 2); b3 = ld_e4<VEC>(ww + 3);
+      }
+      p0 = kb::e_add(a0, kb::e_mul(r, kb::e_sub(a1, a0)));
+      w0 = kb::e_add(b0, kb::e_mul(r, kb::e_sub(b1, b0)));
+      st_e4<VEC>(p_out + 2 * m, p0);
+      st_e4<VEC>(w_out + 2 * m, w0);
+      if (two) {
+        p1 = kb::e_add(a2, kb::e_mul(r, kb::e_sub(a3, a2)));
+        w1 = kb::e_add(b2, kb::e_mul(r, kb::e_sub(b3, b2)));
+        st_e4<VEC>(p_out + 2 * m + 1, p1);
+        st_e4<VEC>(w_out + 2 * m + 1, w1);
       }
     } else {
-      p0 = p_in[2 * m]; w0 = w_in[2 * m];
-      if (2 * m + 1 < n) { p1 = p_in[2 * m + 1]; w1 = w_in[2 * m + 1]; }
+      p0 = ld_e4<VEC>(p_in + 2 * m); w0 = ld_e4<VEC>(w_in + 2 * m);
+      if (2 * m + 1 < n) { p1 = ld_e4<VEC>(p_in + 2 * m + 1); w1 = ld_e4<VEC>(w_in + 2 * m + 1); }
     }
     if (coeffs && 2 * m + 1 < n) {
       sums[0] = kb::e_add(sums[0], kb::e_mul(w0, p0));
@@ -531,8 +558,14 @@ cudaError_t sumcheck_round(const E4 *p_in, const E4 *w_in, size_t n_in, bool fol
   unsigned T = 256;
   size_t g = (pairs + T - 1) / T;
   unsigned grid = (unsigned)(g < 152 * 8 ? (g ? g : 1) : 152 * 8);
-  round_kernel<<<grid, T, 0, st>>>(p_in, w_in, n_in, fold ? 1 : 0, r, p_out, w_out,
-                                   coeffs ? 1 : 0, acc, coeffs ? pub : Publish());
+  const bool vec = aligned16(p_in) && aligned16(w_in) &&
+                   (!fold || (aligned16(p_out) && aligned16(w_out)));
+  if (vec)
+    round_kernel<true><<<grid, T, 0, st>>>(p_in, w_in, n_in, fold ? 1 : 0, r, p_out, w_out,
+                                           coeffs ? 1 : 0, acc, coeffs ? pub : Publish());
+  else
+    round_kernel<false><<<grid, T, 0, st>>>(p_in, w_in, n_in, fold ? 1 : 0, r, p_out, w_out,
+                                            coeffs ? 1 : 0, acc, coeffs ? pub : Publish());
   count_launches(1);
   return cudaGetLastError();
 }
