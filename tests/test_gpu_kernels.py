@@ -127,3 +127,50 @@ def test_combine_pows(ctx, oracle, k, n, shift):
     dw2 = ctx.to_device(w)
     W.combine_pows_scaled(ctx, dw2, k, vars_, n, scales)
     assert np.array_equal(dw2.download(4 << k), oracle.combine_pows_scaled(w, k, vars_, n, scales))
+
+
+class Shifted:
+    """A device array starting one word past a 16-byte boundary: extension
+    elements there are 4-byte aligned only, which the kernels must accept."""
+
+    def __init__(self, ctx, arr):
+        arr = np.ascontiguousarray(arr, np.uint32)
+        self.ctx = ctx
+        self.base = W.DeviceArray(ctx, arr.nbytes + 16)
+        self.ptr = self.base.ptr + 4
+        W._check(W.lib().whir_copy_to_device(ctx.h, self.ptr, arr.ctypes.data, arr.nbytes))
+
+    def download(self, n_words):
+        out = np.empty(n_words, np.uint32)
+        W._check(W.lib().whir_copy_to_host(self.ctx.h, out.ctypes.data, self.ptr, out.nbytes))
+        return out
+
+
+@pytest.mark.parametrize("k", [9, 16])
+def test_unaligned_extension_arrays(ctx, oracle, k):
+    # the word-by-word variants of the kernels that otherwise move extension
+    # elements as 16-byte vectors
+    p = rand(oracle, 31, 4 << k)
+    w = rand(oracle, 32, 4 << k)
+    pt = rand(oracle, 33, 4 * k)
+    assert np.array_equal(W.eval_ext(ctx, Shifted(ctx, p), k, pt), oracle.eval_ext(p, k, pt))
+    c0, c2 = W.sumcheck_coeffs(ctx, Shifted(ctx, p), Shifted(ctx, w), k)
+    e0, e2 = oracle.coeffs(p, w, k)
+    assert np.array_equal(c0, e0) and np.array_equal(c2, e2)
+    r = rand(oracle, 34, 4)
+    po, wo = W.sumcheck_fold(ctx, Shifted(ctx, p), Shifted(ctx, w), k, r)
+    assert np.array_equal(po.download(4 << (k - 1)), oracle.fix_lo(p, k, r))
+    assert np.array_equal(wo.download(4 << (k - 1)), oracle.fix_lo(w, k, r))
+    pts = rand(oracle, 35, 4 * k * 3)
+    alpha = rand(oracle, 36, 4)
+    dw = Shifted(ctx, w)
+    W.combine_eqs(ctx, dw, k, pts, 3, alpha)
+    assert np.array_equal(dw.download(4 << k), oracle.combine_eqs(w, k, pts, 3, alpha))
+    vars_ = rand(oracle, 37, 5)
+    dw = Shifted(ctx, w)
+    W.combine_pows(ctx, dw, k, vars_, 5, alpha, 1)
+    assert np.array_equal(dw.download(4 << k), oracle.combine_pows(w, k, vars_, 5, alpha, 1))
+    base = rand(oracle, 38, 1 << k)
+    rs = rand(oracle, 39, 4 * 4)
+    got = W.compress_lo(ctx, Shifted(ctx, base), k, rs, 4).download(4 << (k - 4))
+    assert np.array_equal(got, oracle.compress_lo(base, k, rs, 4))

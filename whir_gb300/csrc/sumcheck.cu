@@ -20,6 +20,25 @@ __device__ __forceinline__ void acc_add(unsigned long long *a, const E4 &v) {
   for (int c = 0; c < 4; c++) atomicAdd(a + c, (unsigned long long)v.c[c]);
 }
 
+// Extension elements through 16-byte accesses when the arrays are 16-byte
+// aligned (VEC; E4 itself only promises 4), word by word otherwise.
+template <bool VEC>
+__device__ __forceinline__ E4 ld_e4(const E4 *p) {
+  if constexpr (VEC) {
+    const uint4 v = *reinterpret_cast<const uint4 *>(p);
+    return E4{{v.x, v.y, v.z, v.w}};
+  } else {
+    return *p;
+  }
+}
+template <bool VEC>
+__device__ __forceinline__ void st_e4(E4 *p, const E4 &a) {
+  if constexpr (VEC) *reinterpret_cast<uint4 *>(p) = make_uint4(a.c[0], a.c[1], a.c[2], a.c[3]);
+  else *p = a;
+}
+__host__ __forceinline__ bool aligned16(const void *p) { return ((uintptr_t)p & 15) == 0; }
+
+
 // eq table entries over z[off .. off+nv) times scale: entry b selects z_i
 // when bit i of b is set, 1 - z_i otherwise (Point::eq, point.rs:159-175).
 // Publish (kernels.h): after this CTA's atomics into acc, the last CTA of
@@ -260,6 +279,7 @@ cudaError_t compress_hi(const uint32_t *poly, int k, int ks, const E4 *eq_lo, in
 }
 
 // compress_lo: out[i] = sum_j eq(rs)[j] * P[i * 2^ks + j]
+template <bool VEC>
 __global__ void compress_lo_kernel(const uint32_t *__restrict__ poly, int ks, size_t n_out,
                                    Point rs, E4 *__restrict__ out) {
   __shared__ E4 eq[256];
@@ -275,8 +295,18 @@ __global__ void compress_lo_kernel(const uint32_t *__restrict__ poly, int ks, si
        i += (size_t)gridDim.x * blockDim.x) {
     const uint32_t *row = poly + i * W;
     E4 acc = kb::e_zero();
-    for (int j = 0; j < W; j++) acc = kb::e_add(acc, kb::e_scale(eq[j], __ldg(row + j)));
-    out[i] = acc;
+    if (VEC) {  // rows of a multiple of 4 words, 16-byte aligned
+      for (int j = 0; j < W; j += 4) {
+        const uint4 v = __ldg(reinterpret_cast<const uint4 *>(row + j));
+        acc = kb::e_add(acc, kb::e_scale(eq[j], v.x));
+        acc = kb::e_add(acc, kb::e_scale(eq[j + 1], v.y));
+        acc = kb::e_add(acc, kb::e_scale(eq[j + 2], v.z));
+        acc = kb::e_add(acc, kb::e_scale(eq[j + 3], v.w));
+      }
+    } else {
+      for (int j = 0; j < W; j++) acc = kb::e_add(acc, kb::e_scale(eq[j], __ldg(row + j)));
+    }
+    st_e4<VEC>(out + i, acc);
   }
 }
 
@@ -287,22 +317,26 @@ cudaError_t compress_lo(const uint32_t *poly, int k, const Point &rs, E4 *out, c
   unsigned T = 256;
   size_t g = (n_out + T - 1) / T;
   unsigned grid = (unsigned)(g < 152 * 16 ? g : 152 * 16);
-  compress_lo_kernel<<<grid, T, 0, st>>>(poly, ks, n_out, rs, out);
+  if (ks >= 2 && aligned16(poly) && aligned16(out))
+    compress_lo_kernel<true><<<grid, T, 0, st>>>(poly, ks, n_out, rs, out);
+  else
+    compress_lo_kernel<false><<<grid, T, 0, st>>>(poly, ks, n_out, rs, out);
   count_launches(1);
   return cudaGetLastError();
 }
 
 // w[i] += sum_t lo_t[i & mask] * hi_t[i >> s]
+template <bool VEC>
 __global__ void add_eq_kernel(E4 *w, size_t n, int s, size_t n_lo, size_t n_hi,
                               const E4 *__restrict__ tables, int n_tables) {
   for (size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x; i < n;
        i += (size_t)gridDim.x * blockDim.x) {
-    E4 acc = w[i];
+    E4 acc = ld_e4<VEC>(w + i);
     for (int t = 0; t < n_tables; t++) {
       const E4 *lo = tables + t * (n_lo + n_hi), *hi = lo + n_lo;
-      acc = kb::e_add(acc, kb::e_mul(lo[i & (n_lo - 1)], hi[i >> s]));
+      acc = kb::e_add(acc, kb::e_mul(ld_e4<VEC>(lo + (i & (n_lo - 1))), ld_e4<VEC>(hi + (i >> s))));
     }
-    w[i] = acc;
+    st_e4<VEC>(w + i, acc);
   }
 }
 
@@ -313,8 +347,12 @@ cudaError_t add_eq(E4 *w, int k, const E4 *tables, int n_tables, cudaStream_t st
   unsigned T = 256;
   size_t g = (n + T - 1) / T;
   unsigned grid = (unsigned)(g < 152 * 16 ? g : 152 * 16);
-  add_eq_kernel<<<grid, T, 0, st>>>(w, n, s, (size_t)1 << s, (size_t)1 << (k - s), tables,
-                                    n_tables);
+  if (aligned16(w) && aligned16(tables))
+    add_eq_kernel<true><<<grid, T, 0, st>>>(w, n, s, (size_t)1 << s, (size_t)1 << (k - s),
+                                            tables, n_tables);
+  else
+    add_eq_kernel<false><<<grid, T, 0, st>>>(w, n, s, (size_t)1 << s, (size_t)1 << (k - s),
+                                             tables, n_tables);
   count_launches(1);
   return cudaGetLastError();
 }
@@ -343,7 +381,7 @@ constexpr uint32_t FOLD_2_32 = (uint32_t)((1ull << 32) % kb::P);
 __device__ __forceinline__ unsigned long long fold_2_32(unsigned long long x) {
   return (unsigned long long)(uint32_t)(x >> 32) * FOLD_2_32 + (uint32_t)x;  // < 2^57 + 2^32
 }
-template <class SCALE>
+template <bool VEC, class SCALE>
 __device__ __forceinline__ void add_pows_body(E4 *__restrict__ w, size_t n_out, int s, int n,
                                               const uint32_t *__restrict__ tab,
                                               const SCALE &scale) {
@@ -381,18 +419,18 @@ __device__ __forceinline__ void add_pows_body(E4 *__restrict__ w, size_t n_out, 
     E4 add;
 #pragma unroll
     for (int c = 0; c < 4; c++) add.c[c] = kb::reduce_wide(a[c]);
-    w[i] = kb::e_add(w[i], add);
+    st_e4<VEC>(w + i, kb::e_add(ld_e4<VEC>(w + i), add));
     return;
   }
   if (i >= n_out) return;
   const size_t il = i & (nlo - 1), ih = nlo + (i >> s);
-  E4 acc = w[i];
+  E4 acc = ld_e4<VEC>(w + i);
   for (int t = 0; t < n; t++) {
     const uint32_t *tb = tab + (size_t)t * per;
     uint32_t pw = kb::mul(__ldg(tb + il), __ldg(tb + ih));
     acc = kb::e_add(acc, kb::e_scale(scale(t), pw));
   }
-  w[i] = acc;
+  st_e4<VEC>(w + i, acc);
 }
 struct ScalePtr {
   const E4 *p;
@@ -402,9 +440,10 @@ struct ScaleVal {
   const PowArgs *a;
   __device__ __forceinline__ E4 operator()(int t) const { return a->scales[t]; }
 };
+template <bool VEC>
 __global__ void add_pows_kernel(E4 *__restrict__ w, size_t n_out, int s, int n,
                                 const uint32_t *__restrict__ tab, const E4 *__restrict__ scales) {
-  add_pows_body(w, n_out, s, n, tab, ScalePtr{scales});
+  add_pows_body<VEC>(w, n_out, s, n, tab, ScalePtr{scales});
 }
 
 // the same two passes with the variables and scales passed by value
@@ -417,10 +456,11 @@ __global__ void pow_tables_val_kernel(const __grid_constant__ PowArgs a, int n, 
   uint64_t e = j < nlo ? j : (uint64_t)(j - nlo) << s;
   tab[x] = kb::pow(a.vars[t], e);
 }
+template <bool VEC>
 __global__ void add_pows_val_kernel(E4 *__restrict__ w, size_t n_out, int s, int n,
                                     const uint32_t *__restrict__ tab,
                                     const __grid_constant__ PowArgs a) {
-  add_pows_body(w, n_out, s, n, tab, ScaleVal{&a});
+  add_pows_body<VEC>(w, n_out, s, n, tab, ScaleVal{&a});
 }
 
 // shared memory of add_pows_body: the S_t of one CTA (none without them)
@@ -437,8 +477,11 @@ cudaError_t add_pows_val(E4 *w, int k, const PowArgs &a, int n, uint32_t *tab, c
   pow_tables_val_kernel<<<(unsigned)((words + 255) / 256), 256, 0, st>>>(a, n, s, k, tab);
   count_launches(1);
   size_t N = (size_t)1 << k;
-  add_pows_val_kernel<<<(unsigned)((N + AP_T - 1) / AP_T), AP_T, add_pows_smem(k, n), st>>>(
-      w, N, s, n, tab, a);
+  const unsigned g = (unsigned)((N + AP_T - 1) / AP_T);
+  if (aligned16(w))
+    add_pows_val_kernel<true><<<g, AP_T, add_pows_smem(k, n), st>>>(w, N, s, n, tab, a);
+  else
+    add_pows_val_kernel<false><<<g, AP_T, add_pows_smem(k, n), st>>>(w, N, s, n, tab, a);
   count_launches(1);
   return cudaGetLastError();
 }
@@ -458,7 +501,11 @@ cudaError_t add_pows(E4 *w, int k, const uint32_t *vars, const E4 *scales, int n
   size_t N = (size_t)1 << k;
   const size_t smem = add_pows_smem(k, n);
   if (smem > 48 * 1024) return cudaErrorInvalidValue;  // more than 3072 points
-  add_pows_kernel<<<(unsigned)((N + AP_T - 1) / AP_T), AP_T, smem, st>>>(w, N, s, n, tab, scales);
+  const unsigned g = (unsigned)((N + AP_T - 1) / AP_T);
+  if (aligned16(w))
+    add_pows_kernel<true><<<g, AP_T, smem, st>>>(w, N, s, n, tab, scales);
+  else
+    add_pows_kernel<false><<<g, AP_T, smem, st>>>(w, N, s, n, tab, scales);
   count_launches(1);
   return cudaGetLastError();
 }
@@ -487,24 +534,6 @@ __device__ __forceinline__ void block_acc(const E4 (&v)[NV], unsigned long long 
 
 // One round: new[i] = a[2i] + r (a[2i+1] - a[2i]) for poly and weights (when
 // folding), then c0 += w[2m] p[2m], c2 += (2 w[2m+1] - w[2m]) (2 p[2m+1] - p[2m]).
-// Extension elements through 16-byte accesses when the arrays are 16-byte
-// aligned (VEC; E4 itself only promises 4), word by word otherwise.
-template <bool VEC>
-__device__ __forceinline__ E4 ld_e4(const E4 *p) {
-  if constexpr (VEC) {
-    const uint4 v = __ldg(reinterpret_cast<const uint4 *>(p));
-    return E4{{v.x, v.y, v.z, v.w}};
-  } else {
-    return *p;
-  }
-}
-template <bool VEC>
-__device__ __forceinline__ void st_e4(E4 *p, const E4 &a) {
-  if constexpr (VEC) *reinterpret_cast<uint4 *>(p) = make_uint4(a.c[0], a.c[1], a.c[2], a.c[3]);
-  else *p = a;
-}
-__host__ __forceinline__ bool aligned16(const void *p) { return ((uintptr_t)p & 15) == 0; }
-
 template <bool VEC>
 __global__ void __launch_bounds__(256) round_kernel(const E4 *__restrict__ p_in,
                                                     const E4 *__restrict__ w_in, size_t n_in,
@@ -571,6 +600,7 @@ cudaError_t sumcheck_round(const E4 *p_in, const E4 *w_in, size_t n_in, bool fol
 }
 
 // <eq(z), poly>: CTA walks hi blocks of 2^s_lo contiguous entries
+template <bool VEC>
 __global__ void __launch_bounds__(256) eval_ext_kernel(const E4 *__restrict__ poly, int k,
                                                        const E4 *__restrict__ eq_lo, int s_lo,
                                                        const E4 *__restrict__ eq_hi,
@@ -580,8 +610,8 @@ __global__ void __launch_bounds__(256) eval_ext_kernel(const E4 *__restrict__ po
   for (size_t hh = blockIdx.x; hh < n_hi; hh += gridDim.x) {
     E4 inner = kb::e_zero();
     for (size_t l = threadIdx.x; l < n_lo; l += blockDim.x)
-      inner = kb::e_add(inner, kb::e_mul(eq_lo[l], poly[hh * n_lo + l]));
-    outer = kb::e_add(outer, kb::e_mul(inner, eq_hi[hh]));
+      inner = kb::e_add(inner, kb::e_mul(ld_e4<VEC>(eq_lo + l), ld_e4<VEC>(poly + hh * n_lo + l)));
+    outer = kb::e_add(outer, kb::e_mul(inner, ld_e4<VEC>(eq_hi + hh)));
   }
   E4 v[1] = {outer};
   block_acc<1>(v, acc, pub);
@@ -591,7 +621,10 @@ cudaError_t eval_ext(const E4 *poly, int k, const E4 *eq_lo, int s_lo, const E4 
                      unsigned long long *acc, cudaStream_t st, const Publish &pub) {
   size_t n_hi = (size_t)1 << (k - s_lo);
   unsigned grid = (unsigned)(n_hi < 152 * 8 ? n_hi : 152 * 8);
-  eval_ext_kernel<<<grid, 256, 0, st>>>(poly, k, eq_lo, s_lo, eq_hi, acc, pub);
+  if (aligned16(poly) && aligned16(eq_lo) && aligned16(eq_hi))
+    eval_ext_kernel<true><<<grid, 256, 0, st>>>(poly, k, eq_lo, s_lo, eq_hi, acc, pub);
+  else
+    eval_ext_kernel<false><<<grid, 256, 0, st>>>(poly, k, eq_lo, s_lo, eq_hi, acc, pub);
   count_launches(1);
   return cudaGetLastError();
 }
