@@ -586,7 +586,7 @@ cudaError_t sumcheck_round(const E4 *p_in, const E4 *w_in, size_t n_in, bool fol
   size_t pairs = (n + 1) / 2;
   unsigned T = 256;
   size_t g = (pairs + T - 1) / T;
-  unsigned grid = (unsigned)(g < 152 * 8 ? (g ? g : 1) : 152 * 8);
+  unsigned grid = (unsigned)(g < 152 * 4 ? (g ? g : 1) : 152 * 4);
   const bool vec = aligned16(p_in) && aligned16(w_in) &&
                    (!fold || (aligned16(p_out) && aligned16(w_out)));
   if (vec)
