@@ -279,6 +279,9 @@ WHIR_API int whir_tune_reset(void);
  * blocked waiting for the stream (ms and number of waits).  read returns and
  * clears total ms, launches and algorithmic bytes since enabling. ---- */
 WHIR_API int whir_prof_enable(whir_ctx *ctx, int on);
+/* time only the classes whose bit (1 << klass) is set: fewer events on the
+ * stream while the rest runs untimed */
+WHIR_API int whir_prof_enable_classes(whir_ctx *ctx, unsigned mask);
 WHIR_API int whir_prof_read(whir_ctx *ctx, int klass, double *ms, long *launches, double *bytes);
 /* kernels launched by this library in this process, and the bytes the
  * prover of this context copied host->device / device->host, since start */

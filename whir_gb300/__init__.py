@@ -223,6 +223,13 @@ class Context:
     def prof_enable(self, on=True):
         _check(lib().whir_prof_enable(self.h, 1 if on else 0))
 
+    def prof_enable_classes(self, classes):
+        """Time only these classes (PROF_DFT, PROF_LEAF, ...)."""
+        mask = 0
+        for c in classes:
+            mask |= 1 << c
+        _check(lib().whir_prof_enable_classes(self.h, ctypes.c_uint(mask)))
+
     def counters(self):
         """(kernel launches in this process, prover h2d bytes, prover d2h bytes)"""
         a, b, c = ctypes.c_uint64(), ctypes.c_uint64(), ctypes.c_uint64()

@@ -746,6 +746,12 @@ int whir_prof_enable(whir_ctx *ctx, int on) {
   ctx->ctx.prof_enable(on != 0);
   API_END
 }
+int whir_prof_enable_classes(whir_ctx *ctx, unsigned mask) {
+  API_BEGIN
+  need(ctx != nullptr, "null context");
+  ctx->ctx.prof_enable_classes(mask);
+  API_END
+}
 int whir_prof_read(whir_ctx *ctx, int klass, double *ms, long *launches, double *bytes) {
   API_BEGIN
   need(ctx && ms && launches && bytes, "null argument");

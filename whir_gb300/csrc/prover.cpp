@@ -165,7 +165,7 @@ void Context::wait_flag(unsigned int seq) {
     }
     if (yield_) std::this_thread::yield();
   }
-  if (prof_) {
+  if (prof_on(K_SYNC)) {
     acc_ms_[K_SYNC] +=
         std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t0).count();
     acc_n_[K_SYNC] += 1;
@@ -173,7 +173,7 @@ void Context::wait_flag(unsigned int seq) {
 }
 
 void Context::sync() {
-  if (!prof_) {
+  if (!prof_on(K_SYNC)) {
     wait_stream();
     return;
   }
@@ -193,15 +193,14 @@ cudaEvent_t Context::take_event() {
   cuda_check(cudaEventCreate(&e), "cudaEventCreate");
   return e;
 }
-void Context::prof_enable(bool on) { prof_ = on; }
 void Context::prof_begin(int klass) {
-  if (!prof_) return;
+  if (!prof_on(klass)) return;
   open_klass_ = klass;
   open_ev_ = take_event();
   cudaEventRecord(open_ev_, stream_);
 }
 void Context::prof_end(int klass, double bytes) {
-  if (!prof_ || open_klass_ != klass) return;
+  if (!prof_on(klass) || open_klass_ != klass) return;
   cudaEvent_t b = take_event();
   cudaEventRecord(b, stream_);
   evs_.push_back(Ev{open_ev_, b, klass, bytes});

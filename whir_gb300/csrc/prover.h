@@ -104,7 +104,9 @@ class Context {
   // per-kernel-class CUDA-event timing on this stream
   // kernel classes timed with events, and K_SYNC: host time blocked in sync()
   enum Klass { K_DFT = 0, K_LEAF = 1, K_TREE = 2, K_SUMCHECK = 3, K_SYNC = 4, K_NCLASS = 5 };
-  void prof_enable(bool on);
+  void prof_enable(bool on) { prof_mask_ = on ? (1u << K_NCLASS) - 1 : 0; }
+  // time only the classes whose bit is set (fewer events on the stream)
+  void prof_enable_classes(unsigned mask) { prof_mask_ = mask & ((1u << K_NCLASS) - 1); }
   void prof_begin(int klass);
   void prof_end(int klass, double bytes);
   // drains recorded events: total ms, launches and bytes per class
@@ -125,7 +127,8 @@ class Context {
   cudaStream_t streams_[2] = {nullptr, nullptr};  // normal, high priority
   void *pinned_ = nullptr;
   size_t pinned_bytes_ = 0;
-  bool prof_ = false;
+  unsigned prof_mask_ = 0;
+  bool prof_on(int klass) const { return (prof_mask_ >> klass) & 1u; }
   struct Ev {
     cudaEvent_t a, b;
     int klass;
