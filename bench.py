@@ -401,11 +401,11 @@ def run_gb300(args):
     torch.cuda.synchronize(local)
     for klass in range(5):
         ctx.prof_read(klass)
-    # events around the DFT, leaf-hash and tree launches (five each per
-    # proof) and host clocks around the waits; the sumcheck passes, launched
-    # right after the transcript round trips, are timed in a second pass
-    # below (their 44 events per proof cost about 1% of the proof time)
-    ctx.prof_enable_classes((W.PROF_DFT, W.PROF_LEAF, W.PROF_TREE, W.PROF_SYNC))
+    # events around the leaf-hash launches (the dominant kernel, five per
+    # proof) and host clocks around the waits; the other classes are timed
+    # in a second pass below (events on every launch cost about 1% of the
+    # proof time)
+    ctx.prof_enable_classes((W.PROF_LEAF, W.PROF_SYNC))
     launches0, _, _ = ctx.counters()
     clocks.start()
     evs = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps + 1)]
@@ -423,26 +423,30 @@ def run_gb300(args):
     total_ms = evs[0].elapsed_time(evs[-1])
     lat = [evs[i].elapsed_time(evs[i + 1]) for i in range(args.steps)]
     prof = {}
-    for klass, name in ((0, "dft"), (1, "leaf_hash"), (2, "merkle_tree")):
+
+    def class_stats(klass, steps, note=None):
         ms, n, b = ctx.prof_read(klass)
-        prof[name] = {"ms_per_step": ms / args.steps, "launches_per_step": n / args.steps,
-                      "share": ms / total_ms if total_ms else None,
-                      "achieved_gbs": (b / (ms * 1e-3) / 1e9) if ms else None,
-                      "bytes_per_step": b / args.steps}
+        d = {"ms_per_step": ms / steps, "launches_per_step": n / steps,
+             "share": ms / steps / (total_ms / args.steps) if total_ms else None,
+             "achieved_gbs": (b / (ms * 1e-3) / 1e9) if ms else None,
+             "bytes_per_step": b / steps}
+        if note:
+            d["note"] = note
+        return d
+
+    prof["leaf_hash"] = class_stats(1, args.steps)
     sync_ms, sync_n, _ = ctx.prof_read(4)
-    # sumcheck passes: a shorter pass with their events on
+    # DFT, tree and sumcheck passes: a shorter pass with their events on
     sc_steps = max(3, args.steps // 3)
-    ctx.prof_enable_classes((W.PROF_SUMCHECK,))
+    ctx.prof_enable_classes((W.PROF_DFT, W.PROF_TREE, W.PROF_SUMCHECK))
     for _ in range(sc_steps):
         prove_dev()
     torch.cuda.synchronize(local)
     ctx.prof_enable(False)
-    ms, n, b = ctx.prof_read(3)
-    prof["sumcheck"] = {"ms_per_step": ms / sc_steps, "launches_per_step": n / sc_steps,
-                        "share": ms / sc_steps / (total_ms / args.steps) if total_ms else None,
-                        "achieved_gbs": (b / (ms * 1e-3) / 1e9) if ms else None,
-                        "bytes_per_step": b / sc_steps,
-                        "note": f"timed in a separate pass of {sc_steps} proofs"}
+    note = f"timed in a separate pass of {sc_steps} proofs"
+    prof["dft"] = class_stats(0, sc_steps, note)
+    prof["merkle_tree"] = class_stats(2, sc_steps, note)
+    prof["sumcheck"] = class_stats(3, sc_steps, note)
     prof["host_wait"] = {"ms_per_step": sync_ms / args.steps, "waits_per_step": sync_n / args.steps,
                          "share": sync_ms / total_ms if total_ms else None,
                          "note": "host time blocked on the stream (transcript round trips)"}
