@@ -34,7 +34,7 @@ def test_dft_batch(ctx, oracle, log_h, width, h_in):
 
 
 @pytest.mark.parametrize("log_h,row_len", [(0, 16), (1, 16), (2, 3), (3, 16), (5, 64), (7, 8),
-                                           (10, 16), (12, 64), (16, 16)])
+                                           (10, 16), (12, 64), (16, 16), (17, 16), (18, 16)])
 def test_merkle_commit_and_open(ctx, oracle, log_h, row_len):
     rows = rand(oracle, 100 + log_h, row_len << log_h)
     want = oracle.merkle_tree(rows, log_h, row_len)
