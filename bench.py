@@ -45,12 +45,12 @@ UNIT = "proofs/s"
 # Per-launch DRAM traffic (dram__bytes_read.sum + dram__bytes_write.sum) of the
 # kernel classes, from one ncu capture of a full k = 24 proof (the five
 # leaf-hash launches: 1473.0 MB per proof / 5 launches); the capture, its
-# command and the per-launch figures are in profiles/hash_rows_fixed_leaf_hash.md.
+# command and the per-launch figures are kept with the ncu summaries (profiles/).
 NCU_TRAFFIC_BYTES = {"leaf_hash": 294.6e6}
 NCU_TRAFFIC_K = 24
 # Thread instructions per width-24 permutation of the leaf hash
 # (smsp__inst_executed.sum * 32 / permutations of hash_rows_fixed<16> on a
-# k = 22 proof, profiles/hash_rows_fixed_leaf_hash.md).  With one warp
+# k = 22 proof, the ncu summary of the leaf hash in profiles/).  With one warp
 # instruction issued per cycle on each of the 4 sub-partitions of each SM,
 # the issue-bound rate is SMs * 4 * 32 * clock / this.
 LEAF_INSTR_PER_PERM24 = 8576
@@ -132,7 +132,7 @@ def integer_roofline(k, prof, clk):
             "achieved": achieved, "peak": peak, "frac": achieved / peak,
             "peak_source": f"{LEAF_INSTR_PER_PERM24} instructions per permutation (ncu) at "
                            f"{mhz:.0f} MHz, 152 SMs x 4 issue slots",
-            "note": "profiles/hash_rows_fixed_leaf_hash.md"}
+            "note": "instruction count from one ncu capture of hash_rows_fixed (profiles/)"}
 
 
 def workload_config(k):
