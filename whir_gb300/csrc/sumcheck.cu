@@ -266,6 +266,83 @@ __global__ void __launch_bounds__(CH_T, 4) compress_hi_kernel(const uint32_t *__
   publish_if_last(acc, pub);
 }
 
+// The same pass when a block is exactly 16 words per thread (W 2^s_lo =
+// 16 CH_T, the SVO shape): the next block's words and eq_hi entry are
+// loaded before this block's products (two blocks in registers, three CTAs
+// per SM), and the 64-bit sums fold every three products (2^32 = 2^32 - 2p
+// mod p keeps them below 2^58) with one reduction per block.
+constexpr uint32_t CH_FOLD = (uint32_t)((1ull << 32) % kb::P);
+__device__ __forceinline__ unsigned long long ch_fold(unsigned long long x) {
+  return (unsigned long long)(uint32_t)(x >> 32) * CH_FOLD + (uint32_t)x;  // < 2^57 + 2^32
+}
+__global__ void __launch_bounds__(CH_T, 3) compress_hi_pipe_kernel(
+    const uint32_t *__restrict__ poly, int k, int ks, const E4 *__restrict__ eq_lo, int s_lo,
+    const E4 *__restrict__ eq_hi, unsigned long long *acc, Publish pub) {
+  extern __shared__ unsigned char smraw[];
+  E4 *lo = reinterpret_cast<E4 *>(smraw);
+  unsigned long long *part = reinterpret_cast<unsigned long long *>(lo + ((size_t)1 << s_lo));
+  const int W = 1 << ks;
+  const int tid = threadIdx.x;
+  for (int i = tid; i < (1 << s_lo); i += CH_T) lo[i] = eq_lo[i];
+  for (int i = tid; i < W * 4; i += CH_T) part[i] = 0;
+  __syncthreads();
+  const uint32_t step_rows = CH_T >> ks;
+  const size_t n_hi = (size_t)1 << (k - ks - s_lo);
+  const E4 *lrow = lo + (tid >> ks);
+  E4 outer = kb::e_zero();
+  size_t hh = blockIdx.x;
+  uint32_t xa[16];
+  E4 ha = kb::e_zero();
+  if (hh < n_hi) {
+    const uint32_t *b = poly + hh * (size_t)(16 * CH_T) + tid;
+#pragma unroll
+    for (int q = 0; q < 16; q++) xa[q] = __ldcs(b + q * CH_T);
+    ha = eq_hi[hh];
+  }
+  for (; hh < n_hi; hh += gridDim.x) {
+    uint32_t xb[16];
+    E4 hb = kb::e_zero();
+    const size_t nx = hh + gridDim.x;
+    if (nx < n_hi) {
+      const uint32_t *b = poly + nx * (size_t)(16 * CH_T) + tid;
+#pragma unroll
+      for (int q = 0; q < 16; q++) xb[q] = __ldcs(b + q * CH_T);
+      hb = eq_hi[nx];
+    }
+    unsigned long long a4[4] = {0, 0, 0, 0};
+#pragma unroll
+    for (int q = 0; q < 16; q++) {
+      const E4 l = lrow[q * step_rows];
+#pragma unroll
+      for (int c = 0; c < 4; c++) a4[c] += (unsigned long long)l.c[c] * xa[q];
+      if (q % 3 == 2) {
+#pragma unroll
+        for (int c = 0; c < 4; c++) a4[c] = ch_fold(a4[c]);
+      }
+    }
+    E4 inner;
+#pragma unroll
+    for (int c = 0; c < 4; c++) inner.c[c] = kb::reduce_wide(ch_fold(a4[c]));
+    outer = kb::e_add(outer, kb::e_mul(inner, ha));
+#pragma unroll
+    for (int q = 0; q < 16; q++) xa[q] = xb[q];
+    ha = hb;
+  }
+  const int lane = tid & 31;
+  for (int off = W; off < 32; off <<= 1)
+#pragma unroll
+    for (int c = 0; c < 4; c++)
+      outer.c[c] = kb::add(outer.c[c], __shfl_xor_sync(0xffffffffu, outer.c[c], off));
+  if (W >= 32 || lane < W) {
+    const int j = tid & (W - 1);
+#pragma unroll
+    for (int c = 0; c < 4; c++) atomicAdd(part + j * 4 + c, (unsigned long long)outer.c[c]);
+  }
+  __syncthreads();
+  for (int i = tid; i < W * 4; i += CH_T) atomicAdd(acc + i, part[i]);
+  publish_if_last(acc, pub);
+}
+
 cudaError_t compress_hi(const uint32_t *poly, int k, int ks, const E4 *eq_lo, int s_lo,
                         const E4 *eq_hi, unsigned long long *acc, cudaStream_t st,
                         const Publish &pub) {
@@ -273,7 +350,12 @@ cudaError_t compress_hi(const uint32_t *poly, int k, int ks, const E4 *eq_lo, in
   size_t n_hi = (size_t)1 << (k - ks - s_lo);
   unsigned grid = (unsigned)(n_hi < 152 * 4 ? n_hi : 152 * 4);
   size_t smem = ((size_t)1 << s_lo) * sizeof(E4) + ((size_t)4 << ks) * 8;
-  compress_hi_kernel<<<grid, CH_T, smem, st>>>(poly, k, ks, eq_lo, s_lo, eq_hi, acc, pub);
+  if (((size_t)1 << (ks + s_lo)) == 16 * (size_t)CH_T) {
+    grid = (unsigned)(n_hi < 152 * 3 ? n_hi : 152 * 3);
+    compress_hi_pipe_kernel<<<grid, CH_T, smem, st>>>(poly, k, ks, eq_lo, s_lo, eq_hi, acc, pub);
+  } else {
+    compress_hi_kernel<<<grid, CH_T, smem, st>>>(poly, k, ks, eq_lo, s_lo, eq_hi, acc, pub);
+  }
   count_launches(1);
   return cudaGetLastError();
 }
