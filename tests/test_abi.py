@@ -35,3 +35,14 @@ def test_product_does_not_link_the_oracle():
     import whir_gb300 as W
     out = subprocess.run(["nm", "-D", W.lib_path()], capture_output=True, text=True).stdout
     assert " wo_" not in out and "whir_oracle" not in out
+
+
+def test_every_entry_point_has_a_ctypes_signature():
+    # a function called without argtypes passes pointers as 32-bit ints
+    import re
+    import whir_gb300 as W
+    header = open(os.path.join(ROOT, "include", "whir_gb300.h")).read()
+    declared = set(re.findall(r"WHIR_API\s+[\w\s\*]+?\b(whir_\w+)\s*\(", header))
+    # the allocation-free entry point is bound by its own test with its signature
+    missing = declared - set(W._SIGS) - {"whir_compress_hi_noalloc"}
+    assert not missing, sorted(missing)

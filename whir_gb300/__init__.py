@@ -96,6 +96,7 @@ _SIGS = {
     "whir_prove": (ctypes.c_int, [vp, vp, vp, ctypes.c_int, i32p, ctypes.c_int, i32p,
                                   ctypes.c_int, i32p]),
     "whir_prof_enable": (ctypes.c_int, [vp, ctypes.c_int]),
+    "whir_prof_enable_classes": (ctypes.c_int, [vp, ctypes.c_uint]),
     "whir_prof_read": (ctypes.c_int, [vp, ctypes.c_int, ctypes.POINTER(ctypes.c_double),
                                       ctypes.POINTER(ctypes.c_long),
                                       ctypes.POINTER(ctypes.c_double)]),
