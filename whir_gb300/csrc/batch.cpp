@@ -76,7 +76,8 @@ RunStats run_jobs(std::vector<Job> &jobs, std::vector<void *> &states, std::vect
                   size_t budget, bool honor_arrival,
                   const std::function<size_t(const Params &)> &need,
                   const std::function<void *(int worker)> &make_worker,
-                  const std::function<size_t(void *state, Job &job)> &exec) {
+                  const std::function<size_t(void *state, Job &job)> &exec,
+                  const std::function<size_t(void *state)> &prepare) {
   const int workers = (int)states.size();
   if (workers < 1 || held.size() != states.size()) throw WhirError(-1, "at least one worker");
   std::vector<double> arr(jobs.size());
@@ -103,6 +104,14 @@ RunStats run_jobs(std::vector<Job> &jobs, std::vector<void *> &states, std::vect
         }
       }
       void *state = states[w];
+      if (state && prepare) {
+        try {
+          adm.release(w, prepare(state));
+        } catch (const std::exception &e) {
+          start_err[w] = e.what();
+          state = nullptr;  // its jobs fail with the reason
+        }
+      }
       for (;;) {
         bool too_big = false;
         int j = adm.take(w, &too_big);
@@ -193,6 +202,37 @@ RunStats Server::run(std::vector<Job> &jobs, bool honor_arrival) {
     w->ctx->set_yield_wait(yield);
     return w.release();
   };
+  // Grow every worker's buffers to all shapes of this run first, in a pass
+  // of its own before the run's clock starts: a buffer that grows during
+  // the run frees its old allocation, and cudaFree synchronises every stream
+  // of the device, stalling all workers (the served stream's p99 latency
+  // rose from 20 to 150+ ms when that happened).  Only when every worker
+  // can hold the union of the shapes within the budget.
+  std::vector<Params> shapes;
+  for (auto &j : jobs) {
+    bool seen = false;
+    for (auto &q : shapes)
+      seen = seen || (q.k == j.params.k && q.folding == j.params.folding &&
+                      q.rate == j.params.rate && q.initial_reduction == j.params.initial_reduction &&
+                      q.soundness == j.params.soundness &&
+                      q.security_level == j.params.security_level);
+    if (!seen) shapes.push_back(j.params);
+  }
+  if (!shapes.empty() && workspace_union_bytes(shapes) * states_.size() <= budget_) {
+    auto prepare = [device, &shapes](void *state) -> size_t {
+      cuda_check(cudaSetDevice(device), "cudaSetDevice");
+      auto *w = static_cast<GpuWorker *>(state);
+      if (!w->prover) w->prover.reset(new Prover(w->ctx.get(), shapes[0]));
+      for (auto &p : shapes) {
+        w->prover->set_params(p);
+        w->prover->reserve();
+      }
+      cuda_check(cudaStreamSynchronize(w->ctx->stream()), "sync");
+      return w->prover->device_bytes();
+    };
+    std::vector<Job> none;
+    run_jobs(none, states_, held_, budget_, false, need, make, nullptr, prepare);
+  }
   auto exec = [device](void *state, Job &job) -> size_t {
     cuda_check(cudaSetDevice(device), "cudaSetDevice");
     auto *w = static_cast<GpuWorker *>(state);

@@ -81,11 +81,14 @@ struct RunStats {
 // state, created on first use by make_worker on its own thread).  exec(state,
 // job) does the work and returns the device bytes the worker holds
 // afterwards.  held[w] (in/out) is what worker w holds across runs.
+// prepare (optional) runs once on each worker thread before it takes jobs
+// and returns the device bytes the worker then holds.
 RunStats run_jobs(std::vector<Job> &jobs, std::vector<void *> &states, std::vector<size_t> &held,
                   size_t budget, bool honor_arrival,
                   const std::function<size_t(const Params &)> &need,
                   const std::function<void *(int worker)> &make_worker,
-                  const std::function<size_t(void *state, Job &job)> &exec);
+                  const std::function<size_t(void *state, Job &job)> &exec,
+                  const std::function<size_t(void *state)> &prepare = nullptr);
 
 // A pool of GPU workers on one device, kept between runs: each worker's
 // stream, pinned staging and prover buffers stay allocated, so a run starts

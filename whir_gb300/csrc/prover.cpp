@@ -402,6 +402,18 @@ Workspace workspace_plan(const Params &p) {
   w.acc = 8 * 4096;
   w.small = 1 << 20;
   w.gather = (size_t)4 * 4096 * (((size_t)4 << f) + 8 * 32);
+  // fold_with_code's per-query state (Impl::fold_with_code's layout) for
+  // the most STIR queries any round draws, so that no proof grows it: a
+  // cudaFree in the middle of a run synchronises every stream of the device
+  size_t nq = 0;
+  for (int r = 0; r <= n_rounds; r++) {
+    int kfd, this_rate, prev_rate;
+    round_params(p, r, &kfd, &this_rate, &prev_rate);
+    nq = std::max(nq, (size_t)n_stir_queries(p.soundness, p.security_level, prev_rate));
+  }
+  const size_t T = (size_t)1 << f;
+  w.code = 16 * nq * T + 16 * nq + 16 * ((nq + 3) & ~(size_t)3) + 4 * ((T + 3) & ~(size_t)3) +
+           4 * nq * T + 64;
   return w;
 }
 
@@ -434,9 +446,29 @@ size_t proof_bytes_max(const Params &p, int n_claims) {
   return b;
 }
 
+size_t workspace_union_bytes(const std::vector<Params> &ps) {
+  Workspace u{};
+  for (const Params &p : ps) {
+    Workspace w = workspace_plan(p);
+    u.stacked = std::max(u.stacked, w.stacked);
+    u.cw0 = std::max(u.cw0, w.cw0);
+    u.tree0 = std::max(u.tree0, w.tree0);
+    u.scratch = std::max(u.scratch, w.scratch);
+    u.cw = std::max(u.cw, w.cw);
+    u.tree = std::max(u.tree, w.tree);
+    u.sumcheck = std::max(u.sumcheck, w.sumcheck);
+    u.eqbuf = std::max(u.eqbuf, w.eqbuf);
+    u.acc = std::max(u.acc, w.acc);
+    u.small = std::max(u.small, w.small);
+    u.gather = std::max(u.gather, w.gather);
+    u.code = std::max(u.code, w.code);
+  }
+  return u.total();
+}
+
 size_t Workspace::total() const {
   return stacked + cw0 + tree0 + scratch + 2 * (cw + tree + 2 * sumcheck) + eqbuf + acc + small +
-         gather;
+         gather + code;
 }
 
 struct Prover::Impl {
@@ -601,6 +633,7 @@ struct Prover::Impl {
     acc.reserve(w.acc);
     small.reserve(w.small);
     gather.reserve(w.gather);
+    codebuf.reserve(w.code);
   }
 
   void round_params(int round, int *kfd, int *this_rate, int *prev_rate) const {
@@ -1243,6 +1276,8 @@ void Prover::set_params(const Params &p) {
   m_->p = p;
   m_->ks = p.folding;
 }
+
+void Prover::reserve() { m_->reserve(); }
 
 size_t Prover::workspace_bytes(const Params &p) {
   check_params(p);

@@ -48,10 +48,13 @@ void round_params(const Params &p, int round, int *kfd, int *this_rate, int *pre
 
 // device buffer sizes (bytes) of one prover for params p
 struct Workspace {
-  size_t stacked, cw0, tree0, scratch, cw, tree, sumcheck, eqbuf, acc, small, gather;
+  size_t stacked, cw0, tree0, scratch, cw, tree, sumcheck, eqbuf, acc, small, gather, code;
   size_t total() const;
 };
 Workspace workspace_plan(const Params &p);
+// device bytes of the buffers that serve every one of these parameter sets
+// (per buffer, the largest need)
+size_t workspace_union_bytes(const std::vector<Params> &ps);
 // upper bound of the proof bytes with n_claims claims
 size_t proof_bytes_max(const Params &p, int n_claims);
 
@@ -184,6 +187,9 @@ class Prover {
   // re-target the prover at new parameters; device buffers are kept and
   // grown on the next commit when they are too small
   void set_params(const Params &p);
+  // grow the device buffers to the current parameters' workspace now (they
+  // only grow; a proof would otherwise do it on its first use)
+  void reserve();
   // device bytes a prover holds after proving with params p
   static size_t workspace_bytes(const Params &p);
 
