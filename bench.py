@@ -91,6 +91,8 @@ def parse():
                     help="concurrent provers of the batched / served runs (0: from host cores)")
     ap.add_argument("--serve-seconds", type=float, default=2.0,
                     help="length of the served Poisson request stream")
+    ap.add_argument("--no-whir-bench-shape", action="store_true",
+                    help="skip the plain proofs at the reference's whir_bench shape")
     return ap.parse_args()
 
 
@@ -358,6 +360,52 @@ def run_batched(W, args, device):
     return out
 
 
+# The reference's own benchmark test, whir_bench (crates/whir/src/test.rs:284-290):
+# k = 25, folding 5, rate 1/2, initial_reduction 3, JohnsonBound, 123-bit, 1 claim.
+WHIR_BENCH_SHAPE = dict(k=25, folding=5, rate=1, initial_reduction=3, soundness_id=1,
+                        security_level=123, claims=1, seed=1)
+
+
+def run_whir_bench_shape(W, ctx, stream, steps=10, warmup=3):
+    """Plain proofs at whir_bench's shape, polynomial resident in HBM, timed
+    with CUDA events on the prover's stream (a secondary line: the headline
+    workload is the k = 24 one)."""
+    import torch
+    s = WHIR_BENCH_SHAPE
+    k = s["k"]
+    params = (k, s["folding"], s["rate"], s["initial_reduction"], s["soundness_id"],
+              s["security_level"])
+    whir = W.Whir(ctx, *params)
+    dev = ctx.to_device(W.random_field(s["seed"], 1 << k))
+    groups = [[0]] * s["claims"]
+
+    def one():
+        t = W.PoseidonWriter()
+        whir.prove(t, dev, [k], groups)
+        t.draw_base()
+        return t
+
+    for _ in range(warmup):
+        proof = one().finalize()
+    evs = [torch.cuda.Event(enable_timing=True) for _ in range(steps + 1)]
+    evs[0].record(stream)
+    for i in range(steps):
+        one()
+        evs[i + 1].record(stream)
+    evs[-1].synchronize()
+    lat = [evs[i].elapsed_time(evs[i + 1]) for i in range(steps)]
+    total_ms = evs[0].elapsed_time(evs[-1])
+    whir.close()
+    dev.close()
+    return {"config": {"workload": "whir_bench shape: k=25 (2^25 KoalaBear), rate 1/2, folding 5, "
+                                   "initial_reduction 3, JohnsonBound, 123-bit, 1 claim",
+                       "polynomial": "resident in HBM"},
+            "proofs_per_s": steps / (total_ms * 1e-3), "ms_per_proof": total_ms / steps,
+            "latency_ms": {"p50": float(np.percentile(lat, 50)),
+                           "p99": float(np.percentile(lat, 99))},
+            "proof_bytes": len(proof), "steps": steps, "warmup": warmup}
+
+
 def run_gb300(args):
     import torch
     import whir_gb300 as W
@@ -522,6 +570,8 @@ def run_gb300(args):
     }
     if not args.no_batched:
         line["batched_served"] = run_batched(W, args, local)
+    if not args.no_whir_bench_shape:
+        line["whir_bench_shape"] = run_whir_bench_shape(W, ctx, stream)
     if not args.no_cpu_baseline and world == 1:
         line["cpu_baseline"] = cpu_baseline(k, args.cpu_seconds, expect_proof=gpu_proof)
     print(json.dumps(line), flush=True)

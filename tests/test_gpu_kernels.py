@@ -25,7 +25,9 @@ def rand(oracle, seed, n):
     (15, 32, 1000),
     # two passes over a zero-padded input (pass 1 skips the zero stages):
     # ragged h_in, 4-column tiles, and a padding too deep for the short form
-    (18, 8, 70000), (19, 4, 40000), (14, 16, 4097), (20, 8, 4000), (17, 8, 10000)])
+    (18, 8, 70000), (19, 4, 40000), (14, 16, 4097), (20, 8, 4000), (17, 8, 10000),
+    # the row widths of foldings 5 and 6 (base 32 / 64, extension 128 / 256)
+    (16, 32, 1 << 15), (13, 128, 1 << 10), (12, 256, 1 << 9)])
 def test_dft_batch(ctx, oracle, log_h, width, h_in):
     x = rand(oracle, 7 + log_h, h_in * width)
     want = oracle.dft_batch(x, h_in, width, log_h)
@@ -34,7 +36,9 @@ def test_dft_batch(ctx, oracle, log_h, width, h_in):
 
 
 @pytest.mark.parametrize("log_h,row_len", [(0, 16), (1, 16), (2, 3), (3, 16), (5, 64), (7, 8),
-                                           (10, 16), (12, 64), (16, 16), (17, 16), (18, 16)])
+                                           (10, 16), (12, 64), (16, 16), (17, 16), (18, 16),
+                                           # foldings 5 and 6: base rows 32 / 64, extension rows 128 / 256
+                                           (9, 32), (8, 128), (6, 256), (4, 48)])
 def test_merkle_commit_and_open(ctx, oracle, log_h, row_len):
     rows = rand(oracle, 100 + log_h, row_len << log_h)
     want = oracle.merkle_tree(rows, log_h, row_len)

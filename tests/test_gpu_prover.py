@@ -5,7 +5,8 @@ The parameter sweep follows the reference's test_whir_poseidon
 (crates/whir/src/test.rs:256-282: three soundness assumptions, k = 4..12,
 folding 1..3, initial_reduction 1..folding, 1..4 claims, rate 1, 32-bit
 security) on a subset that keeps the run short, plus the benchmark shapes
-(k = 20 and k = 24, folding 4) and stacked multi-polynomial layouts.
+(k = 20 and k = 24, folding 4), foldings 5 and 6, the reference's whir_bench
+shape (k = 25, folding 5) and stacked multi-polynomial layouts.
 """
 import itertools
 
@@ -43,6 +44,24 @@ def test_whir_sweep(ctx, oracle, s, k, f, ir, n):
 def test_whir_folding4_security100(ctx, oracle, k, rate, n):
     poly = oracle.rand_fe(1, 1 << k)
     check(ctx, oracle, (k, 4, rate, 1, 1, 100), [poly], [k], [[0]] * n)
+
+
+# foldings 5 and 6: base rows of 32 / 64 words, extension rows of 128 / 256
+# words, SVO grids of 3^5 / 3^6 points, fold_with_code over 32 / 64 rows
+@pytest.mark.parametrize("params,n", [((14, 5, 1, 1, 1, 100), 2), ((16, 5, 2, 1, 1, 100), 2),
+                                      ((13, 5, 1, 3, 0, 32), 1), ((12, 5, 1, 5, 2, 32), 4),
+                                      ((15, 6, 1, 1, 1, 100), 3), ((18, 6, 2, 2, 1, 100), 1)])
+def test_whir_folding5_6(ctx, oracle, params, n):
+    k = params[0]
+    poly = oracle.rand_fe(2, 1 << k)
+    check(ctx, oracle, params, [poly], [k], [[0]] * n)
+
+
+def test_reference_bench_shape_k25(ctx, oracle):
+    # the reference's own benchmark, whir_bench (crates/whir/src/test.rs:284-290):
+    # k = 25, folding 5, rate 1/2, initial_reduction 3, JohnsonBound, 123-bit, 1 claim
+    poly = oracle.rand_fe(1, 1 << 25)
+    check(ctx, oracle, (25, 5, 1, 3, 1, 123), [poly], [25], [[0]])
 
 
 def test_stacked_layout(ctx, oracle):

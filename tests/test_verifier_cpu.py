@@ -32,6 +32,17 @@ def test_accepts_folding4_security100(oracle, k, rate, n):
     assert W.verify(params, [k], [[0]] * n, proof) == (0, cp)
 
 
+@pytest.mark.parametrize("params,n", [((14, 5, 1, 1, 1, 100), 2), ((13, 5, 1, 3, 0, 32), 1),
+                                      ((12, 5, 1, 5, 2, 32), 4), ((15, 6, 1, 1, 1, 100), 3),
+                                      # whir_bench's shape (crates/whir/src/test.rs:284-290) at k = 16
+                                      ((16, 5, 1, 3, 1, 123), 1)])
+def test_accepts_folding5_6(oracle, params, n):
+    k = params[0]
+    poly = oracle.rand_fe(4, 1 << k)
+    proof, cp = oracle.prove(params, [poly], [k], [[0]] * n)
+    assert W.verify(params, [k], [[0]] * n, proof) == (0, cp)
+
+
 def test_accepts_stacked_layout(oracle):
     ks = [8, 6, 6, 8, 5]
     polys = [oracle.rand_fe(20 + i, 1 << k) for i, k in enumerate(ks)]

@@ -36,8 +36,9 @@ cudaError_t init_poseidon2_tables() {
   return upload_p2(24);
 }
 
-// One row per thread; rows of 16 words are one permutation, rows of 64 words
-// four (PaddingFreeSponge: overwrite the 16 rate lanes, permute).
+// One row per thread; a row of ROW = 16·c words is c permutations
+// (PaddingFreeSponge: overwrite the 16 rate lanes, permute).  Base rows are
+// 2^f words and extension rows 4·2^f, so foldings 4..6 use 16..256.
 template <int ROW>
 __global__ void __launch_bounds__(128) hash_rows_fixed(const uint32_t *__restrict__ rows,
                                                        size_t n_rows,
@@ -92,9 +93,14 @@ cudaError_t hash_rows(const uint32_t *rows, size_t n_rows, int row_len, uint32_t
   unsigned grid = (unsigned)((n_rows + T - 1) / T);
   // the fixed-width kernels use 16-byte vector loads and stores
   bool aligned = (((uintptr_t)rows | (uintptr_t)digests) & 15) == 0;
-  if (aligned && row_len == 16) hash_rows_fixed<16><<<grid, T, 0, st>>>(rows, n_rows, digests);
-  else if (aligned && row_len == 64) hash_rows_fixed<64><<<grid, T, 0, st>>>(rows, n_rows, digests);
-  else hash_rows_generic<<<grid, T, 0, st>>>(rows, n_rows, row_len, digests);
+  switch (aligned ? row_len : 0) {
+    case 16: hash_rows_fixed<16><<<grid, T, 0, st>>>(rows, n_rows, digests); break;
+    case 32: hash_rows_fixed<32><<<grid, T, 0, st>>>(rows, n_rows, digests); break;
+    case 64: hash_rows_fixed<64><<<grid, T, 0, st>>>(rows, n_rows, digests); break;
+    case 128: hash_rows_fixed<128><<<grid, T, 0, st>>>(rows, n_rows, digests); break;
+    case 256: hash_rows_fixed<256><<<grid, T, 0, st>>>(rows, n_rows, digests); break;
+    default: hash_rows_generic<<<grid, T, 0, st>>>(rows, n_rows, row_len, digests);
+  }
   count_launches(1);
   return cudaGetLastError();
 }
