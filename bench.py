@@ -403,7 +403,24 @@ def run_whir_bench_shape(W, ctx, stream, steps=10, warmup=3):
             "proofs_per_s": steps / (total_ms * 1e-3), "ms_per_proof": total_ms / steps,
             "latency_ms": {"p50": float(np.percentile(lat, 50)),
                            "p99": float(np.percentile(lat, 99))},
-            "proof_bytes": len(proof), "steps": steps, "warmup": warmup}
+            "proof_bytes": len(proof), "steps": steps, "warmup": warmup}, proof
+
+
+def cpu_whir_bench_shape(expect_proof):
+    """One oracle proof at whir_bench's shape on the host cores, compared with
+    the GPU's proof bytes."""
+    from oracle import oracle as O
+    s = WHIR_BENCH_SHAPE
+    k = s["k"]
+    params = (k, s["folding"], s["rate"], s["initial_reduction"], s["soundness_id"],
+              s["security_level"])
+    poly = O.rand_fe(s["seed"], 1 << k)
+    t0 = time.perf_counter()
+    proof, _ = O.prove(params, [poly], [k], [[0]] * s["claims"])
+    el = time.perf_counter() - t0
+    return {"value": 1.0 / el, "unit": UNIT, "cores": O.lib().wo_threads(), "kind": "port",
+            "sample": f"1 full proof in {el:.1f} s (oracle/: C restatement, OpenMP)",
+            "gpu_proof_identical": bool(proof == expect_proof)}
 
 
 def run_gb300(args):
@@ -571,7 +588,9 @@ def run_gb300(args):
     if not args.no_batched:
         line["batched_served"] = run_batched(W, args, local)
     if not args.no_whir_bench_shape:
-        line["whir_bench_shape"] = run_whir_bench_shape(W, ctx, stream)
+        line["whir_bench_shape"], wb_proof = run_whir_bench_shape(W, ctx, stream)
+        if not args.no_cpu_baseline and world == 1:
+            line["whir_bench_shape"]["cpu_baseline"] = cpu_whir_bench_shape(wb_proof)
     if not args.no_cpu_baseline and world == 1:
         line["cpu_baseline"] = cpu_baseline(k, args.cpu_seconds, expect_proof=gpu_proof)
     print(json.dumps(line), flush=True)
