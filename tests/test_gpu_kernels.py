@@ -27,7 +27,10 @@ def rand(oracle, seed, n):
     # ragged h_in, 4-column tiles, and a padding too deep for the short form
     (18, 8, 70000), (19, 4, 40000), (14, 16, 4097), (20, 8, 4000), (17, 8, 10000),
     # the row widths of foldings 5 and 6 (base 32 / 64, extension 128 / 256)
-    (16, 32, 1 << 15), (13, 128, 1 << 10), (12, 256, 1 << 9)])
+    (16, 32, 1 << 15), (13, 128, 1 << 10), (12, 256, 1 << 9),
+    # 2^12-point coset transforms on 4-column tiles (the extension round two
+    # of the k = 24 proof is (20, 64, 4096))
+    (20, 64, 4096), (14, 16, 4096), (18, 8, 2049), (13, 4, 3000)])
 def test_dft_batch(ctx, oracle, log_h, width, h_in):
     x = rand(oracle, 7 + log_h, h_in * width)
     want = oracle.dft_batch(x, h_in, width, log_h)

@@ -46,6 +46,9 @@ DftTune dft_tune(int log_h, size_t width);
 void set_dft_tune(int log_h, size_t width, DftTune t);
 bool tree_tune_valid(int log_h, TreeTune t);
 bool dft_tune_valid(int log_h, DftTune t);
+// true when dft_batch runs one pass of coset transforms for this shape
+// (16-byte aligned buffers), so the two-pass split does not apply
+bool dft_coset_one_pass(int log_h, size_t h_in, size_t width);
 
 // ---- kernel launches issued by this library (all contexts), for reporting ----
 unsigned long long launch_count();

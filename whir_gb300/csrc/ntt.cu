@@ -606,6 +606,17 @@ static cudaError_t tile_any(const uint32_t *in, uint32_t *out, int S, size_t wid
                         pre_log, tw_log, st);
 }
 
+static int ceil_log2(size_t x) {
+  int l = 0;
+  while (((size_t)1 << l) < x) l++;
+  return l;
+}
+bool dft_coset_one_pass(int log_h, size_t h_in, size_t width) {
+  if (log_h <= 11) return false;
+  const int L0 = ceil_log2(h_in);
+  return log_h - L0 <= 15 && (L0 <= 11 || (L0 == 12 && width % 4 == 0));
+}
+
 // per-size overrides of the two-pass split (0: default), by log_h and width class
 static std::atomic<int> g_dft_tune[25][2];
 static int width_class(size_t width) { return width > 16 ? 1 : 0; }
@@ -634,14 +645,20 @@ cudaError_t dft_batch(const uint32_t *in, size_t h_in, size_t width, int log_h, 
   if (width >= (1u << 16) || (h * width) >= ((size_t)1 << 32)) return cudaErrorInvalidValue;
   if (log_h <= 11)
     return tile_any(in, out, log_h, width, h_in, 1, 0, 1, 0, 1, 0, 0, st);
-  int L0 = 0;
-  while (((size_t)1 << L0) < h_in) L0++;
+  const int L0 = ceil_log2(h_in);
   if (L0 <= 11 && log_h - L0 <= 15) {
     // coset form: with N0 = 2^L0 >= h_in and M1 = 2^(log_h - L0),
     // out[k1 + M1 k2] = sum_{n < N0} (x[n] w^(n k1)) w_{N0}^(n k2): M1 transforms
     // of size N0 of the pre-twiddled input, one pass, no scratch
     size_t M1 = h >> L0;
     return tile_any(in, out, L0, width, h_in, M1, 0, 1, 1, M1, log_h, 0, st);
+  }
+  if (L0 == 12 && log_h - L0 <= 15 && width % 4 == 0 &&
+      (((uintptr_t)in | (uintptr_t)out) & 15) == 0) {
+    // the same coset form on 2^12-row tiles of 4 columns (64 KB of shared
+    // memory, three CTAs per SM; 8 columns would leave one)
+    size_t M1 = h >> L0;
+    return launch_tile_v<4>(in, out, L0, width, h_in, M1, 0, 1, 1, M1, log_h, 0, st);
   }
   DftTune tune = dft_tune(log_h, width);
   if (!dft_tune_valid(log_h, tune)) tune = DftTune();

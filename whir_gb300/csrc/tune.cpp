@@ -83,9 +83,7 @@ std::string autotune(Context &ctx, int lo, int hi) {
         size_t words = width << h;
         if (words > max_words) break;
         size_t h_in = (size_t)1 << std::max(0, h - ratio);
-        int L0 = 0;
-        while (((size_t)1 << L0) < h_in) L0++;
-        if (L0 <= 11 && h - L0 <= 15) continue;  // one coset pass: nothing to choose
+        if (gpu::dft_coset_one_pass(h, h_in, width)) continue;  // nothing to choose
         DeviceBuffer in, out, scr;
         in.reserve(4 * h_in * width);
         out.reserve(4 * words);
