@@ -92,7 +92,7 @@ def parse():
     ap.add_argument("--serve-seconds", type=float, default=2.0,
                     help="length of the served Poisson request stream")
     ap.add_argument("--no-whir-bench-shape", action="store_true",
-                    help="skip the plain proofs at the reference's whir_bench shape")
+                    help="skip the reference's benchmark shapes (whir_bench, Merkle benches)")
     return ap.parse_args()
 
 
@@ -423,6 +423,43 @@ def cpu_whir_bench_shape(expect_proof):
             "gpu_proof_identical": bool(proof == expect_proof)}
 
 
+# The reference's Merkle benchmarks (crates/merkle/src/lib.rs:314-349, 384-420):
+# commit and one query of 2^21 rows of 32 base elements, and of 2^18 rows of 32
+# extension elements (128 words).
+MERKLE_BENCH_SHAPES = [("bench_merkle_base_packed", 21, 32), ("bench_merkle_ext_packed", 18, 128)]
+
+
+def run_merkle_bench_shapes(W, ctx, steps=10, warmup=3):
+    """Commit + one opening through the public ABI (whir_merkle_commit, which
+    reserves the tree, hashes the rows, builds the levels and reads the root
+    back, then whir_merkle_open), rows resident in HBM, host clock per call."""
+    out = {}
+    for name, k, row_len in MERKLE_BENCH_SHAPES:
+        rows = ctx.to_device(W.random_field(0, row_len << k))
+
+        def one():
+            t = W.MerkleTree(ctx, rows, k, row_len)
+            t.open([(5 << k) // 7])
+            t.close()
+
+        for _ in range(warmup):
+            one()
+        lat = []
+        for _ in range(steps):
+            t0 = time.perf_counter()
+            one()
+            lat.append(time.perf_counter() - t0)
+        rows.close()
+        ms = 1e3 * float(np.mean(lat))
+        perm24 = (row_len // 16) << k
+        perm16 = (1 << k) - 1
+        out[name] = {"rows": 1 << k, "row_words": row_len, "ms_per_commit_and_query": ms,
+                     "p50_ms": 1e3 * float(np.percentile(lat, 50)),
+                     "leaf_perm24_per_s": perm24 / (ms * 1e-3),
+                     "tree_perm16": perm16, "steps": steps, "warmup": warmup}
+    return out
+
+
 def run_gb300(args):
     import torch
     import whir_gb300 as W
@@ -589,6 +626,7 @@ def run_gb300(args):
         line["batched_served"] = run_batched(W, args, local)
     if not args.no_whir_bench_shape:
         line["whir_bench_shape"], wb_proof = run_whir_bench_shape(W, ctx, stream)
+        line["merkle_bench_shapes"] = run_merkle_bench_shapes(W, ctx)
         if not args.no_cpu_baseline and world == 1:
             line["whir_bench_shape"]["cpu_baseline"] = cpu_whir_bench_shape(wb_proof)
     if not args.no_cpu_baseline and world == 1:

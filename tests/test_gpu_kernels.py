@@ -64,6 +64,21 @@ def test_merkle_commit_and_open(ctx, oracle, log_h, row_len):
     t.close()
 
 
+@pytest.mark.parametrize("log_h,row_len", [(21, 32), (18, 128)])
+def test_merkle_reference_bench_shapes(ctx, oracle, log_h, row_len):
+    # bench_merkle_base_packed (2^21 rows of 32 base elements) and
+    # bench_merkle_ext_packed (2^18 rows of 32 extension elements = 128 words),
+    # crates/merkle/src/lib.rs:314-349 and :384-420: every level and one opening
+    rows = oracle.rand_fe(0, row_len << log_h)
+    want = oracle.merkle_tree(rows, log_h, row_len)
+    t = W.MerkleTree(ctx, ctx.to_device(rows), log_h, row_len)
+    assert np.array_equal(t.levels(), want)
+    i = (5 << log_h) // 7
+    op = t.open([i])
+    assert np.array_equal(op[0, :row_len], rows[i * row_len:(i + 1) * row_len])
+    t.close()
+
+
 @pytest.mark.parametrize("k", [0, 1, 5, 12, 20])
 def test_eq_table(ctx, oracle, k):
     pt = rand(oracle, 3, 4 * k)

@@ -6,6 +6,8 @@
 
 #include <algorithm>
 #include <chrono>
+#include <memory>
+#include <mutex>
 #include <thread>
 
 #include <new>
@@ -28,6 +30,10 @@ using kb::E4;
 struct whir_ctx {
   Context ctx;
   DeviceBuffer scratch, eq, acc, small;
+  // the node buffer of the last freed tree, reused by the next commit (a
+  // fresh reservation and its release cost ~0.3 ms at 2^21 leaves)
+  std::unique_ptr<DeviceBuffer> spare_nodes;
+  std::mutex spare_mu;
   explicit whir_ctx(int dev) : ctx(dev) {}
 };
 struct whir_transcript {
@@ -40,7 +46,7 @@ struct whir_prover {
 };
 struct whir_tree {
   whir_ctx *ctx;
-  DeviceBuffer nodes;
+  std::unique_ptr<DeviceBuffer> nodes;
   whir::DeviceTree t;
 };
 
@@ -176,19 +182,24 @@ int whir_merkle_commit(whir_ctx *ctx, const uint32_t *rows, int log_h, size_t ro
   whir_tree *t = new whir_tree();
   t->ctx = ctx;
   try {
-    t->nodes.reserve(4 * whir::gpu::tree_words(log_h));
+    {
+      std::lock_guard<std::mutex> lock(ctx->spare_mu);
+      t->nodes = std::move(ctx->spare_nodes);
+    }
+    if (!t->nodes) t->nodes.reset(new DeviceBuffer());
+    t->nodes->reserve(4 * whir::gpu::tree_words(log_h));
     cudaStream_t st = ctx->ctx.stream();
     size_t n = (size_t)1 << log_h;
-    whir::cuda_check(whir::gpu::hash_rows(rows, n, (int)row_len, t->nodes.as<uint32_t>(), st),
+    whir::cuda_check(whir::gpu::hash_rows(rows, n, (int)row_len, t->nodes->as<uint32_t>(), st),
                      "hash_rows");
-    whir::cuda_check(whir::gpu::build_tree(t->nodes.as<uint32_t>(), log_h, st), "build_tree");
+    whir::cuda_check(whir::gpu::build_tree(t->nodes->as<uint32_t>(), log_h, st), "build_tree");
     uint32_t h[8];
-    whir::cuda_check(cudaMemcpyAsync(h, t->nodes.as<uint32_t>() + whir::gpu::tree_words(log_h) - 8,
+    whir::cuda_check(cudaMemcpyAsync(h, t->nodes->as<uint32_t>() + whir::gpu::tree_words(log_h) - 8,
                                      32, cudaMemcpyDeviceToHost, st),
                      "d2h");
     ctx->ctx.sync();
     t->t.rows = rows;
-    t->t.nodes = t->nodes.as<uint32_t>();
+    t->t.nodes = t->nodes->as<uint32_t>();
     t->t.log_h = log_h;
     t->t.row_len = (int)row_len;
     memcpy(t->t.root, h, 32);
@@ -235,7 +246,13 @@ int whir_merkle_open(whir_tree *tree, const size_t *idx, size_t n, uint32_t *out
 }
 int whir_merkle_free(whir_tree *tree) {
   API_BEGIN
-  if (tree) tree->ctx->ctx.sync();
+  if (tree) {
+    whir_ctx *c = tree->ctx;
+    c->ctx.sync();
+    std::lock_guard<std::mutex> lock(c->spare_mu);
+    if (tree->nodes && (!c->spare_nodes || c->spare_nodes->bytes() < tree->nodes->bytes()))
+      c->spare_nodes = std::move(tree->nodes);
+  }
   delete tree;
   API_END
 }
