@@ -6,6 +6,8 @@ crates/merkle/src/lib.rs tests) and compares the CUDA result with the CPU
 restatement on seeded inputs.  Field arithmetic is exact, so the tolerance is
 zero.
 """
+import ctypes
+
 import numpy as np
 import pytest
 
@@ -196,3 +198,30 @@ def test_unaligned_extension_arrays(ctx, oracle, k):
     rs = rand(oracle, 39, 4 * 4)
     got = W.compress_lo(ctx, Shifted(ctx, base), k, rs, 4).download(4 << (k - 4))
     assert np.array_equal(got, oracle.compress_lo(base, k, rs, 4))
+
+
+def test_abi_errors_leave_the_context_usable(ctx, oracle):
+    # bad shapes and parameters are refused with WHIR_ERR_ARG before any
+    # launch, and the context keeps working afterwards
+    L = W.lib()
+    x = rand(oracle, 3, 64 * 16)
+    dev = ctx.to_device(x)
+    out = ctx.alloc(4 * (16 << 8))
+    assert L.whir_dft_batch(ctx.h, dev.ptr, 64, 16, 25, out.ptr) == -1  # beyond two-adicity
+    assert b"log_h" in L.whir_last_error()
+    assert L.whir_dft_batch(ctx.h, dev.ptr, 64, 0, 8, out.ptr) == -1     # no columns
+    assert L.whir_dft_batch(ctx.h, dev.ptr, 512, 16, 8, out.ptr) == -1   # input taller than the code
+    h, root = W.vp(), np.zeros(8, np.uint32)
+    assert L.whir_merkle_commit(ctx.h, dev.ptr, 6, 0, ctypes.byref(h),
+                                root.ctypes.data_as(W.u32p)) == -1         # empty rows
+    t = W.MerkleTree(ctx, dev, 6, 16)
+    with pytest.raises(W.WhirError):
+        t.open([64])                                                     # past the last leaf
+    with pytest.raises(W.WhirError):
+        W.Whir(ctx, 12, 9, 1, 1, 1, 100)                                 # folding above 8
+    with pytest.raises(W.WhirError):
+        W.Whir(ctx, 3, 4, 1, 1, 1, 100)                                  # k below the folding
+    got = W.dft_batch(ctx, dev, 64, 16, 8).download(16 << 8)
+    assert np.array_equal(got, oracle.dft_batch(x, 64, 16, 8))
+    assert np.array_equal(t.levels(), oracle.merkle_tree(x, 6, 16))
+    t.close()
