@@ -64,6 +64,23 @@ def test_batch_matches_oracle(oracle):
         assert j.proof == want and j.checkpoint == wcp
 
 
+def test_batch_mixed_parameters(oracle):
+    # jobs of different foldings (1..6), initial reductions, soundness modes
+    # and security levels share the pool's provers, whose buffers are grown
+    # to the union of the shapes before the run
+    shapes = [(12, 5, 1, 3, 1, 100), (11, 3, 2, 2, 0, 32), (13, 6, 1, 1, 2, 64),
+              (10, 1, 1, 1, 1, 32), (14, 4, 2, 1, 1, 100), (12, 2, 3, 2, 2, 80)]
+    jobs = [W.Job(p, oracle.rand_fe(50 + i, 1 << p[0]), claims=1 + i % 3)
+            for i, p in enumerate(shapes * 2)]
+    W.prove_jobs(jobs, workers=3)
+    for j in jobs:
+        p = j.params
+        params = (p.k, p.folding, p.rate, p.initial_reduction, p.soundness, p.security_level)
+        want, wcp = oracle.prove(params, [j.poly], [p.k], [[0]] * j.claims)
+        assert j.status == 0
+        assert j.proof == want and j.checkpoint == wcp
+
+
 def test_served_stream_same_as_batch(oracle):
     a = mixed_jobs(oracle, 3, 16, arrival_gap=0.004)
     b = mixed_jobs(oracle, 3, 16)

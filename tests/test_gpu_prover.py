@@ -73,6 +73,15 @@ def test_stacked_layout(ctx, oracle):
     check(ctx, oracle, (k, 3, 1, 1, 1, 32), polys, ks, groups)
 
 
+@pytest.mark.parametrize("f,ir,s,sec", [(5, 2, 1, 100), (6, 1, 0, 32)])
+def test_stacked_layout_folding5_6(ctx, oracle, f, ir, s, sec):
+    ks = [10, 8, 10, 7, 8]
+    polys = [oracle.rand_fe(30 + i, 1 << k) for i, k in enumerate(ks)]
+    k = int(np.ceil(np.log2(sum(1 << x for x in ks))))
+    groups = [[0, 2], [1, 4], [3], [2]]
+    check(ctx, oracle, (k, f, 1, ir, s, sec), polys, ks, groups)
+
+
 def test_proof_is_deterministic_across_calls(ctx, oracle):
     poly = oracle.rand_fe(5, 1 << 12)
     w = W.Whir(ctx, 12, 4, 1, 1, 1, 100)
