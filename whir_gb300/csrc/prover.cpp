@@ -683,11 +683,14 @@ struct Prover::Impl {
   // grid point u in {0,1,2}^r x {0 or 2}: acc += eq(u, svo[..r+1]) * <w pe_r, eq_u>.
   // The eq tables eq_u have base-field entries and do not depend on the claim
   // (Svo::new, svo.rs:158-222), so they are built once per prover (svo_eq).
+  // Table r depends on r alone: a prover reused with a larger folding
+  // (set_params) only adds the missing rounds.
   void build_svo_tables() {
-    if (!svo_eq.empty()) return;
+    const int have = (int)svo_eq.size();
+    if (have >= ks) return;
     svo_eq.resize(ks);
     const uint32_t vals[3][2] = {{ONE, 0}, {0, ONE}, {neg(ONE), dbl(ONE)}};  // (1-u, u)
-    for (int r = 0; r < ks; r++) {
+    for (int r = have; r < ks; r++) {
       int l = r + 1;
       size_t n = ipow3(r), na = (size_t)1 << l;
       std::vector<uint32_t> &tab = svo_eq[r];
