@@ -131,3 +131,31 @@ def test_server_reuse_across_runs(oracle):
             assert x.proof == y.proof and x.checkpoint == y.checkpoint
     finally:
         srv.close()
+
+
+def test_server_reuse_with_growing_folding(ctx, oracle):
+    # one pool, three runs whose foldings grow (2, then 6, then 5) and mix
+    # commit-only jobs in: every proof equals the oracle's (full proofs) or
+    # the plain prover's (commitments)
+    srv = W.Server(workers=2)
+    try:
+        runs = [[(11, 2, 1, 1, 1, 100), (10, 2, 2, 2, 0, 32)],
+                [(13, 6, 1, 1, 1, 100), (12, 6, 1, 3, 2, 64)],
+                [(12, 5, 2, 1, 1, 100), (11, 5, 1, 5, 0, 32)]]
+        for r, shapes in enumerate(runs):
+            jobs = [W.Job(p, oracle.rand_fe(70 + 10 * r + i, 1 << p[0]), claims=1 + i % 2,
+                          commit_only=(i == 2))
+                    for i, p in enumerate(shapes + shapes[:1])]
+            srv.run(jobs)
+            for j in jobs:
+                assert j.status == 0
+                if j.commit_only:
+                    proof, cp = alone(ctx, j)
+                else:
+                    p = j.params
+                    params = (p.k, p.folding, p.rate, p.initial_reduction, p.soundness,
+                              p.security_level)
+                    proof, cp = oracle.prove(params, [j.poly], [p.k], [[0]] * j.claims)
+                assert j.proof == proof and j.checkpoint == cp
+    finally:
+        srv.close()
