@@ -82,6 +82,56 @@ def test_stacked_layout_folding5_6(ctx, oracle, f, ir, s, sec):
     check(ctx, oracle, (k, f, 1, ir, s, sec), polys, ks, groups)
 
 
+def test_one_prover_across_layouts(ctx, oracle):
+    # one Whir object proves different stacks in turn (polynomial counts,
+    # sizes and claim groups change between proofs); each proof equals the
+    # oracle's
+    params = (10, 3, 1, 1, 1, 32)
+    w = W.Whir(ctx, *params)
+    for ks, groups in [([8, 6, 6, 8, 5], [[0, 3], [1, 2], [4], [3]]), ([10], [[0], [0]]),
+                       ([9, 9], [[0, 1]]), ([8, 6, 6, 8, 5], [[4], [0]])]:
+        polys = [oracle.rand_fe(40 + i, 1 << k) for i, k in enumerate(ks)]
+        proof, cp = W.prove_harness(ctx, None, polys, ks, groups, whir=w)
+        want, wcp = oracle.prove(params, polys, ks, groups)
+        assert proof == want and cp == wcp
+    w.close()
+
+
+def _emul(a, b):
+    # Ext4 product of Montgomery words (x^4 = 3), for expanding points in Python
+    rinv = pow(2 ** 32, -1, W.P)
+    c = [0] * 4
+    for i in range(4):
+        for j in range(4):
+            t = a[i] * b[j] * rinv % W.P
+            c[(i + j) % 4] += t if i + j < 4 else 3 * t
+    return [x % W.P for x in c]
+
+
+def test_fine_grained_calls_match_whir_prove(ctx, oracle):
+    # whir_commit, then for each claim a transcript-drawn point expanded as
+    # the harness does (Point::expand: z_i = x^(2^i), crates/whir/src/test.rs:225-228)
+    # through whir_stack_eval, then whir_open: the bytes of whir_prove
+    k = 12
+    params = (k, 4, 1, 1, 1, 100)
+    poly = oracle.rand_fe(77, 1 << k)
+    want, wcp = W.prove_harness(ctx, params, [poly], [k], [[0], [0]])
+    w = W.Whir(ctx, *params)
+    t = W.PoseidonWriter()
+    w.commit(t, [poly], [k])
+    for _ in range(2):
+        x = [int(v) for v in t.draw()]
+        pt = []
+        for _ in range(k):
+            pt.append(x)
+            x = _emul(x, x)
+        w.stack_eval(t, 0, np.array(pt, np.uint32).ravel())
+    w.open(t)
+    cp = t.draw_base()
+    assert t.finalize() == want and cp == wcp
+    w.close()
+
+
 def test_proof_is_deterministic_across_calls(ctx, oracle):
     poly = oracle.rand_fe(5, 1 << 12)
     w = W.Whir(ctx, 12, 4, 1, 1, 1, 100)
