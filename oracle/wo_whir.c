@@ -34,9 +34,16 @@ static double log_1_delta(int s, int lir) {
   else delta = 1. - rate - eta;
   return log2(1. - delta);
 }
+/* params.rs:118-122 converts with Rust's `as usize`, which saturates: NaN
+ * and negative values (rate 1, log_inv_rate 0, where log(1 - delta) is 0 or
+ * positive) give 0 queries.  Counts past MAX_STIR (the size of the index
+ * arrays here) are reported as -1. */
+#define MAX_STIR 4096
 int wo_n_stir_queries(int s, int security, int lir) {
-  double q = -(double)security / log_1_delta(s, lir);
-  return (int)ceil(q);
+  double q = ceil(-(double)security / log_1_delta(s, lir));
+  if (!(q > 0.)) return 0;
+  if (q > (double)MAX_STIR) return -1;
+  return (int)q;
 }
 static double ood_error(int s, int log_degree, int lir, int field_bits, int samples) {
   if (s == 0) return 0.;
@@ -585,6 +592,18 @@ static int whir_open(const wo_params *p, wo_ts *ts, commitment *c0, prover_layou
   return ok;
 }
 
+/* every round's and the final STIR query count is within MAX_STIR */
+static int stir_counts_ok(const wo_params *p) {
+  int n_rounds, final_rounds;
+  wo_number_of_rounds(p->folding, p->k, &n_rounds, &final_rounds);
+  for (int round = 0; round <= n_rounds; round++) {
+    int kfd, this_rate, prev_rate;
+    round_params(p, round, &kfd, &this_rate, &prev_rate);
+    if (wo_n_stir_queries(p->soundness, p->security_level, prev_rate) < 0) return 0;
+  }
+  return 1;
+}
+
 static int group_offset(const wo_claims *cl, int g) {
   int o = 0;
   for (int i = 0; i < g; i++) o += cl->group_n[i];
@@ -593,6 +612,7 @@ static int group_offset(const wo_claims *cl, int g) {
 
 int wo_prove(const wo_params *prm, const wo_claims *cl, const uint32_t *polys, uint8_t *proof,
              size_t cap, size_t *len, uint32_t *checkpoint) {
+  if (!stir_counts_ok(prm)) return -1;
   wo_ts ts;
   ts_writer(&ts, proof, cap);
   prover_layout L;
@@ -680,6 +700,7 @@ static int reduce_round(wo_ts *ts, ext *sum, ext *r) {
 
 int wo_verify(const wo_params *p, const wo_claims *cl, const uint8_t *proof, size_t len,
               uint32_t *checkpoint) {
+  if (!stir_counts_ok(p)) return -1;
   wo_ts ts;
   ts_reader(&ts, proof, len);
   int rc = 0;

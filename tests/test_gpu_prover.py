@@ -57,6 +57,16 @@ def test_whir_folding5_6(ctx, oracle, params, n):
     check(ctx, oracle, params, [poly], [k], [[0]] * n)
 
 
+@pytest.mark.parametrize("params", [(6, 1, 0, 1, 1, 32), (9, 3, 0, 2, 2, 64),
+                                    (12, 4, 0, 1, 1, 100), (14, 5, 0, 1, 0, 100)])
+def test_rate_one(ctx, oracle, params):
+    # log_inv_rate 0: no STIR queries in any round (Rust's saturating cast of
+    # the query count, params.rs:118-122); nothing is opened or gathered
+    k = params[0]
+    poly = oracle.rand_fe(8, 1 << k)
+    check(ctx, oracle, params, [poly], [k], [[0]] * 2)
+
+
 def test_reference_bench_shape_k25(ctx, oracle):
     # the reference's own benchmark, whir_bench (crates/whir/src/test.rs:284-290):
     # k = 25, folding 5, rate 1/2, initial_reduction 3, JohnsonBound, 123-bit, 1 claim

@@ -43,6 +43,25 @@ def test_accepts_folding5_6(oracle, params, n):
     assert W.verify(params, [k], [[0]] * n, proof) == (0, cp)
 
 
+@pytest.mark.parametrize("params", [(6, 1, 0, 1, 1, 32), (8, 2, 0, 1, 0, 32), (9, 3, 0, 2, 2, 64),
+                                    (12, 4, 0, 1, 1, 100)])
+def test_rate_one_has_no_queries(oracle, params):
+    # log_inv_rate 0: params.rs:118-122 casts a negative or -inf query count
+    # with Rust's saturating `as usize`, so every round has 0 STIR queries
+    k = params[0]
+    poly = oracle.rand_fe(6, 1 << k)
+    proof, cp = oracle.prove(params, [poly], [k], [[0]] * 2)
+    assert W.verify(params, [k], [[0]] * 2, proof) == (0, cp)
+
+
+def test_query_count_out_of_range_is_refused(oracle):
+    params = (10, 2, 1, 1, 0, 100000)  # unique decoding, 100000-bit: ~10^5 queries
+    with pytest.raises(W.WhirError):
+        W.workspace_bytes(params)
+    with pytest.raises(RuntimeError):
+        oracle.prove(params, [oracle.rand_fe(1, 1 << 10)], [10], [[0]])
+
+
 def test_accepts_stacked_layout(oracle):
     ks = [8, 6, 6, 8, 5]
     polys = [oracle.rand_fe(20 + i, 1 << k) for i, k in enumerate(ks)]

@@ -36,8 +36,14 @@ static double log_1_delta(int s, int lir) {
   double delta = s == 0 ? 0.5 * (1. - rate) : s == 1 ? 1. - sqrt(rate) - eta : 1. - rate - eta;
   return log2(1. - delta);
 }
+// params.rs:118-122 converts with Rust's `as usize`, which saturates: NaN
+// and negative values (rate 1, log_inv_rate 0, where log(1 - delta) is 0 or
+// positive) give 0 queries.  Counts that no codeword could serve are refused.
 int n_stir_queries(int s, int security, int lir) {
-  return (int)ceil(-(double)security / log_1_delta(s, lir));
+  const double q = ceil(-(double)security / log_1_delta(s, lir));
+  if (!(q > 0.)) return 0;
+  if (q > (double)(1 << 16)) throw WhirError(-1, "STIR query count out of range");
+  return (int)q;
 }
 int n_ood_queries(int s, int security, int log_degree, int lir, int field_bits) {
   if (s == 0) return 0;
@@ -556,6 +562,7 @@ struct Prover::Impl {
   }
   // copy host bytes to `dst` (device) through the argument space
   void upload(void *dst, const void *src, size_t bytes) {
+    if (bytes == 0) return;
     uint8_t *h = args_alloc(bytes);
     memcpy(h, src, bytes);
     cuda_check(copy_async(*ctx, dst, h, bytes, cudaMemcpyHostToDevice), "h2d");
@@ -808,7 +815,9 @@ struct Prover::Impl {
                     E4 code_r = E4{}) {
     unsigned long long *a = acc.as<unsigned long long>();
     // the last reducing launch publishes the sums to pinned memory and
-    // re-zeroes them (no memset, no copy)
+    // re-zeroes them (no memset, no copy); with no queries (rate 1) there is
+    // no code pass and the round pass publishes
+    if (code && code->n == 0) code = nullptr;
     gpu::Publish pub = publish(12);
     gpu::Publish none;
     size_t n = (size_t)1 << kc;
