@@ -592,13 +592,19 @@ static int whir_open(const wo_params *p, wo_ts *ts, commitment *c0, prover_layou
   return ok;
 }
 
-/* every round's and the final STIR query count is within MAX_STIR */
+/* Parameter sets the reference can run: its round shapes are usize
+ * arithmetic (params.rs:190-203, whir.rs:150-166) that panics when a result
+ * would be negative; and every round's and the final STIR query count is
+ * within MAX_STIR. */
 static int stir_counts_ok(const wo_params *p) {
+  if (p->folding < 1 || p->k < p->folding) return 0;
   int n_rounds, final_rounds;
   wo_number_of_rounds(p->folding, p->k, &n_rounds, &final_rounds);
+  if (final_rounds < 0) return 0;
   for (int round = 0; round <= n_rounds; round++) {
     int kfd, this_rate, prev_rate;
     round_params(p, round, &kfd, &this_rate, &prev_rate);
+    if (kfd < 0 || this_rate < 0 || prev_rate < 0) return 0;
     if (wo_n_stir_queries(p->soundness, p->security_level, prev_rate) < 0) return 0;
   }
   return 1;
@@ -612,7 +618,7 @@ static int group_offset(const wo_claims *cl, int g) {
 
 int wo_prove(const wo_params *prm, const wo_claims *cl, const uint32_t *polys, uint8_t *proof,
              size_t cap, size_t *len, uint32_t *checkpoint) {
-  if (!stir_counts_ok(prm)) return -1;
+  if (!stir_counts_ok(prm)) return -1;  /* parameters the reference cannot run */
   wo_ts ts;
   ts_writer(&ts, proof, cap);
   prover_layout L;

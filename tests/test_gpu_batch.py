@@ -159,3 +159,15 @@ def test_server_reuse_with_growing_folding(ctx, oracle):
                 assert j.proof == proof and j.checkpoint == cp
     finally:
         srv.close()
+
+
+def test_run_with_parameters_the_reference_cannot_run_is_refused(oracle):
+    # initial_reduction 5 > rate + folding: the whole run is refused before
+    # any job starts, and the pool still works afterwards
+    good = W.Job((10, 2, 1, 1, 1, 32), oracle.rand_fe(1, 1 << 10))
+    bad = W.Job((10, 2, 1, 5, 1, 32), oracle.rand_fe(2, 1 << 10))
+    with pytest.raises(W.WhirError):
+        W.prove_jobs([good, bad], workers=2)
+    W.prove_jobs([good], workers=2)
+    want, wcp = oracle.prove((10, 2, 1, 1, 1, 32), [good.poly], [10], [[0]])
+    assert good.status == 0 and good.proof == want and good.checkpoint == wcp

@@ -221,6 +221,8 @@ def test_abi_errors_leave_the_context_usable(ctx, oracle):
         W.Whir(ctx, 12, 9, 1, 1, 1, 100)                                 # folding above 8
     with pytest.raises(W.WhirError):
         W.Whir(ctx, 3, 4, 1, 1, 1, 100)                                  # k below the folding
+    with pytest.raises(W.WhirError):
+        W.Whir(ctx, 10, 2, 1, 5, 1, 32)                                  # a negative round rate
     got = W.dft_batch(ctx, dev, 64, 16, 8).download(16 << 8)
     assert np.array_equal(got, oracle.dft_batch(x, 64, 16, 8))
     assert np.array_equal(t.levels(), oracle.merkle_tree(x, 6, 16))

@@ -62,6 +62,27 @@ def test_query_count_out_of_range_is_refused(oracle):
         oracle.prove(params, [oracle.rand_fe(1, 1 << 10)], [10], [[0]])
 
 
+@pytest.mark.parametrize("params", [(10, 2, 1, 5, 1, 32), (8, 1, 1, 3, 0, 32), (7, 8, 1, 1, 1, 32)])
+def test_parameters_the_reference_cannot_run_are_refused(oracle, params):
+    # round shapes that go negative in the reference's usize arithmetic
+    # (whir.rs:150-166, params.rs:190-203) panic there; here they are refused
+    k = params[0]
+    with pytest.raises(W.WhirError):
+        W.workspace_bytes(params)
+    with pytest.raises(W.WhirError):
+        W.verify(params, [k], [[0]], b"\0" * 64)
+    with pytest.raises(RuntimeError):
+        oracle.prove(params, [oracle.rand_fe(1, 1 << k)], [k], [[0]])
+
+
+def test_reduction_up_to_rate_plus_folding_is_accepted(oracle):
+    # initial_reduction 4 > folding 3 at rate 1/2 keeps every shape >= 0
+    params = (12, 3, 1, 4, 1, 32)
+    poly = oracle.rand_fe(12, 1 << 12)
+    proof, cp = oracle.prove(params, [poly], [12], [[0]] * 2)
+    assert W.verify(params, [12], [[0]] * 2, proof) == (0, cp)
+
+
 def test_accepts_stacked_layout(oracle):
     ks = [8, 6, 6, 8, 5]
     polys = [oracle.rand_fe(20 + i, 1 << k) for i, k in enumerate(ks)]

@@ -1273,6 +1273,19 @@ static void check_params(const Params &p) {
   if (p.folding < 1 || p.folding > 8 || p.k < p.folding || p.k > 26 || p.rate < 0 ||
       p.rate > 8 || p.initial_reduction < 1 || p.soundness < 0 || p.soundness > 2)
     throw WhirError(-1, "invalid WHIR parameters");
+  // the reference computes the round shapes in usize (params.rs:190-203,
+  // whir.rs:150-166), where a negative result panics: refuse those sets
+  // (e.g. an initial_reduction above rate + folding, or a folding that
+  // leaves a negative number of final sumcheck rounds)
+  int n_rounds, fin;
+  number_of_rounds(p.folding, p.k, &n_rounds, &fin);
+  if (fin < 0) throw WhirError(-1, "invalid WHIR parameters: negative final sumcheck rounds");
+  for (int r = 0; r <= n_rounds; r++) {
+    int kfd, this_rate, prev_rate;
+    round_params(p, r, &kfd, &this_rate, &prev_rate);
+    if (kfd < 0 || this_rate < 0 || prev_rate < 0)
+      throw WhirError(-1, "invalid WHIR parameters: a round's domain or rate is negative");
+  }
 }
 
 Prover::Prover(Context *ctx, const Params &p) : m_(new Impl), ctx_(ctx), p_(p) {
