@@ -594,10 +594,11 @@ static int whir_open(const wo_params *p, wo_ts *ts, commitment *c0, prover_layou
 
 /* Parameter sets the reference can run: its round shapes are usize
  * arithmetic (params.rs:190-203, whir.rs:150-166) that panics when a result
- * would be negative; and every round's and the final STIR query count is
- * within MAX_STIR. */
+ * would be negative, every codeword fits the 2^24 two-adic subgroup, and
+ * every round's and the final STIR query count is within MAX_STIR. */
 static int stir_counts_ok(const wo_params *p) {
-  if (p->folding < 1 || p->k < p->folding) return 0;
+  if (p->folding < 1 || p->k < p->folding || p->security_level < 0) return 0;
+  if (p->k + p->rate - p->folding > 24) return 0; /* two-adicity of KoalaBear */
   int n_rounds, final_rounds;
   wo_number_of_rounds(p->folding, p->k, &n_rounds, &final_rounds);
   if (final_rounds < 0) return 0;
@@ -605,6 +606,7 @@ static int stir_counts_ok(const wo_params *p) {
     int kfd, this_rate, prev_rate;
     round_params(p, round, &kfd, &this_rate, &prev_rate);
     if (kfd < 0 || this_rate < 0 || prev_rate < 0) return 0;
+    if (round < n_rounds && p->k - p->folding * (round + 1) + this_rate - p->folding > 24) return 0;
     if (wo_n_stir_queries(p->soundness, p->security_level, prev_rate) < 0) return 0;
   }
   return 1;

@@ -62,17 +62,20 @@ def test_query_count_out_of_range_is_refused(oracle):
         oracle.prove(params, [oracle.rand_fe(1, 1 << 10)], [10], [[0]])
 
 
-@pytest.mark.parametrize("params", [(10, 2, 1, 5, 1, 32), (8, 1, 1, 3, 0, 32), (7, 8, 1, 1, 1, 32)])
+@pytest.mark.parametrize("params", [(10, 2, 1, 5, 1, 32), (8, 1, 1, 3, 0, 32), (7, 8, 1, 1, 1, 32),
+                                    (22, 2, 6, 1, 1, 32), (10, 2, 1, 1, 1, -5)])
 def test_parameters_the_reference_cannot_run_are_refused(oracle, params):
     # round shapes that go negative in the reference's usize arithmetic
-    # (whir.rs:150-166, params.rs:190-203) panic there; here they are refused
+    # (whir.rs:150-166, params.rs:190-203) panic there, and a codeword above
+    # 2^24 rows has no two-adic subgroup: all are refused here
     k = params[0]
     with pytest.raises(W.WhirError):
         W.workspace_bytes(params)
     with pytest.raises(W.WhirError):
         W.verify(params, [k], [[0]], b"\0" * 64)
-    with pytest.raises(RuntimeError):
-        oracle.prove(params, [oracle.rand_fe(1, 1 << k)], [k], [[0]])
+    if k <= 12:
+        with pytest.raises(RuntimeError):
+            oracle.prove(params, [oracle.rand_fe(1, 1 << k)], [k], [[0]])
 
 
 def test_reduction_up_to_rate_plus_folding_is_accepted(oracle):

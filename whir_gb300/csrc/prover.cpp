@@ -1271,8 +1271,12 @@ struct Prover::Impl {
 
 static void check_params(const Params &p) {
   if (p.folding < 1 || p.folding > 8 || p.k < p.folding || p.k > 26 || p.rate < 0 ||
-      p.rate > 8 || p.initial_reduction < 1 || p.soundness < 0 || p.soundness > 2)
+      p.rate > 8 || p.initial_reduction < 1 || p.soundness < 0 || p.soundness > 2 ||
+      p.security_level < 0)
     throw WhirError(-1, "invalid WHIR parameters");
+  // every codeword lies on a subgroup of KoalaBear's 2^24 two-adic group
+  if (p.k + p.rate - p.folding > 24)
+    throw WhirError(-1, "invalid WHIR parameters: codeword above 2^24 rows");
   // the reference computes the round shapes in usize (params.rs:190-203,
   // whir.rs:150-166), where a negative result panics: refuse those sets
   // (e.g. an initial_reduction above rate + folding, or a folding that
@@ -1285,6 +1289,8 @@ static void check_params(const Params &p) {
     round_params(p, r, &kfd, &this_rate, &prev_rate);
     if (kfd < 0 || this_rate < 0 || prev_rate < 0)
       throw WhirError(-1, "invalid WHIR parameters: a round's domain or rate is negative");
+    if (r < n_rounds && p.k - p.folding * (r + 1) + this_rate - p.folding > 24)
+      throw WhirError(-1, "invalid WHIR parameters: codeword above 2^24 rows");
   }
 }
 
