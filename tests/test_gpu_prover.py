@@ -74,6 +74,16 @@ def test_reference_bench_shape_k25(ctx, oracle):
     check(ctx, oracle, (25, 5, 1, 3, 1, 123), [poly], [25], [[0]])
 
 
+@pytest.mark.parametrize("params,n", [((10, 2, 1, 1, 1, 32), 0), ((12, 4, 1, 1, 1, 100), 12),
+                                      ((11, 3, 1, 1, 1, 32), 20)])
+def test_claim_counts(ctx, oracle, params, n):
+    # no claim at all (only the OOD claims), and more points than the split
+    # eq tables take by value (8): the uploaded-point path
+    k = params[0]
+    poly = oracle.rand_fe(5, 1 << k)
+    check(ctx, oracle, params, [poly], [k], [[0]] * n)
+
+
 def test_stacked_layout(ctx, oracle):
     # several polynomials of different sizes in one layout (ProverStack::layout)
     ks = [8, 6, 6, 8, 5]
