@@ -67,6 +67,16 @@ def test_rate_one(ctx, oracle, params):
     check(ctx, oracle, params, [poly], [k], [[0]] * 2)
 
 
+# the largest foldings: 2^7 / 2^8-word base rows, 2^10-word extension rows
+# (the generic leaf sponge), SVO claims over 2^8 columns
+@pytest.mark.parametrize("params", [(12, 7, 1, 2, 0, 32), (16, 8, 1, 1, 1, 100),
+                                    (14, 7, 2, 3, 2, 64), (10, 8, 1, 1, 1, 32)])
+def test_whir_folding7_8(ctx, oracle, params):
+    k = params[0]
+    poly = oracle.rand_fe(9, 1 << k)
+    check(ctx, oracle, params, [poly], [k], [[0]] * 2)
+
+
 def test_reference_bench_shape_k25(ctx, oracle):
     # the reference's own benchmark, whir_bench (crates/whir/src/test.rs:284-290):
     # k = 25, folding 5, rate 1/2, initial_reduction 3, JohnsonBound, 123-bit, 1 claim
