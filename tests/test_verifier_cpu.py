@@ -139,3 +139,30 @@ def test_argument_errors():
         W.verify((10, 4, 1, 1, 1, 100), [9], [[0]], b"\\0" * 64)   # layout size != 2^k
     with pytest.raises(W.WhirError):
         W.verify((10, 4, 1, 1, 1, 100), [10], [[1]], b"\\0" * 64)  # unknown poly id
+
+
+@pytest.mark.parametrize("params,ks,groups", [
+    ((10, 2, 1, 1, 1, 32), [10], [[0]] * 2),
+    ((12, 4, 2, 1, 1, 100), [12], [[0]]),
+    ((10, 3, 1, 1, 1, 32), [8, 6, 6, 8, 5], [[0, 3], [1, 2], [4], [3]]),
+    ((6, 1, 0, 1, 1, 32), [6], [[0]])])
+def test_rejects_random_and_corrupted_bytes(oracle, params, ks, groups):
+    # random byte strings, proofs with random bytes overwritten, and random
+    # prefixes: every one is rejected (never accepted, never a crash)
+    polys = [oracle.rand_fe(3 + i, 1 << k) for i, k in enumerate(ks)]
+    proof, _ = oracle.prove(params, polys, ks, groups)
+    rng = np.random.default_rng(sum(ks))
+    for trial in range(150):
+        kind = trial % 3
+        if kind == 0:
+            b = rng.integers(0, 256, int(rng.integers(0, len(proof) + 100)), dtype=np.uint8).tobytes()
+        elif kind == 1:
+            m = bytearray(proof)
+            for _ in range(int(rng.integers(1, 20))):
+                m[int(rng.integers(0, len(m)))] = int(rng.integers(0, 256))
+            if bytes(m) == proof:
+                continue
+            b = bytes(m)
+        else:
+            b = proof[:int(rng.integers(0, len(proof)))]
+        assert W.verify(params, ks, groups, b)[0] != 0
