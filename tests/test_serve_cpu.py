@@ -86,3 +86,24 @@ def test_proof_bound_covers_oracle_proofs(oracle):
         poly = oracle.rand_fe(k, 1 << k)
         proof, _ = oracle.prove((k, f, r, 1, 1, 100), [poly], [k], [[0]] * n)
         assert len(proof) <= W.proof_bound((k, f, r, 1, 1, 100), n)
+
+
+def test_short_polynomial_buffers_are_refused_before_the_library():
+    # the C ABI reads 2^k words from the pointers it is given; the binding
+    # checks the buffers' sizes first (no GPU needed: the check comes first)
+    class FakeDev(W.DeviceArray):
+        def __init__(self, nbytes):
+            self.nbytes, self.ptr, self.ctx = nbytes, 0, None
+
+        def close(self):
+            pass
+
+    with pytest.raises(W.WhirError):
+        W.Whir._polys([np.zeros(100, np.uint32)], [7])
+    with pytest.raises(W.WhirError):
+        W.Whir._polys(np.zeros(100, np.uint32), [7])
+    with pytest.raises(W.WhirError):
+        W.Whir._polys(FakeDev(4 * 127), [7])
+    assert W.Whir._polys([np.zeros(128, np.uint32), np.zeros(64, np.uint32)], [7, 6])[1] == 0
+    with pytest.raises(W.WhirError):
+        W._jobs_in([W.Job((12, 4, 1, 1, 1, 100), FakeDev(4 << 11))])

@@ -422,15 +422,27 @@ class Whir:
         self.h = h.value
 
     @staticmethod
-    def _polys(polys):
+    def _polys(polys, poly_k):
+        # the C ABI reads sum(2^k) words from the pointer it is given: check
+        # the buffer holds them (a short device buffer would be read past)
+        need = 4 * sum(1 << int(k) for k in poly_k if 0 <= int(k) <= 40)
         if isinstance(polys, DeviceArray):
+            if polys.nbytes < need:
+                raise WhirError(f"device polynomials hold {polys.nbytes} bytes, the layout needs {need}")
             return polys.ptr, 1, None
-        flat = np.ascontiguousarray(np.concatenate([np.asarray(p, np.uint32) for p in polys])
-                                    if isinstance(polys, (list, tuple)) else polys, np.uint32)
+        if isinstance(polys, (list, tuple)):
+            parts = [np.asarray(p, np.uint32) for p in polys]
+            if len(parts) != len(poly_k) or any(q.size != 1 << int(k) for q, k in zip(parts, poly_k)):
+                raise WhirError("each polynomial must hold 2^k words for its k")
+            flat = np.ascontiguousarray(np.concatenate(parts), np.uint32)
+        else:
+            flat = np.ascontiguousarray(polys, np.uint32)
+            if flat.nbytes < need:
+                raise WhirError(f"polynomials hold {flat.nbytes} bytes, the layout needs {need}")
         return flat.ctypes.data, 0, flat
 
     def commit(self, transcript, polys, poly_k):
-        ptr, dev, keep = self._polys(polys)
+        ptr, dev, keep = self._polys(polys, poly_k)
         ks = (ctypes.c_int32 * len(poly_k))(*poly_k)
         _check(lib().whir_commit(self.h, transcript.h, ptr, dev, ks, len(poly_k)))
 
@@ -444,7 +456,7 @@ class Whir:
         _check(lib().whir_open(self.h, transcript.h))
 
     def prove(self, transcript, polys, poly_k, groups):
-        ptr, dev, keep = self._polys(polys)
+        ptr, dev, keep = self._polys(polys, poly_k)
         ks = (ctypes.c_int32 * len(poly_k))(*poly_k)
         gn = (ctypes.c_int32 * max(1, len(groups)))(*[len(g) for g in groups])
         flat = [i for g in groups for i in g]
@@ -524,6 +536,8 @@ def _jobs_in(jobs):
         c = arr[i]
         c.params = j.params
         if isinstance(j.poly, DeviceArray):
+            if 0 <= j.params.k <= 40 and j.poly.nbytes < 4 << j.params.k:
+                raise WhirError("device polynomial smaller than 2^params.k words")
             c.poly, c.poly_on_device = j.poly.ptr, 1
         else:
             a = np.ascontiguousarray(j.poly, np.uint32)
