@@ -86,6 +86,15 @@ def test_proof_bound_covers_oracle_proofs(oracle):
         poly = oracle.rand_fe(k, 1 << k)
         proof, _ = oracle.prove((k, f, r, 1, 1, 100), [poly], [k], [[0]] * n)
         assert len(proof) <= W.proof_bound((k, f, r, 1, 1, 100), n)
+    # other foldings, rates, reductions and soundness modes (a served job's
+    # proof buffer is sized by this bound)
+    for params in [(12, 5, 1, 5, 2, 32), (15, 6, 1, 1, 1, 100), (12, 7, 1, 2, 0, 32),
+                   (16, 8, 1, 1, 1, 100), (12, 4, 0, 1, 1, 100), (12, 3, 1, 4, 1, 32),
+                   (14, 4, 3, 1, 2, 100), (9, 1, 1, 1, 0, 32)]:
+        k = params[0]
+        for n in (1, 4):
+            proof, _ = oracle.prove(params, [oracle.rand_fe(k, 1 << k)], [k], [[0]] * n)
+            assert len(proof) <= W.proof_bound(params, n)
 
 
 def test_short_polynomial_buffers_are_refused_before_the_library():
