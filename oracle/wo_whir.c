@@ -36,9 +36,9 @@ static double log_1_delta(int s, int lir) {
 }
 /* params.rs:118-122 converts with Rust's `as usize`, which saturates: NaN
  * and negative values (rate 1, log_inv_rate 0, where log(1 - delta) is 0 or
- * positive) give 0 queries.  Counts past MAX_STIR (the size of the index
- * arrays here) are reported as -1. */
-#define MAX_STIR 4096
+ * positive) give 0 queries.  Counts past MAX_STIR (the library's limit,
+ * within the 4096-entry index arrays here) are reported as -1. */
+#define MAX_STIR 3072 /* the library's limit */
 int wo_n_stir_queries(int s, int security, int lir) {
   double q = ceil(-(double)security / log_1_delta(s, lir));
   if (!(q > 0.)) return 0;

@@ -77,6 +77,16 @@ def test_whir_folding7_8(ctx, oracle, params):
     check(ctx, oracle, params, [poly], [k], [[0]] * 2)
 
 
+@pytest.mark.parametrize("params", [(12, 2, 1, 1, 0, 1000), (14, 4, 1, 1, 0, 1200)])
+def test_many_queries(ctx, oracle, params):
+    # unique decoding at 1000-1200 bits: 2410 and 2892 STIR queries, past the
+    # 2048 indexes the opening gather takes by value (the uploaded-index
+    # path) and near the 3072 the pow-claim combination holds
+    k = params[0]
+    poly = oracle.rand_fe(4, 1 << k)
+    check(ctx, oracle, params, [poly], [k], [[0]] * 2)
+
+
 def test_reference_bench_shape_k25(ctx, oracle):
     # the reference's own benchmark, whir_bench (crates/whir/src/test.rs:284-290):
     # k = 25, folding 5, rate 1/2, initial_reduction 3, JohnsonBound, 123-bit, 1 claim

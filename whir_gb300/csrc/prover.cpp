@@ -38,11 +38,14 @@ static double log_1_delta(int s, int lir) {
 }
 // params.rs:118-122 converts with Rust's `as usize`, which saturates: NaN
 // and negative values (rate 1, log_inv_rate 0, where log(1 - delta) is 0 or
-// positive) give 0 queries.  Counts that no codeword could serve are refused.
+// positive) give 0 queries.  Counts above MAX_STIR_QUERIES are refused (the
+// pow-claim combination keeps one extension element per query in shared
+// memory: 48 KB).
+constexpr int MAX_STIR_QUERIES = 3072;
 int n_stir_queries(int s, int security, int lir) {
   const double q = ceil(-(double)security / log_1_delta(s, lir));
   if (!(q > 0.)) return 0;
-  if (q > (double)(1 << 16)) throw WhirError(-1, "STIR query count out of range");
+  if (q > (double)MAX_STIR_QUERIES) throw WhirError(-1, "STIR query count above 3072");
   return (int)q;
 }
 int n_ood_queries(int s, int security, int log_degree, int lir, int field_bits) {
