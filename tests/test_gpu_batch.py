@@ -171,3 +171,16 @@ def test_run_with_parameters_the_reference_cannot_run_is_refused(oracle):
     W.prove_jobs([good], workers=2)
     want, wcp = oracle.prove((10, 2, 1, 1, 1, 32), [good.poly], [10], [[0]])
     assert good.status == 0 and good.proof == want and good.checkpoint == wcp
+
+
+@pytest.mark.parametrize("params,n", [((16, 4, 2, 1, 1, 100), 4), ((14, 4, 1, 1, 0, 1200), 2),
+                                      ((16, 8, 1, 1, 1, 100), 2), ((12, 3, 1, 1, 1, 32), 20),
+                                      ((18, 6, 2, 2, 1, 100), 3), ((12, 4, 0, 1, 1, 100), 2)])
+def test_workspace_plan_covers_a_proof(oracle, params, n):
+    # admission charges a job whir_workspace_bytes; the device memory its
+    # worker holds after the proof (many queries, many claims, large
+    # foldings, rate 1 included) must not exceed it
+    j = W.Job(params, oracle.rand_fe(3, 1 << params[0]), claims=n)
+    _, peak = W.prove_jobs([j], workers=1)
+    assert j.status == 0
+    assert peak <= W.workspace_bytes(params)
