@@ -618,9 +618,26 @@ static int group_offset(const wo_claims *cl, int g) {
   return o;
 }
 
+/* a group's point is expanded to the size of its first polynomial, so every
+ * member must have that size (and every id must name a polynomial) */
+static int groups_ok(const wo_claims *cl) {
+  int o = 0;
+  for (int g = 0; g < cl->n_groups; g++) {
+    if (cl->group_n[g] < 1) return 0;
+    for (int j = 0; j < cl->group_n[g]; j++) {
+      int id = cl->group_ids[o + j];
+      if (id < 0 || id >= cl->n_polys) return 0;
+      if (cl->poly_k[id] != cl->poly_k[cl->group_ids[o]]) return 0;
+    }
+    o += cl->group_n[g];
+  }
+  return 1;
+}
+
 int wo_prove(const wo_params *prm, const wo_claims *cl, const uint32_t *polys, uint8_t *proof,
              size_t cap, size_t *len, uint32_t *checkpoint) {
   if (!stir_counts_ok(prm)) return -1;  /* parameters the reference cannot run */
+  if (!groups_ok(cl)) return -1;
   wo_ts ts;
   ts_writer(&ts, proof, cap);
   prover_layout L;
@@ -708,7 +725,7 @@ static int reduce_round(wo_ts *ts, ext *sum, ext *r) {
 
 int wo_verify(const wo_params *p, const wo_claims *cl, const uint8_t *proof, size_t len,
               uint32_t *checkpoint) {
-  if (!stir_counts_ok(p)) return -1;
+  if (!stir_counts_ok(p) || !groups_ok(cl)) return -1;
   wo_ts ts;
   ts_reader(&ts, proof, len);
   int rc = 0;

@@ -166,3 +166,17 @@ def test_rejects_random_and_corrupted_bytes(oracle, params, ks, groups):
         else:
             b = proof[:int(rng.integers(0, len(proof)))]
         assert W.verify(params, ks, groups, b)[0] != 0
+
+
+def test_claim_group_of_mixed_sizes_is_refused(oracle):
+    # one point per group, expanded to its first polynomial's size: every
+    # member must have that size (library and oracle refuse alike)
+    ks = [10, 9, 9]
+    polys = [oracle.rand_fe(1 + i, 1 << k) for i, k in enumerate(ks)]
+    params = (11, 3, 1, 1, 1, 32)
+    with pytest.raises(RuntimeError):
+        oracle.prove(params, polys, ks, [[0, 1]])
+    with pytest.raises(W.WhirError):
+        W.verify(params, ks, [[0, 1]], b"\0" * 64)
+    proof, cp = oracle.prove(params, polys, ks, [[1, 2], [0]])
+    assert W.verify(params, ks, [[1, 2], [0]], proof) == (0, cp)
