@@ -95,7 +95,7 @@ WHIR_API int whir_merkle_free(whir_tree *tree);
 
 /* ---- polynomial and sumcheck passes (crates/poly/src/{point,eq,poly}.rs,
  * crates/whir/src/sumcheck/{svo,expr,combine}.rs) ---- */
-/* Point::eq (point.rs:159-175): 2^k extension words at out (device) */
+/* Point::eq (point.rs:110-126): 2^k extension words at out (device) */
 WHIR_API int whir_eq_table(whir_ctx *ctx, const uint32_t *point, int k, const uint32_t scale[4],
                   uint32_t *out);
 /* SplitEq::compress_hi (eq.rs:290-398): fix the high kz variables of a base
@@ -105,13 +105,13 @@ WHIR_API int whir_compress_hi(whir_ctx *ctx, const uint32_t *poly, int k, const 
 /* SplitEq::compress_lo (eq.rs:400-489): fix the low kz variables; out (device) */
 WHIR_API int whir_compress_lo(whir_ctx *ctx, const uint32_t *poly, int k, const uint32_t *point, int kz,
                      uint32_t *out);
-/* Poly::eval_ext (poly.rs:312-318) of an extension poly (device) */
+/* Poly::eval_ext (poly.rs:89-95) of an extension poly (device) */
 WHIR_API int whir_eval_ext(whir_ctx *ctx, const uint32_t *poly, int k, const uint32_t *point,
                   uint32_t out[4]);
 /* coeffs (expr.rs:14-27) of extension poly and weights (device, 2^k each) */
 WHIR_API int whir_sumcheck_coeffs(whir_ctx *ctx, const uint32_t *poly, const uint32_t *weights, int k,
                          uint32_t c0[4], uint32_t c2[4]);
-/* fix_lo_var_mut (poly.rs:354-365) of both arrays into poly_out/w_out
+/* fix_lo_var_mut (poly.rs:131-142) of both arrays into poly_out/w_out
  * (device, 2^(k-1) each; must not alias the inputs) */
 WHIR_API int whir_sumcheck_fold(whir_ctx *ctx, const uint32_t *poly, const uint32_t *weights, int k,
                        const uint32_t r[4], uint32_t *poly_out, uint32_t *weights_out);
@@ -253,8 +253,12 @@ WHIR_API int whir_serve_simulate(const double *arrival_s, const uint64_t *need,
  * cuda_stream (NULL: the default stream) of the current device and returns
  * once out (host, 2^(k-kz) extension elements) is written.  The first call
  * on a device looks up the array's device address; make it before any
- * stream capture.  All calls share the array: calls that overlap on the GPU
- * (other streams, other threads) race; calls on one stream are safe. ---- */
+ * stream capture, and do not call it after a cudaDeviceReset in the same
+ * process (the address is kept; a reset may move the array).  All calls share
+ * the array, so calls must be serialised: issued to one stream from one host
+ * thread, or under the caller's own lock.  Calls that overlap on the GPU
+ * (other streams), or that two host threads queue on one stream at the same
+ * time, race. ---- */
 WHIR_API int whir_compress_hi_noalloc(void *cuda_stream, const uint32_t *poly, int k,
                                       const uint32_t *point, int kz, uint32_t *out);
 

@@ -8,7 +8,7 @@
  */
 #include "wo_internal.h"
 
-/* Point::eq (crates/poly/src/point.rs:159-175): LSB-first doubling, bit i of
+/* Point::eq (crates/poly/src/point.rs:110-126): LSB-first doubling, bit i of
  * the index selects z_i. */
 void eq_table(const ext *z, int k, ext scale, ext *out) {
   out[0] = scale;

@@ -593,7 +593,7 @@ static int whir_open(const wo_params *p, wo_ts *ts, commitment *c0, prover_layou
 }
 
 /* Parameter sets the reference can run: its round shapes are usize
- * arithmetic (params.rs:190-203, whir.rs:150-166) that panics when a result
+ * arithmetic (params.rs:186-202, whir.rs:150-166) that panics when a result
  * would be negative, every codeword fits the 2^24 two-adic subgroup, and
  * every round's and the final STIR query count is within MAX_STIR. */
 static int stir_counts_ok(const wo_params *p) {

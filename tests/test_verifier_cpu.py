@@ -66,7 +66,7 @@ def test_query_count_out_of_range_is_refused(oracle):
                                     (22, 2, 6, 1, 1, 32), (10, 2, 1, 1, 1, -5)])
 def test_parameters_the_reference_cannot_run_are_refused(oracle, params):
     # round shapes that go negative in the reference's usize arithmetic
-    # (whir.rs:150-166, params.rs:190-203) panic there, and a codeword above
+    # (whir.rs:150-166, params.rs:186-202) panic there, and a codeword above
     # 2^24 rows has no two-adic subgroup: all are refused here
     k = params[0]
     with pytest.raises(W.WhirError):

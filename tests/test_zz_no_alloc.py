@@ -35,16 +35,21 @@ def _call(ctx, dev_poly, k, point, kz):
     return out
 
 
-def test_noalloc_matches_allocating_entry_point_twice(ctx):
+def test_noalloc_matches_allocating_entry_point_twice(ctx, oracle):
     # two consecutive calls of the same shape (leftover accumulators would
-    # show up in the second), then the largest shape the scratch holds
-    for k, kz, seed in ((20, 16, 3), (20, 16, 4), (28, 20, 5)):
+    # show up in the second), the largest shape the scratch holds, and the
+    # shapes whose split eq tables are smaller than the 2^10-entry halves
+    # (kz < 10: a one-entry high table at kz = 0); each result also equals
+    # the oracle's (exact: field arithmetic, zero tolerance)
+    for k, kz, seed in ((20, 16, 3), (20, 16, 4), (8, 0, 8), (12, 5, 9), (18, 10, 10),
+                        (28, 20, 5)):
         poly = W.random_field(seed, 1 << k)
         point = W.random_field(seed + 100, 4 * kz)
         dev = ctx.to_device(poly)
-        want = W.compress_hi(ctx, dev, k, point, kz)  # exact: field arithmetic, zero tolerance
+        want = W.compress_hi(ctx, dev, k, point, kz)
         got = _call(ctx, dev, k, point, kz)
-        assert np.array_equal(got, want)
+        assert np.array_equal(got, want), (k, kz)
+        assert np.array_equal(got, oracle.compress_hi(poly, k, point, kz)), (k, kz)
         dev.close()
 
 

@@ -15,13 +15,18 @@
 // elements) and hi (2^10), then the 64-bit accumulators (4 words for each of
 // at most 2^8 outputs).  The tables are rewritten by every call; the
 // accumulators are cleared by every call before use.  All calls share the
-// array, so calls that overlap on the GPU (different streams, or different
-// host threads) race and corrupt each other's results; calls issued to one
-// stream run one after another and are safe.
+// array, so calls must be serialised: issued to one stream from one host
+// thread, or under the caller's own lock.  Calls that overlap on the GPU
+// (different streams) race, and so do calls that two host threads queue on
+// the same stream at the same time (their launches interleave, and both read
+// the combined accumulators).
 //
 // The device address of the array is looked up once per device
 // (cudaGetSymbolAddress with that device current) by the first call made on
-// that device; make that first call before any stream capture begins.
+// that device; make that first call before any stream capture begins.  The
+// address is kept for the life of the process: a cudaDeviceReset reloads the
+// module and may move the array, so do not call this entry point after
+// resetting the device in the same process.
 #include <mutex>
 
 #include "../../include/whir_gb300.h"

@@ -1280,7 +1280,7 @@ static void check_params(const Params &p) {
   // every codeword lies on a subgroup of KoalaBear's 2^24 two-adic group
   if (p.k + p.rate - p.folding > 24)
     throw WhirError(-1, "invalid WHIR parameters: codeword above 2^24 rows");
-  // the reference computes the round shapes in usize (params.rs:190-203,
+  // the reference computes the round shapes in usize (params.rs:186-202,
   // whir.rs:150-166), where a negative result panics: refuse those sets
   // (e.g. an initial_reduction above rate + folding, or a folding that
   // leaves a negative number of final sumcheck rounds)

@@ -40,7 +40,7 @@ __host__ __forceinline__ bool aligned16(const void *p) { return ((uintptr_t)p & 
 
 
 // eq table entries over z[off .. off+nv) times scale: entry b selects z_i
-// when bit i of b is set, 1 - z_i otherwise (Point::eq, point.rs:159-175).
+// when bit i of b is set, 1 - z_i otherwise (Point::eq, point.rs:110-126).
 // Publish (kernels.h): after this CTA's atomics into acc, the last CTA of
 // the launch copies the sums out and zeroes them.  Every thread of the CTA
 // calls it.
@@ -553,7 +553,7 @@ static size_t add_pows_smem(int k, int n) {
 
 cudaError_t add_pows_val(E4 *w, int k, const PowArgs &a, int n, uint32_t *tab, cudaStream_t st) {
   if (n == 0) return cudaSuccess;
-  if (n > PowArgs::N) return cudaErrorInvalidValue;
+  if (n > PowArgs::N || add_pows_smem(k, n) > 48 * 1024) return cudaErrorInvalidValue;
   int s = k / 2;
   size_t words = add_pows_scratch_words(k, n);
   pow_tables_val_kernel<<<(unsigned)((words + 255) / 256), 256, 0, st>>>(a, n, s, k, tab);
@@ -576,13 +576,13 @@ size_t add_pows_scratch_words(int k, int n) {
 cudaError_t add_pows(E4 *w, int k, const uint32_t *vars, const E4 *scales, int n, uint32_t *tab,
                      cudaStream_t st) {
   if (n == 0) return cudaSuccess;
+  const size_t smem = add_pows_smem(k, n);
+  if (smem > 48 * 1024) return cudaErrorInvalidValue;  // more than 3072 points
   int s = k / 2;
   size_t words = add_pows_scratch_words(k, n);
   pow_tables_kernel<<<(unsigned)((words + 255) / 256), 256, 0, st>>>(vars, n, s, k, tab);
   count_launches(1);
   size_t N = (size_t)1 << k;
-  const size_t smem = add_pows_smem(k, n);
-  if (smem > 48 * 1024) return cudaErrorInvalidValue;  // more than 3072 points
   const unsigned g = (unsigned)((N + AP_T - 1) / AP_T);
   if (aligned16(w))
     add_pows_kernel<true><<<g, AP_T, smem, st>>>(w, N, s, n, tab, scales);
