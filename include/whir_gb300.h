@@ -171,6 +171,25 @@ WHIR_API int whir_prove(whir_prover *p, whir_transcript *t, const uint32_t *poly
                const int32_t *poly_k, int n_polys, const int32_t *group_n, int n_groups,
                const int32_t *group_ids);
 
+/* Lock-step proving of `batch` polynomials of one shape: the reference
+ * harness (crates/whir/src/test.rs:218-235) on each polynomial (commit, then
+ * n_claims claims at transcript-drawn points, then Whir::open; or the
+ * commitment alone), with every device pass of all instances in one launch
+ * and every transcript round trip waited for once.  No counterpart in the
+ * reference, whose harness proves one polynomial per call; each instance's
+ * proof bytes equal whir_prove's on the same polynomial.  polys[b]: 2^k
+ * words each (host, or device when on_device != 0).  Proof b is copied to
+ * proofs + b * proof_cap (up to proof_cap bytes; proof_len[b] is its full
+ * length) and checkpoints[b] is the base element drawn after it
+ * (test.rs:236).  1 <= batch <= whir_batch_max(params). */
+WHIR_API int whir_prove_batch(whir_ctx *ctx, const whir_params *params,
+                              const uint32_t *const *polys, int on_device, int batch,
+                              int n_claims, int commit_only, uint8_t *proofs, size_t proof_cap,
+                              size_t *proof_len, uint32_t *checkpoints);
+/* the largest batch whir_prove_batch takes for these parameters (the batched
+ * codewords must fit the DFT's 32-bit indexing) */
+WHIR_API int whir_batch_max(const whir_params *params, int32_t *max_batch);
+
 /* Whir::verify (crates/whir/src/whir.rs:361-522, sumcheck/verifier.rs) on the
  * host: checks a proof of whir_prove with the same parameters, polynomial
  * sizes and claim groups.  *result: 0 accepted; 1 the bytes ran out or held a

@@ -127,6 +127,11 @@ _SIGS = {
                                            ctypes.c_int, ctypes.c_uint64,
                                            ctypes.POINTER(ctypes.c_double),
                                            ctypes.POINTER(ctypes.c_double), i32p, i32p]),
+    "whir_prove_batch": (ctypes.c_int, [vp, ctypes.POINTER(Params), ctypes.POINTER(vp),
+                                        ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_int,
+                                        ctypes.c_char_p, ctypes.c_size_t,
+                                        ctypes.POINTER(ctypes.c_size_t), u32p]),
+    "whir_batch_max": (ctypes.c_int, [ctypes.POINTER(Params), i32p]),
     "whir_counters": (ctypes.c_int, [vp, ctypes.POINTER(ctypes.c_uint64),
                                      ctypes.POINTER(ctypes.c_uint64),
                                      ctypes.POINTER(ctypes.c_uint64)]),
@@ -483,6 +488,48 @@ def prove_harness(ctx, params, polys, poly_k, groups, whir=None):
     w.prove(t, polys, poly_k, groups)
     cp = t.draw_base()
     return t.finalize(), cp
+
+
+def batch_max(params):
+    """The most polynomials one whir_prove_batch call takes for these parameters."""
+    p = params if isinstance(params, Params) else Params(*params)
+    out = ctypes.c_int32()
+    _check(lib().whir_batch_max(ctypes.byref(p), ctypes.byref(out)))
+    return out.value
+
+
+def prove_batch(ctx, params, polys, claims=1, commit_only=False):
+    """whir_prove_batch: the harness on each polynomial of one shape, in lock
+    step.  polys: np.uint32 arrays of 2^k words, or DeviceArrays (all of one
+    kind).  Returns [(proof bytes, checkpoint)] in input order."""
+    p = params if isinstance(params, Params) else Params(*params)
+    n = len(polys)
+    on_device = n > 0 and isinstance(polys[0], DeviceArray)
+    keep, ptrs = [], (vp * max(1, n))()
+    for i, a in enumerate(polys):
+        if on_device:
+            if not isinstance(a, DeviceArray) or a.nbytes < 4 << p.k:
+                raise WhirError("device polynomial smaller than 2^params.k words")
+            ptrs[i] = a.ptr
+        else:
+            a = np.ascontiguousarray(a, np.uint32)
+            if a.size != (1 << p.k):
+                raise WhirError("polynomial size does not match params.k")
+            keep.append(a)
+            ptrs[i] = a.ctypes.data
+    cap = 64 if commit_only else proof_bound(p, claims)
+    buf = ctypes.create_string_buffer(cap * max(1, n))
+    lens = (ctypes.c_size_t * max(1, n))()
+    cps = np.zeros(max(1, n), np.uint32)
+    _check(lib().whir_prove_batch(ctx.h, ctypes.byref(p), ptrs, 1 if on_device else 0, n,
+                                  0 if commit_only else claims, 1 if commit_only else 0, buf, cap,
+                                  lens, cps.ctypes.data_as(u32p)))
+    out = []
+    for i in range(n):
+        if lens[i] > cap:
+            raise WhirError("proof longer than its buffer")
+        out.append((buf.raw[i * cap:i * cap + lens[i]], int(cps[i])))
+    return out
 
 
 class Job:

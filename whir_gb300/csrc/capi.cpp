@@ -17,6 +17,7 @@
 #include "kernels.h"
 #include "poseidon2_host.h"
 #include "batch.h"
+#include "batch_prover.h"
 #include "prover.h"
 #include "tune.h"
 #include "verifier.h"
@@ -34,6 +35,7 @@ struct whir_ctx {
   // fresh reservation and its release cost ~0.3 ms at 2^21 leaves)
   std::unique_ptr<DeviceBuffer> spare_nodes;
   std::mutex spare_mu;
+  std::unique_ptr<whir::BatchProver> batch;  // whir_prove_batch's prover, made on first use
   explicit whir_ctx(int dev) : ctx(dev) {}
 };
 struct whir_transcript {
@@ -568,6 +570,41 @@ static whir::Params params_in(const whir_params *q) {
   need(q != nullptr, "null parameters");
   return whir::Params{q->k, q->folding, q->rate, q->initial_reduction, q->soundness,
                       q->security_level};
+}
+
+int whir_prove_batch(whir_ctx *ctx, const whir_params *params, const uint32_t *const *polys,
+                     int on_device, int batch, int n_claims, int commit_only, uint8_t *proofs,
+                     size_t proof_cap, size_t *proof_len, uint32_t *checkpoints) {
+  API_BEGIN
+  need(ctx && polys && proof_len && checkpoints, "null argument");
+  need(proof_cap == 0 || proofs != nullptr, "proof buffer missing");
+  need(n_claims >= 0 && n_claims <= 64, "claims per instance out of range");
+  whir::Params p = params_in(params);
+  need(batch >= 1 && batch <= whir::BatchProver::max_batch(p), "batch size out of range");
+  for (int b = 0; b < batch; b++) need(polys[b] != nullptr, "null polynomial");
+  if (!ctx->batch)
+    ctx->batch.reset(new whir::BatchProver(&ctx->ctx, p, (int)std::min(16u, std::max(1u, std::thread::hardware_concurrency()))));
+  else
+    ctx->batch->set_params(p);
+  std::vector<whir::Transcript> ts(batch);
+  std::vector<whir::Transcript *> tp(batch);
+  std::vector<const uint32_t *> pp(polys, polys + batch);
+  for (int b = 0; b < batch; b++) tp[b] = &ts[b];
+  ctx->batch->prove(tp, pp, on_device != 0, n_claims, commit_only != 0);
+  for (int b = 0; b < batch; b++) {
+    checkpoints[b] = ts[b].draw_fe();
+    const std::vector<uint8_t> &bytes = ts[b].bytes();
+    proof_len[b] = bytes.size();
+    if (proof_cap) memcpy(proofs + (size_t)b * proof_cap, bytes.data(), std::min(proof_cap, bytes.size()));
+  }
+  API_END
+}
+
+int whir_batch_max(const whir_params *params, int32_t *max_batch) {
+  API_BEGIN
+  need(max_batch != nullptr, "null argument");
+  *max_batch = whir::BatchProver::max_batch(params_in(params));
+  API_END
 }
 
 struct whir_server {

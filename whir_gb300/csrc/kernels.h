@@ -162,6 +162,12 @@ struct CodeState {
   const uint32_t *wd;   // 2^d powers of w^-S
   int n, d, k_data;
   uint32_t omega, winv, two_inv;  // w, w^-1 (w = two_adic_generator(k_data)), 1/2
+  // several instances' queries in one launch: query i belongs to instance
+  // inst[i], whose challenge (r_prev, r_last) is r_b[inst[i]] and whose sums
+  // go to acc + inst[i] * acc_stride (all unset for one instance)
+  const int *inst = nullptr;
+  const kb::E4 *r_b = nullptr;
+  size_t acc_stride = 0;
 };
 // round r: G update with r_prev (r >= 1), then this round's part of (c0, c2)
 // added to acc[0..8) (and, at round 0, the sum term to acc[8..12))
@@ -171,6 +177,64 @@ cudaError_t code_finish(const CodeState &s, kb::E4 r_last, cudaStream_t st);
 // out[q] = <eq(rs), row(idx[q])> over base rows (fold_with_code evals, prover.rs:497-506)
 cudaError_t row_evals(const uint32_t *rows, int row_len, const uint32_t *idx, int n,
                       const Point &rs, kb::E4 *out, cudaStream_t st);
+
+// ---- many instances of one shape in one launch (batched proving) ----
+// Instance y of a launch (blockIdx.y) works on its own arrays, found at y
+// times a stride from each base, with its own challenges from per-instance
+// device arrays; reductions land in acc + y * (words per instance), and the
+// last CTA of the whole launch publishes every instance's words at once.
+// A batched codeword is the row-major matrix whose row r holds row r of
+// every instance in turn (row r of instance y = row r batch + y); its
+// Merkle tree is the halves-paired tree over those rows stopped at the level
+// of `batch` nodes, which are the instances' roots (with halves pairing the
+// instances never meet below that level).
+struct HiStrides {
+  size_t poly = 0, tab = 0, acc = 0;  // elements between consecutive instances
+};
+cudaError_t compress_hi_batch(const uint32_t *poly, int k, int ks, const kb::E4 *eq_lo, int s_lo,
+                              const kb::E4 *eq_hi, unsigned long long *acc, int batch,
+                              const HiStrides &sd, cudaStream_t st,
+                              const Publish &pub = Publish());
+// rs_b: batch x ks challenges; instance y reads poly + y poly_stride, writes
+// out + y 2^(k - ks)
+cudaError_t compress_lo_batch(const uint32_t *poly, int k, int ks, const kb::E4 *rs_b, int batch,
+                              size_t poly_stride, kb::E4 *out, cudaStream_t st);
+// instance y: w + y 2^k and n_tables tables from tables + y n_tables (2^s + 2^(k-s))
+cudaError_t add_eq_batch(kb::E4 *w, int k, const kb::E4 *tables, int n_tables, int batch,
+                         cudaStream_t st);
+// ragged: instance y adds vars[off[y] .. off[y+1]) with their scales into
+// w + y 2^k (off: batch + 1 device ints, max_n the largest count)
+cudaError_t add_pows_batch(kb::E4 *w, int k, const uint32_t *vars, const kb::E4 *scales,
+                           const int *off, int n_total, int max_n, int batch, uint32_t *tab,
+                           cudaStream_t st);
+// arrays of instance y at y n_in (in) and y n_in / 2 (out), challenge r_b[y]
+// (fold), sums at acc + y acc_stride
+cudaError_t sumcheck_round_batch(const kb::E4 *p_in, const kb::E4 *w_in, size_t n_in, bool fold,
+                                 const kb::E4 *r_b, kb::E4 *p_out, kb::E4 *w_out, bool coeffs,
+                                 unsigned long long *acc, size_t acc_stride, int batch,
+                                 cudaStream_t st, const Publish &pub = Publish());
+// instance y: poly + y 2^k, tables at y tab_stride, sum at acc + 4 y
+cudaError_t eval_ext_batch(const kb::E4 *poly, int k, const kb::E4 *eq_lo, int s_lo,
+                           const kb::E4 *eq_hi, size_t tab_stride, int batch,
+                           unsigned long long *acc, cudaStream_t st,
+                           const Publish &pub = Publish());
+// instance y: rows idx[off[y] .. off[y+1]) of its part of a batched codeword
+// (rows of 2^ks words) at its rs_b[y ks ..]
+cudaError_t row_evals_batch(const uint32_t *rows, int row_len, const uint32_t *idx,
+                            const int *off, int max_n, int ks, const kb::E4 *rs_b, int batch,
+                            kb::E4 *out, cudaStream_t st);
+// src: batch matrices of rows x w words back to back; dst: the batched
+// matrix (row r = row r of each instance in turn)
+cudaError_t interleave_rows(const uint32_t *src, size_t rows, size_t w, int batch, uint32_t *dst,
+                            cudaStream_t st);
+// the batched tree over batch * 2^log_h leaves up to the instances' roots:
+// level l (batch 2^(log_h - l) nodes) at batch * level_offset_words(log_h, l)
+cudaError_t build_tree_batch(uint32_t *nodes, int log_h, int batch, cudaStream_t st);
+// per query q: instance inst[q], index idx[q] of its codeword; out + q (row_len
+// + 8 log_h) gets the row then log_h sibling digests bottom-up
+cudaError_t gather_openings_batch(const uint32_t *rows, int row_len, const uint32_t *nodes,
+                                  int log_h, int batch, const uint32_t *idx, const int *inst,
+                                  int n, uint32_t *out, cudaStream_t st);
 
 }  // namespace gpu
 }  // namespace whir

@@ -202,9 +202,14 @@ __device__ __forceinline__ void p2q_permute(uint32_t (&x)[4], int l, const uint3
 // level by two launches per tree (G CTAs up to the level of G nodes, then one
 // CTA, G = 1, to the root), and each node is compressed by a quad of lanes.
 // Threads: 4 per node of the first level made (at most 1024).
+// A batched tree (kernels.h: batch instances' leaves interleaved) is the
+// same ascent over batch 2^log_h leaves: level l holds batch 2^(log_h - l)
+// nodes at batch * level_offset_words(log_h, l), and G is a multiple of
+// batch, so every subtree lies inside one instance.
 __global__ void __launch_bounds__(1024) tree_subtrees(uint32_t *__restrict__ nodes, int log_h,
                                                      int l0, int steps, uint32_t *host_root,
-                                                     unsigned int *flag, unsigned int seq) {
+                                                     unsigned int *flag, unsigned int seq,
+                                                     unsigned batch) {
   extern __shared__ uint4 sm[];  // 2 uint4 per node of this CTA's share
   __shared__ uint32_t kc[8 * 16 + 20];
   for (int i = threadIdx.x; i < 8 * 16 + 20; i += blockDim.x) kc[i] = c_p2_16[i];
@@ -213,8 +218,8 @@ __global__ void __launch_bounds__(1024) tree_subtrees(uint32_t *__restrict__ nod
 #pragma unroll
   for (int i = 0; i < 4; i++) dg[i] = c_p2_16[8 * 16 + 20 + 4 * l + i];
   const size_t G = gridDim.x, j = blockIdx.x;
-  int n = (int)(((size_t)1 << (log_h - l0)) / G);
-  const uint4 *src = reinterpret_cast<const uint4 *>(nodes + level_offset_words(log_h, l0));
+  int n = (int)(((size_t)batch << (log_h - l0)) / G);
+  const uint4 *src = reinterpret_cast<const uint4 *>(nodes + batch * level_offset_words(log_h, l0));
   for (int q = threadIdx.x; q < 2 * n; q += blockDim.x) sm[q] = src[(j + G * (q >> 1)) * 2 + (q & 1)];
   __syncthreads();
   for (int st = 0; st < steps; st++) {
@@ -230,7 +235,8 @@ __global__ void __launch_bounds__(1024) tree_subtrees(uint32_t *__restrict__ nod
       }
       p2q_permute(x, l, kc, dg);
       if (live && l < 2) {
-        uint4 *dst = reinterpret_cast<uint4 *>(nodes + level_offset_words(log_h, l0 + st + 1));
+        uint4 *dst =
+            reinterpret_cast<uint4 *>(nodes + batch * level_offset_words(log_h, l0 + st + 1));
         dst[(j + G * m) * 2 + l] = make_uint4(x[0], x[1], x[2], x[3]);
         if (host_root && G == 1 && half == 1) {  // the root, also to the host
 #pragma unroll
@@ -285,7 +291,7 @@ static cudaError_t launch_subtrees(uint32_t *nodes, int log_h, int l0, int log_g
   int n = 1 << steps;  // nodes per CTA at level l0
   int threads = 2 * n < 32 ? 32 : 2 * n;  // a quad per node made at the first step
   tree_subtrees<<<1u << log_g, threads, (size_t)n * 32, st>>>(nodes, log_h, l0, steps,
-                                                              host_root, flag, seq);
+                                                              host_root, flag, seq, 1u);
   count_launches(1);
   return cudaGetLastError();
 }
@@ -310,6 +316,105 @@ cudaError_t build_tree(uint32_t *nodes, int log_h, cudaStream_t st, uint32_t *ho
   cudaError_t e = launch_subtrees(nodes, log_h, l, log_g, st, host_root, flag, seq);
   if (e != cudaSuccess) return e;
   return launch_subtrees(nodes, log_h, log_h - log_g, 0, st, host_root, flag, seq);
+}
+
+// ---- batched trees (kernels.h) ----
+// Wide levels one thread per node, as build_tree; the remaining S levels up
+// to the instances' roots in two subtree launches: batch 2^g CTAs climb
+// S - g levels, then batch CTAs climb g (each CTA holds at most 512 nodes).
+cudaError_t build_tree_batch(uint32_t *nodes, int log_h, int batch, cudaStream_t st) {
+  if (batch < 1 || log_h < 0 || log_h > 30) return cudaErrorInvalidValue;
+  const int T = 128;
+  const size_t B = (size_t)batch;
+  int l = 0;
+  for (; l < log_h && (B << (log_h - l)) / 2 >= ((size_t)1 << 15); l++) {
+    size_t half = (B << (log_h - l)) / 2;
+    compress_level<<<(unsigned)((half + T - 1) / T), T, 0, st>>>(
+        nodes + B * level_offset_words(log_h, l), nodes + B * level_offset_words(log_h, l + 1),
+        half);
+    count_launches(1);
+  }
+  const int S = log_h - l;
+  if (S == 0) return cudaGetLastError();
+  int g = S / 2;
+  if (S - g > 9) g = S - 9;
+  if (g > 9 || (B << g) > 0x7fffffffu) return cudaErrorInvalidValue;
+  const int parts[2][2] = {{l, S - g}, {log_h - g, g}};  // (first level, steps)
+  for (int i = 0; i < 2; i++) {
+    const int l0 = parts[i][0], steps = parts[i][1];
+    if (steps == 0) continue;
+    const size_t G = B << (i == 0 ? g : 0);
+    const int n = 1 << steps;
+    const int threads = 2 * n < 32 ? 32 : 2 * n;
+    tree_subtrees<<<(unsigned)G, threads, (size_t)n * 32, st>>>(nodes, log_h, l0, steps, nullptr,
+                                                               nullptr, 0, (unsigned)batch);
+    count_launches(1);
+  }
+  return cudaGetLastError();
+}
+
+__global__ void gather_openings_batch_kernel(const uint32_t *__restrict__ rows, int row_len,
+                                             const uint32_t *__restrict__ nodes, int log_h,
+                                             unsigned batch, const uint32_t *__restrict__ idx,
+                                             const int *__restrict__ inst, int n,
+                                             uint32_t *__restrict__ out) {
+  const int q = blockIdx.x;
+  if (q >= n) return;
+  const size_t b = (size_t)inst[q], r = idx[q];
+  const size_t per = (size_t)row_len + 8 * (size_t)log_h;
+  uint32_t *o = out + q * per;
+  const uint32_t *row = rows + (r * batch + b) * row_len;
+  for (int j = threadIdx.x; j < row_len; j += blockDim.x) o[j] = row[j];
+  for (int t = threadIdx.x; t < 8 * log_h; t += blockDim.x) {
+    const int l = t / 8, w = t % 8;
+    const size_t at = r & (((size_t)1 << (log_h - l)) - 1);  // the instance's node at level l
+    const size_t sib = at ^ ((size_t)1 << (log_h - l - 1));
+    o[row_len + t] = nodes[batch * level_offset_words(log_h, l) + (sib * batch + b) * 8 + w];
+  }
+}
+
+cudaError_t gather_openings_batch(const uint32_t *rows, int row_len, const uint32_t *nodes,
+                                  int log_h, int batch, const uint32_t *idx, const int *inst,
+                                  int n, uint32_t *out, cudaStream_t st) {
+  if (n == 0) return cudaSuccess;
+  if (batch < 1) return cudaErrorInvalidValue;
+  gather_openings_batch_kernel<<<n, 128, 0, st>>>(rows, row_len, nodes, log_h, (unsigned)batch,
+                                                  idx, inst, n, out);
+  count_launches(1);
+  return cudaGetLastError();
+}
+
+// dst row r = (src row r of instance 0, of instance 1, ...): 16-byte
+// pieces when the row width allows, one thread per piece of dst
+template <class T>
+__global__ void interleave_kernel(const T *__restrict__ src, size_t rows, size_t w, size_t batch,
+                                  T *__restrict__ dst) {
+  const size_t total = rows * w * batch;
+  for (size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x; i < total;
+       i += (size_t)gridDim.x * blockDim.x) {
+    const size_t j = i % w, rb = i / w, b = rb % batch, r = rb / batch;
+    dst[i] = src[(b * rows + r) * w + j];
+  }
+}
+
+cudaError_t interleave_rows(const uint32_t *src, size_t rows, size_t w, int batch, uint32_t *dst,
+                            cudaStream_t st) {
+  if (batch < 1) return cudaErrorInvalidValue;
+  const size_t total = rows * w * (size_t)batch;
+  if (total == 0) return cudaSuccess;
+  const unsigned T = 256;
+  const bool vec = w % 4 == 0 && (((uintptr_t)src | (uintptr_t)dst) & 15) == 0;
+  const size_t items = vec ? total / 4 : total;
+  const size_t g = (items + T - 1) / T;
+  const unsigned grid = (unsigned)(g < 152 * 32 ? g : 152 * 32);
+  if (vec)
+    interleave_kernel<uint4><<<grid, T, 0, st>>>(reinterpret_cast<const uint4 *>(src), rows,
+                                                 w / 4, (size_t)batch,
+                                                 reinterpret_cast<uint4 *>(dst));
+  else
+    interleave_kernel<uint32_t><<<grid, T, 0, st>>>(src, rows, w, (size_t)batch, dst);
+  count_launches(1);
+  return cudaGetLastError();
 }
 
 __device__ __forceinline__ void gather_one(const uint32_t *__restrict__ rows, int row_len,

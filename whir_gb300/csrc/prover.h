@@ -81,6 +81,34 @@ class DeviceBuffer {
   size_t bytes_ = 0;
 };
 
+// page-locked host memory owned by one object
+class PinnedBuffer {
+ public:
+  PinnedBuffer() = default;
+  ~PinnedBuffer() {
+    if (p_) cudaFreeHost(p_);
+  }
+  PinnedBuffer(const PinnedBuffer &) = delete;
+  PinnedBuffer &operator=(const PinnedBuffer &) = delete;
+  void reserve(size_t bytes) {
+    if (bytes <= bytes_) return;
+    if (p_) cudaFreeHost(p_);
+    p_ = nullptr;
+    bytes_ = 0;
+    cuda_check(cudaMallocHost(&p_, bytes), "cudaMallocHost");
+    bytes_ = bytes;
+  }
+  uint8_t *data() const { return static_cast<uint8_t *>(p_); }
+  size_t bytes() const { return bytes_; }
+
+ private:
+  void *p_ = nullptr;
+  size_t bytes_ = 0;
+};
+
+// refuses parameter sets the reference cannot run (WhirError code -1)
+void check_params(const Params &p);
+
 // One device, one stream, the device tables and a pinned staging area.
 class Context {
  public:

@@ -39,14 +39,14 @@ __device__ __forceinline__ void st_e4(E4 *p, const E4 &a) {
 __host__ __forceinline__ bool aligned16(const void *p) { return ((uintptr_t)p & 15) == 0; }
 
 
-// eq table entries over z[off .. off+nv) times scale: entry b selects z_i
-// when bit i of b is set, 1 - z_i otherwise (Point::eq, point.rs:110-126).
 // Publish (kernels.h): after this CTA's atomics into acc, the last CTA of
 // the launch copies the sums out and zeroes them.  Every thread of the CTA
-// calls it.
+// calls it.  acc is the accumulator base of the whole launch (every instance
+// of a batched launch, blockIdx.y, publishes from the same base).
 __device__ __forceinline__ void publish_if_last(unsigned long long *acc, const Publish &pub) {
   if (!pub.host) return;
-  if (gridDim.x == 1) {
+  const unsigned ncta = gridDim.x * gridDim.y;
+  if (ncta == 1) {
     // the only CTA is the last: its atomics on acc precede the exchanges
     // below in the same memory location's order, no ticket or fence needed
     __syncthreads();
@@ -54,13 +54,13 @@ __device__ __forceinline__ void publish_if_last(unsigned long long *acc, const P
     __shared__ bool last;
     __threadfence();  // this CTA's atomics are visible before its ticket
     __syncthreads();
-    if (threadIdx.x == 0) last = atomicAdd(pub.counter, 1u) == gridDim.x - 1;
+    if (threadIdx.x == 0) last = atomicAdd(pub.counter, 1u) == ncta - 1;
     __syncthreads();
     if (!last) return;
     __threadfence();
   }
   for (int i = threadIdx.x; i < pub.words; i += blockDim.x) pub.host[i] = atomicExch(acc + i, 0ull);
-  if (threadIdx.x == 0 && gridDim.x > 1) atomicExch(pub.counter, 0u);
+  if (threadIdx.x == 0 && ncta > 1) atomicExch(pub.counter, 0u);
   if (pub.flag) {
     __threadfence_system();  // the results reach host memory before the flag
     __syncthreads();
@@ -68,6 +68,8 @@ __device__ __forceinline__ void publish_if_last(unsigned long long *acc, const P
   }
 }
 
+// eq table entries over z[off .. off+nv) times scale: entry b selects z_i
+// when bit i of b is set, 1 - z_i otherwise (Point::eq, point.rs:110-126).
 __global__ void eq_entries(Point z, int off, int nv, E4 scale, E4 *out) {
   size_t b = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (b >= ((size_t)1 << nv)) return;
@@ -212,8 +214,12 @@ __global__ void __launch_bounds__(CH_T, 4) compress_hi_kernel(const uint32_t *__
                                                               int s_lo,
                                                               const E4 *__restrict__ eq_hi,
                                                               unsigned long long *acc,
-                                                              Publish pub) {
+                                                              Publish pub, HiStrides sd) {
   extern __shared__ unsigned char smraw[];
+  poly += blockIdx.y * sd.poly;
+  eq_lo += blockIdx.y * sd.tab;
+  eq_hi += blockIdx.y * sd.tab;
+  unsigned long long *const acc_y = acc + blockIdx.y * sd.acc;
   E4 *lo = reinterpret_cast<E4 *>(smraw);
   unsigned long long *part = reinterpret_cast<unsigned long long *>(lo + ((size_t)1 << s_lo));
   const int W = 1 << ks;
@@ -262,7 +268,7 @@ __global__ void __launch_bounds__(CH_T, 4) compress_hi_kernel(const uint32_t *__
     for (int c = 0; c < 4; c++) atomicAdd(part + j * 4 + c, (unsigned long long)outer.c[c]);
   }
   __syncthreads();
-  for (int i = tid; i < W * 4; i += CH_T) atomicAdd(acc + i, part[i]);
+  for (int i = tid; i < W * 4; i += CH_T) atomicAdd(acc_y + i, part[i]);
   publish_if_last(acc, pub);
 }
 
@@ -277,8 +283,12 @@ __device__ __forceinline__ unsigned long long ch_fold(unsigned long long x) {
 }
 __global__ void __launch_bounds__(CH_T, 3) compress_hi_pipe_kernel(
     const uint32_t *__restrict__ poly, int k, int ks, const E4 *__restrict__ eq_lo, int s_lo,
-    const E4 *__restrict__ eq_hi, unsigned long long *acc, Publish pub) {
+    const E4 *__restrict__ eq_hi, unsigned long long *acc, Publish pub, HiStrides sd) {
   extern __shared__ unsigned char smraw[];
+  poly += blockIdx.y * sd.poly;
+  eq_lo += blockIdx.y * sd.tab;
+  eq_hi += blockIdx.y * sd.tab;
+  unsigned long long *const acc_y = acc + blockIdx.y * sd.acc;
   E4 *lo = reinterpret_cast<E4 *>(smraw);
   unsigned long long *part = reinterpret_cast<unsigned long long *>(lo + ((size_t)1 << s_lo));
   const int W = 1 << ks;
@@ -339,37 +349,53 @@ __global__ void __launch_bounds__(CH_T, 3) compress_hi_pipe_kernel(
     for (int c = 0; c < 4; c++) atomicAdd(part + j * 4 + c, (unsigned long long)outer.c[c]);
   }
   __syncthreads();
-  for (int i = tid; i < W * 4; i += CH_T) atomicAdd(acc + i, part[i]);
+  for (int i = tid; i < W * 4; i += CH_T) atomicAdd(acc_y + i, part[i]);
   publish_if_last(acc, pub);
 }
 
 cudaError_t compress_hi(const uint32_t *poly, int k, int ks, const E4 *eq_lo, int s_lo,
                         const E4 *eq_hi, unsigned long long *acc, cudaStream_t st,
                         const Publish &pub) {
-  if ((1 << ks) > CH_T || k < ks + s_lo) return cudaErrorInvalidValue;
+  return compress_hi_batch(poly, k, ks, eq_lo, s_lo, eq_hi, acc, 1, HiStrides(), st, pub);
+}
+
+cudaError_t compress_hi_batch(const uint32_t *poly, int k, int ks, const E4 *eq_lo, int s_lo,
+                              const E4 *eq_hi, unsigned long long *acc, int batch,
+                              const HiStrides &sd, cudaStream_t st, const Publish &pub) {
+  if ((1 << ks) > CH_T || k < ks + s_lo || batch < 1 || batch > 65535)
+    return cudaErrorInvalidValue;
   size_t n_hi = (size_t)1 << (k - ks - s_lo);
-  unsigned grid = (unsigned)(n_hi < 152 * 4 ? n_hi : 152 * 4);
+  // about four (three) CTAs per SM over all instances
+  const size_t per4 = ((size_t)152 * 4 + batch - 1) / batch, per3 = ((size_t)152 * 3 + batch - 1) / batch;
+  dim3 grid((unsigned)(n_hi < per4 ? n_hi : per4), (unsigned)batch);
   size_t smem = ((size_t)1 << s_lo) * sizeof(E4) + ((size_t)4 << ks) * 8;
   if (((size_t)1 << (ks + s_lo)) == 16 * (size_t)CH_T) {
-    grid = (unsigned)(n_hi < 152 * 3 ? n_hi : 152 * 3);
-    compress_hi_pipe_kernel<<<grid, CH_T, smem, st>>>(poly, k, ks, eq_lo, s_lo, eq_hi, acc, pub);
+    grid.x = (unsigned)(n_hi < per3 ? n_hi : per3);
+    compress_hi_pipe_kernel<<<grid, CH_T, smem, st>>>(poly, k, ks, eq_lo, s_lo, eq_hi, acc, pub, sd);
   } else {
-    compress_hi_kernel<<<grid, CH_T, smem, st>>>(poly, k, ks, eq_lo, s_lo, eq_hi, acc, pub);
+    compress_hi_kernel<<<grid, CH_T, smem, st>>>(poly, k, ks, eq_lo, s_lo, eq_hi, acc, pub, sd);
   }
   count_launches(1);
   return cudaGetLastError();
 }
 
-// compress_lo: out[i] = sum_j eq(rs)[j] * P[i * 2^ks + j]
+// compress_lo: out[i] = sum_j eq(rs)[j] * P[i * 2^ks + j].  Batched:
+// instance y = blockIdx.y reads poly + y poly_stride with its own rs
+// (rs_b[y ks ..], ks extension elements) and writes out + y n_out.
 template <bool VEC>
 __global__ void compress_lo_kernel(const uint32_t *__restrict__ poly, int ks, size_t n_out,
-                                   Point rs, E4 *__restrict__ out) {
+                                   Point rs, const E4 *__restrict__ rs_b, size_t poly_stride,
+                                   E4 *__restrict__ out) {
   __shared__ E4 eq[256];
   const int W = 1 << ks;
+  poly += blockIdx.y * poly_stride;
+  out += blockIdx.y * n_out;
   for (int b = threadIdx.x; b < W; b += blockDim.x) {
     E4 acc = kb::e_one();
-    for (int i = 0; i < ks; i++)
-      acc = kb::e_mul(acc, ((b >> i) & 1) ? rs.z[i] : kb::e_sub(kb::e_one(), rs.z[i]));
+    for (int i = 0; i < ks; i++) {
+      const E4 zi = rs_b ? rs_b[(size_t)blockIdx.y * ks + i] : rs.z[i];
+      acc = kb::e_mul(acc, ((b >> i) & 1) ? zi : kb::e_sub(kb::e_one(), zi));
+    }
     eq[b] = acc;
   }
   __syncthreads();
@@ -392,25 +418,43 @@ __global__ void compress_lo_kernel(const uint32_t *__restrict__ poly, int ks, si
   }
 }
 
-cudaError_t compress_lo(const uint32_t *poly, int k, const Point &rs, E4 *out, cudaStream_t st) {
-  int ks = rs.k;
-  if (ks > 8 || ks > k) return cudaErrorInvalidValue;
+static cudaError_t compress_lo_launch(const uint32_t *poly, int k, int ks, const Point &rs,
+                                      const E4 *rs_b, int batch, size_t poly_stride, E4 *out,
+                                      cudaStream_t st) {
+  if (ks > 8 || ks > k || batch < 1 || batch > 65535) return cudaErrorInvalidValue;
   size_t n_out = (size_t)1 << (k - ks);
   unsigned T = 256;
-  size_t g = (n_out + T - 1) / T;
-  unsigned grid = (unsigned)(g < 152 * 16 ? g : 152 * 16);
-  if (ks >= 2 && aligned16(poly) && aligned16(out))
-    compress_lo_kernel<true><<<grid, T, 0, st>>>(poly, ks, n_out, rs, out);
+  size_t g = (n_out + T - 1) / T, cap = ((size_t)152 * 16 + batch - 1) / batch;
+  dim3 grid((unsigned)(g < cap ? g : cap), (unsigned)batch);
+  const bool vec = ks >= 2 && aligned16(poly) && aligned16(out) &&
+                   (batch == 1 || poly_stride % 4 == 0);
+  if (vec)
+    compress_lo_kernel<true><<<grid, T, 0, st>>>(poly, ks, n_out, rs, rs_b, poly_stride, out);
   else
-    compress_lo_kernel<false><<<grid, T, 0, st>>>(poly, ks, n_out, rs, out);
+    compress_lo_kernel<false><<<grid, T, 0, st>>>(poly, ks, n_out, rs, rs_b, poly_stride, out);
   count_launches(1);
   return cudaGetLastError();
 }
 
-// w[i] += sum_t lo_t[i & mask] * hi_t[i >> s]
+cudaError_t compress_lo(const uint32_t *poly, int k, const Point &rs, E4 *out, cudaStream_t st) {
+  return compress_lo_launch(poly, k, rs.k, rs, nullptr, 1, 0, out, st);
+}
+
+cudaError_t compress_lo_batch(const uint32_t *poly, int k, int ks, const E4 *rs_b, int batch,
+                              size_t poly_stride, E4 *out, cudaStream_t st) {
+  Point none;
+  none.k = ks;
+  return compress_lo_launch(poly, k, ks, none, rs_b, batch, poly_stride, out, st);
+}
+
+// w[i] += sum_t lo_t[i & mask] * hi_t[i >> s].  Batched: instance y =
+// blockIdx.y adds its n_tables tables (stored after those of instances < y)
+// into w + y n.
 template <bool VEC>
 __global__ void add_eq_kernel(E4 *w, size_t n, int s, size_t n_lo, size_t n_hi,
                               const E4 *__restrict__ tables, int n_tables) {
+  w += blockIdx.y * n;
+  tables += blockIdx.y * (size_t)n_tables * (n_lo + n_hi);
   for (size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x; i < n;
        i += (size_t)gridDim.x * blockDim.x) {
     E4 acc = ld_e4<VEC>(w + i);
@@ -422,13 +466,15 @@ __global__ void add_eq_kernel(E4 *w, size_t n, int s, size_t n_lo, size_t n_hi,
   }
 }
 
-cudaError_t add_eq(E4 *w, int k, const E4 *tables, int n_tables, cudaStream_t st) {
+cudaError_t add_eq_batch(E4 *w, int k, const E4 *tables, int n_tables, int batch,
+                         cudaStream_t st) {
   if (n_tables == 0) return cudaSuccess;
+  if (batch < 1 || batch > 65535) return cudaErrorInvalidValue;
   int s = k / 2;
   size_t n = (size_t)1 << k;
   unsigned T = 256;
-  size_t g = (n + T - 1) / T;
-  unsigned grid = (unsigned)(g < 152 * 16 ? g : 152 * 16);
+  size_t g = (n + T - 1) / T, cap = ((size_t)152 * 16 + batch - 1) / batch;
+  dim3 grid((unsigned)(g < cap ? g : cap), (unsigned)batch);
   if (aligned16(w) && aligned16(tables))
     add_eq_kernel<true><<<grid, T, 0, st>>>(w, n, s, (size_t)1 << s, (size_t)1 << (k - s),
                                             tables, n_tables);
@@ -437,6 +483,10 @@ cudaError_t add_eq(E4 *w, int k, const E4 *tables, int n_tables, cudaStream_t st
                                              tables, n_tables);
   count_launches(1);
   return cudaGetLastError();
+}
+
+cudaError_t add_eq(E4 *w, int k, const E4 *tables, int n_tables, cudaStream_t st) {
+  return add_eq_batch(w, k, tables, n_tables, 1, st);
 }
 
 // var_t^i = lo_t[i mod 2^s] * hi_t[i >> s]: per var, 2^s low powers then
@@ -592,10 +642,44 @@ cudaError_t add_pows(E4 *w, int k, const uint32_t *vars, const E4 *scales, int n
   return cudaGetLastError();
 }
 
-// block-wide sum of E4 values into 64-bit accumulators
+// Batched and ragged: instance y = blockIdx.y adds the variables
+// off[y] .. off[y+1] of the flat arrays (their power tables at the same
+// positions of tab) into w + y 2^k.
+template <bool VEC>
+__global__ void add_pows_batch_kernel(E4 *__restrict__ w, size_t n_out, int s,
+                                      const int *__restrict__ off,
+                                      const uint32_t *__restrict__ tab,
+                                      const E4 *__restrict__ scales) {
+  const int y = blockIdx.y, o = off[y], n = off[y + 1] - o;
+  const size_t per = ((size_t)1 << s) + (n_out >> s);
+  add_pows_body<VEC>(w + (size_t)y * n_out, n_out, s, n, tab + (size_t)o * per,
+                     ScalePtr{scales + o});
+}
+
+cudaError_t add_pows_batch(E4 *w, int k, const uint32_t *vars, const E4 *scales, const int *off,
+                           int n_total, int max_n, int batch, uint32_t *tab, cudaStream_t st) {
+  if (n_total == 0) return cudaSuccess;
+  const size_t smem = add_pows_smem(k, max_n);
+  if (smem > 48 * 1024 || batch < 1 || batch > 65535) return cudaErrorInvalidValue;
+  int s = k / 2;
+  size_t words = add_pows_scratch_words(k, n_total);
+  pow_tables_kernel<<<(unsigned)((words + 255) / 256), 256, 0, st>>>(vars, n_total, s, k, tab);
+  count_launches(1);
+  size_t N = (size_t)1 << k;
+  dim3 grid((unsigned)((N + AP_T - 1) / AP_T), (unsigned)batch);
+  if (aligned16(w))
+    add_pows_batch_kernel<true><<<grid, AP_T, smem, st>>>(w, N, s, off, tab, scales);
+  else
+    add_pows_batch_kernel<false><<<grid, AP_T, smem, st>>>(w, N, s, off, tab, scales);
+  count_launches(1);
+  return cudaGetLastError();
+}
+
+// block-wide sum of E4 values into 64-bit accumulators at acc; acc_base is
+// the launch's accumulator base for publishing (acc itself when unbatched)
 template <int NV>
 __device__ __forceinline__ void block_acc(const E4 (&v)[NV], unsigned long long *acc,
-                                          const Publish &pub) {
+                                          unsigned long long *acc_base, const Publish &pub) {
   __shared__ unsigned long long part[NV * 4];
   for (int i = threadIdx.x; i < NV * 4; i += blockDim.x) part[i] = 0;
   __syncthreads();
@@ -611,17 +695,30 @@ __device__ __forceinline__ void block_acc(const E4 (&v)[NV], unsigned long long 
     }
   __syncthreads();
   for (int i = threadIdx.x; i < NV * 4; i += blockDim.x) atomicAdd(acc + i, part[i]);
-  publish_if_last(acc, pub);
+  publish_if_last(acc_base, pub);
 }
 
 // One round: new[i] = a[2i] + r (a[2i+1] - a[2i]) for poly and weights (when
 // folding), then c0 += w[2m] p[2m], c2 += (2 w[2m+1] - w[2m]) (2 p[2m+1] - p[2m]).
+// Batched: instance y = blockIdx.y has its arrays at y n_in (inputs) and
+// y n_in / 2 (outputs), its challenge at r_b[y] and its sums at
+// acc + y acc_stride.
 template <bool VEC>
 __global__ void __launch_bounds__(256) round_kernel(const E4 *__restrict__ p_in,
                                                     const E4 *__restrict__ w_in, size_t n_in,
                                                     int fold, E4 r, E4 *__restrict__ p_out,
                                                     E4 *__restrict__ w_out, int coeffs,
-                                                    unsigned long long *acc, Publish pub) {
+                                                    unsigned long long *acc, Publish pub,
+                                                    const E4 *__restrict__ r_b,
+                                                    size_t acc_stride) {
+  p_in += blockIdx.y * n_in;
+  w_in += blockIdx.y * n_in;
+  if (fold) {
+    p_out += blockIdx.y * (n_in / 2);
+    w_out += blockIdx.y * (n_in / 2);
+    if (r_b) r = r_b[blockIdx.y];
+  }
+  unsigned long long *const acc_y = acc + blockIdx.y * acc_stride;
   size_t n = fold ? n_in / 2 : n_in;
   size_t pairs = (n + 1) / 2;
   E4 sums[2] = {kb::e_zero(), kb::e_zero()};
@@ -658,36 +755,62 @@ __global__ void __launch_bounds__(256) round_kernel(const E4 *__restrict__ p_in,
       sums[1] = kb::e_add(sums[1], kb::e_mul(dw, dp));
     }
   }
-  if (coeffs) block_acc<2>(sums, acc, pub);
+  if (coeffs) block_acc<2>(sums, acc_y, acc, pub);
+}
+
+static cudaError_t round_launch(const E4 *p_in, const E4 *w_in, size_t n_in, bool fold, E4 r,
+                                const E4 *r_b, E4 *p_out, E4 *w_out, bool coeffs,
+                                unsigned long long *acc, size_t acc_stride, int batch,
+                                cudaStream_t st, const Publish &pub) {
+  if (batch < 1 || batch > 65535) return cudaErrorInvalidValue;
+  size_t n = fold ? n_in / 2 : n_in;
+  size_t pairs = (n + 1) / 2;
+  unsigned T = 256;
+  size_t g = (pairs + T - 1) / T, cap = ((size_t)152 * 4 + batch - 1) / batch;
+  dim3 grid((unsigned)(g < cap ? (g ? g : 1) : cap), (unsigned)batch);
+  const bool vec = aligned16(p_in) && aligned16(w_in) &&
+                   (!fold || (aligned16(p_out) && aligned16(w_out)));
+  if (vec)
+    round_kernel<true><<<grid, T, 0, st>>>(p_in, w_in, n_in, fold ? 1 : 0, r, p_out, w_out,
+                                           coeffs ? 1 : 0, acc, coeffs ? pub : Publish(), r_b,
+                                           acc_stride);
+  else
+    round_kernel<false><<<grid, T, 0, st>>>(p_in, w_in, n_in, fold ? 1 : 0, r, p_out, w_out,
+                                            coeffs ? 1 : 0, acc, coeffs ? pub : Publish(), r_b,
+                                            acc_stride);
+  count_launches(1);
+  return cudaGetLastError();
 }
 
 cudaError_t sumcheck_round(const E4 *p_in, const E4 *w_in, size_t n_in, bool fold, E4 r,
                            E4 *p_out, E4 *w_out, bool coeffs, unsigned long long *acc,
                            cudaStream_t st, const Publish &pub) {
-  size_t n = fold ? n_in / 2 : n_in;
-  size_t pairs = (n + 1) / 2;
-  unsigned T = 256;
-  size_t g = (pairs + T - 1) / T;
-  unsigned grid = (unsigned)(g < 152 * 4 ? (g ? g : 1) : 152 * 4);
-  const bool vec = aligned16(p_in) && aligned16(w_in) &&
-                   (!fold || (aligned16(p_out) && aligned16(w_out)));
-  if (vec)
-    round_kernel<true><<<grid, T, 0, st>>>(p_in, w_in, n_in, fold ? 1 : 0, r, p_out, w_out,
-                                           coeffs ? 1 : 0, acc, coeffs ? pub : Publish());
-  else
-    round_kernel<false><<<grid, T, 0, st>>>(p_in, w_in, n_in, fold ? 1 : 0, r, p_out, w_out,
-                                            coeffs ? 1 : 0, acc, coeffs ? pub : Publish());
-  count_launches(1);
-  return cudaGetLastError();
+  return round_launch(p_in, w_in, n_in, fold, r, nullptr, p_out, w_out, coeffs, acc, 0, 1, st,
+                      pub);
 }
 
-// <eq(z), poly>: CTA walks hi blocks of 2^s_lo contiguous entries
+cudaError_t sumcheck_round_batch(const E4 *p_in, const E4 *w_in, size_t n_in, bool fold,
+                                 const E4 *r_b, E4 *p_out, E4 *w_out, bool coeffs,
+                                 unsigned long long *acc, size_t acc_stride, int batch,
+                                 cudaStream_t st, const Publish &pub) {
+  if (fold && !r_b) return cudaErrorInvalidValue;
+  return round_launch(p_in, w_in, n_in, fold, kb::e_zero(), r_b, p_out, w_out, coeffs, acc,
+                      acc_stride, batch, st, pub);
+}
+
+// <eq(z), poly>: CTA walks hi blocks of 2^s_lo contiguous entries.
+// Batched: instance y = blockIdx.y reads poly + y 2^k, its tables at
+// y tab_stride from eq_lo and eq_hi, and sums into acc + 4 y.
 template <bool VEC>
 __global__ void __launch_bounds__(256) eval_ext_kernel(const E4 *__restrict__ poly, int k,
                                                        const E4 *__restrict__ eq_lo, int s_lo,
                                                        const E4 *__restrict__ eq_hi,
-                                                       unsigned long long *acc, Publish pub) {
+                                                       unsigned long long *acc, Publish pub,
+                                                       size_t tab_stride) {
   size_t n_lo = (size_t)1 << s_lo, n_hi = (size_t)1 << (k - s_lo);
+  poly += blockIdx.y * ((size_t)1 << k);
+  eq_lo += blockIdx.y * tab_stride;
+  eq_hi += blockIdx.y * tab_stride;
   E4 outer = kb::e_zero();
   for (size_t hh = blockIdx.x; hh < n_hi; hh += gridDim.x) {
     E4 inner = kb::e_zero();
@@ -696,34 +819,51 @@ __global__ void __launch_bounds__(256) eval_ext_kernel(const E4 *__restrict__ po
     outer = kb::e_add(outer, kb::e_mul(inner, ld_e4<VEC>(eq_hi + hh)));
   }
   E4 v[1] = {outer};
-  block_acc<1>(v, acc, pub);
+  block_acc<1>(v, acc + 4 * (size_t)blockIdx.y, acc, pub);
 }
 
-cudaError_t eval_ext(const E4 *poly, int k, const E4 *eq_lo, int s_lo, const E4 *eq_hi,
-                     unsigned long long *acc, cudaStream_t st, const Publish &pub) {
-  size_t n_hi = (size_t)1 << (k - s_lo);
-  unsigned grid = (unsigned)(n_hi < 152 * 8 ? n_hi : 152 * 8);
+cudaError_t eval_ext_batch(const E4 *poly, int k, const E4 *eq_lo, int s_lo, const E4 *eq_hi,
+                           size_t tab_stride, int batch, unsigned long long *acc,
+                           cudaStream_t st, const Publish &pub) {
+  if (batch < 1 || batch > 65535 || s_lo > k) return cudaErrorInvalidValue;
+  size_t n_hi = (size_t)1 << (k - s_lo), cap = ((size_t)152 * 8 + batch - 1) / batch;
+  dim3 grid((unsigned)(n_hi < cap ? n_hi : cap), (unsigned)batch);
   if (aligned16(poly) && aligned16(eq_lo) && aligned16(eq_hi))
-    eval_ext_kernel<true><<<grid, 256, 0, st>>>(poly, k, eq_lo, s_lo, eq_hi, acc, pub);
+    eval_ext_kernel<true><<<grid, 256, 0, st>>>(poly, k, eq_lo, s_lo, eq_hi, acc, pub, tab_stride);
   else
-    eval_ext_kernel<false><<<grid, 256, 0, st>>>(poly, k, eq_lo, s_lo, eq_hi, acc, pub);
+    eval_ext_kernel<false><<<grid, 256, 0, st>>>(poly, k, eq_lo, s_lo, eq_hi, acc, pub, tab_stride);
   count_launches(1);
   return cudaGetLastError();
 }
 
+cudaError_t eval_ext(const E4 *poly, int k, const E4 *eq_lo, int s_lo, const E4 *eq_hi,
+                     unsigned long long *acc, cudaStream_t st, const Publish &pub) {
+  return eval_ext_batch(poly, k, eq_lo, s_lo, eq_hi, 0, 1, acc, st, pub);
+}
+
+// Batched: instance y = blockIdx.y evaluates rows idx[off[y] .. off[y+1])
+// of its own codeword, which is interleaved with the others' (row r of
+// instance y is row r batch + y of rows), at its own rs (rs_b[y ks ..]).
 __global__ void row_evals_kernel(const uint32_t *__restrict__ rows, int row_len,
-                                 const uint32_t *__restrict__ idx, int n, Point rs, E4 *out) {
+                                 const uint32_t *__restrict__ idx, int n, Point rs,
+                                 const int *__restrict__ off, const E4 *__restrict__ rs_b,
+                                 int batch, E4 *out) {
   __shared__ E4 eq[256];
+  const int y = blockIdx.y;
   for (int b = threadIdx.x; b < row_len; b += blockDim.x) {
     E4 a = kb::e_one();
-    for (int i = 0; i < rs.k; i++)
-      a = kb::e_mul(a, ((b >> i) & 1) ? rs.z[i] : kb::e_sub(kb::e_one(), rs.z[i]));
+    for (int i = 0; i < rs.k; i++) {
+      const E4 zi = rs_b ? rs_b[(size_t)y * rs.k + i] : rs.z[i];
+      a = kb::e_mul(a, ((b >> i) & 1) ? zi : kb::e_sub(kb::e_one(), zi));
+    }
     eq[b] = a;
   }
   __syncthreads();
   int q = blockIdx.x * blockDim.x + threadIdx.x;
-  if (q >= n) return;
-  const uint32_t *row = rows + (size_t)idx[q] * row_len;
+  const int q0 = off ? off[y] : 0, nq = off ? off[y + 1] - q0 : n;
+  if (q >= nq) return;
+  q += q0;
+  const uint32_t *row = rows + ((size_t)idx[q] * batch + y) * row_len;
   E4 a = kb::e_zero();
   for (int j = 0; j < row_len; j++) a = kb::e_add(a, kb::e_scale(eq[j], row[j]));
   out[q] = a;
@@ -733,7 +873,22 @@ cudaError_t row_evals(const uint32_t *rows, int row_len, const uint32_t *idx, in
                       const Point &rs, E4 *out, cudaStream_t st) {
   if (n == 0) return cudaSuccess;
   if (row_len > 256 || (1 << rs.k) != row_len) return cudaErrorInvalidValue;
-  row_evals_kernel<<<(n + 127) / 128, 128, 0, st>>>(rows, row_len, idx, n, rs, out);
+  row_evals_kernel<<<(n + 127) / 128, 128, 0, st>>>(rows, row_len, idx, n, rs, nullptr, nullptr,
+                                                    1, out);
+  count_launches(1);
+  return cudaGetLastError();
+}
+
+cudaError_t row_evals_batch(const uint32_t *rows, int row_len, const uint32_t *idx,
+                            const int *off, int max_n, int ks, const E4 *rs_b, int batch,
+                            E4 *out, cudaStream_t st) {
+  if (max_n == 0) return cudaSuccess;
+  if (row_len > 256 || (1 << ks) != row_len || batch < 1 || batch > 65535)
+    return cudaErrorInvalidValue;
+  Point rs;
+  rs.k = ks;
+  dim3 grid((unsigned)((max_n + 127) / 128), (unsigned)batch);
+  row_evals_kernel<<<grid, 128, 0, st>>>(rows, row_len, idx, 0, rs, off, rs_b, batch, out);
   count_launches(1);
   return cudaGetLastError();
 }
@@ -814,7 +969,9 @@ __device__ __forceinline__ void code_round_query(CodeState s, int round, E4 r_pr
 
 __global__ void __launch_bounds__(32) code_round_kernel(CodeState s, int round, E4 r_prev,
                                                         unsigned long long *acc, Publish pub) {
-  code_round_query(s, round, r_prev, acc);
+  const int b = s.inst ? s.inst[blockIdx.x] : 0;
+  if (s.r_b && round > 0) r_prev = s.r_b[b];
+  code_round_query(s, round, r_prev, acc + (size_t)b * s.acc_stride);
   publish_if_last(acc, pub);
 }
 
@@ -823,6 +980,7 @@ __global__ void code_finish_kernel(CodeState s, E4 r_last) {
   using namespace kb;
   int i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= s.n) return;
+  if (s.r_b) r_last = s.r_b[s.inst[i]];
   uint32_t ws = s.ws[i];
   E4 f = e_add(e_one(), e_mul(r_last, e_add(e_neg(e_one()), e_from(ws))));
   s.scales[i] = e_mul(s.scales[i], f);
