@@ -243,6 +243,13 @@ WHIR_API int whir_server_new(int device, int n_workers, uint64_t device_budget,
                              whir_server **out);
 WHIR_API int whir_server_run(whir_server *s, whir_job *jobs, int n_jobs, int honor_arrival,
                              whir_run_stats *stats);
+/* Lock-step groups: a worker that takes a job also takes the jobs of the
+ * same shape (parameters, claim count, commit-only, input memory) that have
+ * arrived, and proves them together as whir_prove_batch does, every pass of
+ * the group in one launch.  max_group bounds a group (1: every job alone;
+ * 0: the default, 256); a group also holds at most 2^26 evaluations in all
+ * and shrinks to fit the device budget.  Proof bytes do not change. */
+WHIR_API int whir_server_set_lockstep(whir_server *s, int max_group);
 WHIR_API int whir_server_free(whir_server *s);
 /* one-shot forms on a temporary pool */
 WHIR_API int whir_batch_prove(int device, whir_job *jobs, int n_jobs, int n_workers,
@@ -260,6 +267,15 @@ WHIR_API int whir_serve_simulate(const double *arrival_s, const uint64_t *need,
                                  const double *duration_s, int n_jobs, int n_workers,
                                  uint64_t device_budget, double *start_s, double *done_s,
                                  int32_t *worker, int32_t *status);
+/* The same with lock-step groups (whir_server_set_lockstep): jobs of equal
+ * shape[j] that have arrived are taken together, up to max_group; a group
+ * holds its size times its first job's need and takes its first job's
+ * duration.  Host only. */
+WHIR_API int whir_serve_simulate_groups(const double *arrival_s, const uint64_t *need,
+                                        const double *duration_s, const int32_t *shape,
+                                        int max_group, int n_jobs, int n_workers,
+                                        uint64_t device_budget, double *start_s, double *done_s,
+                                        int32_t *worker, int32_t *status);
 
 /* ---- allocation-free SVO compression.  No counterpart in the reference:
  * an extra entry point for callers that must not allocate device memory (a

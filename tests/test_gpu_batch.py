@@ -184,3 +184,25 @@ def test_workspace_plan_covers_a_proof(oracle, params, n):
     _, peak = W.prove_jobs([j], workers=1)
     assert j.status == 0
     assert peak <= W.workspace_bytes(params)
+
+
+@pytest.mark.parametrize("lockstep", [1, 3, 0])
+def test_server_lockstep_groups_match_alone(ctx, oracle, lockstep):
+    # many jobs of a few shapes released together: with lock step the server
+    # proves same-shape jobs as groups (at most 3 per group, or the default),
+    # without it one at a time; every proof equals the job proved alone
+    rng = np.random.default_rng(40 + lockstep)
+    jobs = []
+    for i in range(20):
+        k = int(rng.choice([10, 12]))
+        claims = int(rng.choice([1, 2]))
+        jobs.append(W.Job((k, 4, 1, 1, 1, 100), oracle.rand_fe(5000 + i, 1 << k), claims=claims,
+                          commit_only=(i % 9 == 4)))
+    srv = W.Server(workers=3, lockstep=lockstep)
+    try:
+        srv.run(jobs)
+    finally:
+        srv.close()
+    for j in jobs:
+        assert j.status == 0
+        assert (j.proof, j.checkpoint) == alone(ctx, j)

@@ -116,3 +116,60 @@ def test_short_polynomial_buffers_are_refused_before_the_library():
     assert W.Whir._polys([np.zeros(128, np.uint32), np.zeros(64, np.uint32)], [7, 6])[1] == 0
     with pytest.raises(W.WhirError):
         W._jobs_in([W.Job((12, 4, 1, 1, 1, 100), FakeDev(4 << 11))])
+
+
+# ---- lock-step groups (whir_server_set_lockstep's admission) ----
+
+def test_groups_take_arrived_jobs_of_one_shape():
+    # eight jobs at t = 0: shapes 0,1,0,1,...; two workers, groups up to 4
+    n = 8
+    shape = [i % 2 for i in range(n)]
+    s, e, wk, st = W.serve_simulate([0.0] * n, [1] * n, [0.03] * n, 2, 10 ** 9,
+                                    shape=shape, max_group=4)
+    assert (st == 0).all()
+    for sh in (0, 1):
+        members = [i for i in range(n) if shape[i] == sh]
+        assert len({wk[i] for i in members}) == 1          # one worker per group
+        assert np.ptp(s[members]) < 1e-3                   # started together
+        assert np.ptp(e[members]) < 1e-3
+    assert e.max() < 0.03 + 0.02                            # two groups side by side
+
+
+def test_groups_respect_max_group_and_arrival():
+    # 6 same-shape jobs at t = 0, one worker, groups of at most 4: the first
+    # four together, then the last two; a job arriving later is not pulled in
+    arrival = [0.0] * 6 + [0.2]
+    s, e, wk, st = W.serve_simulate(arrival, [1] * 7, [0.02] * 7, 1, 10 ** 9,
+                                    shape=[0] * 7, max_group=4)
+    assert (st == 0).all()
+    assert np.ptp(s[:4]) < 1e-3 and np.ptp(s[4:6]) < 1e-3
+    assert s[4] >= e[0] - 1e-3
+    assert s[6] >= 0.2 - 1e-4 and s[6] > e[5] - 1e-3
+
+
+def test_groups_halve_to_fit_the_budget():
+    # a group of 4 would hold 4 units; the budget holds 2: groups of 2
+    n = 4
+    s, e, wk, st = W.serve_simulate([0.0] * n, [1] * n, [0.02] * n, 1, 2,
+                                    shape=[0] * n, max_group=4)
+    assert (st == 0).all()
+    assert np.ptp(s[:2]) < 1e-3 and np.ptp(s[2:]) < 1e-3
+    assert s[2] >= e[0] - 1e-3
+
+
+def test_groups_keep_heads_in_arrival_order():
+    rng = np.random.default_rng(11)
+    n = 40
+    arrival = np.sort(rng.uniform(0, 0.05, n))
+    shape = rng.integers(0, 3, n)
+    s, e, wk, st = W.serve_simulate(arrival, [1] * n, rng.uniform(0.001, 0.005, n), 3, 10 ** 9,
+                                    shape=shape, max_group=8)
+    assert (st == 0).all()
+    assert (s >= arrival - 1e-4).all()
+    # a job never starts before an earlier-arrived job of another group
+    # starts, except when it is grouped with a head that arrived first
+    starts = {}
+    for j in range(n):
+        starts.setdefault(round(s[j], 4), []).append(j)
+    heads = sorted(min(g) for g in starts.values())
+    assert (np.diff([s[h] for h in heads]) >= -1e-4).all()

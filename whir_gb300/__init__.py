@@ -118,6 +118,7 @@ _SIGS = {
     "whir_server_run": (ctypes.c_int, [vp, ctypes.POINTER(JobC), ctypes.c_int, ctypes.c_int,
                                        ctypes.POINTER(RunStatsC)]),
     "whir_server_free": (ctypes.c_int, [vp]),
+    "whir_server_set_lockstep": (ctypes.c_int, [vp, ctypes.c_int]),
     "whir_workspace_bytes": (ctypes.c_int, [ctypes.POINTER(Params), ctypes.POINTER(ctypes.c_uint64)]),
     "whir_proof_bytes_max": (ctypes.c_int, [ctypes.POINTER(Params), ctypes.c_int,
                                             ctypes.POINTER(ctypes.c_uint64)]),
@@ -132,6 +133,13 @@ _SIGS = {
                                         ctypes.c_char_p, ctypes.c_size_t,
                                         ctypes.POINTER(ctypes.c_size_t), u32p]),
     "whir_batch_max": (ctypes.c_int, [ctypes.POINTER(Params), i32p]),
+    "whir_serve_simulate_groups": (ctypes.c_int, [ctypes.POINTER(ctypes.c_double),
+                                                  ctypes.POINTER(ctypes.c_uint64),
+                                                  ctypes.POINTER(ctypes.c_double), i32p,
+                                                  ctypes.c_int, ctypes.c_int, ctypes.c_int,
+                                                  ctypes.c_uint64,
+                                                  ctypes.POINTER(ctypes.c_double),
+                                                  ctypes.POINTER(ctypes.c_double), i32p, i32p]),
     "whir_counters": (ctypes.c_int, [vp, ctypes.POINTER(ctypes.c_uint64),
                                      ctypes.POINTER(ctypes.c_uint64),
                                      ctypes.POINTER(ctypes.c_uint64)]),
@@ -524,11 +532,12 @@ def prove_batch(ctx, params, polys, claims=1, commit_only=False):
     _check(lib().whir_prove_batch(ctx.h, ctypes.byref(p), ptrs, 1 if on_device else 0, n,
                                   0 if commit_only else claims, 1 if commit_only else 0, buf, cap,
                                   lens, cps.ctypes.data_as(u32p)))
+    raw = buf.raw  # one copy of the whole buffer
     out = []
     for i in range(n):
         if lens[i] > cap:
             raise WhirError("proof longer than its buffer")
-        out.append((buf.raw[i * cap:i * cap + lens[i]], int(cps[i])))
+        out.append((raw[i * cap:i * cap + lens[i]], int(cps[i])))
     return out
 
 
@@ -621,11 +630,17 @@ class Server:
     """whir_server: a persistent pool of GPU workers (streams, pinned staging
     and prover buffers stay allocated between runs)."""
 
-    def __init__(self, workers=8, device=0, budget_bytes=150 << 30):
+    def __init__(self, workers=8, device=0, budget_bytes=150 << 30, lockstep=0):
         h = vp()
         _check(lib().whir_server_new(device, workers, budget_bytes, ctypes.byref(h)))
         self.h = h.value
         self.workers = workers
+        if lockstep:
+            self.set_lockstep(lockstep)
+
+    def set_lockstep(self, max_group):
+        """Most same-shape jobs proved together in lock step (1: none; 0: default)."""
+        _check(lib().whir_server_set_lockstep(self.h, max_group))
 
     def run(self, jobs, serve=False):
         """Runs the jobs (serve=True: each released at its arrival_s); fills
@@ -661,19 +676,28 @@ def prove_jobs(jobs, workers=4, device=0, budget_bytes=150 << 30, serve=False):
     return st.seconds, st.peak_device_bytes
 
 
-def serve_simulate(arrival_s, need_bytes, duration_s, workers, budget_bytes):
+def serve_simulate(arrival_s, need_bytes, duration_s, workers, budget_bytes, shape=None,
+                   max_group=1):
     """Admission order of whir_serve with host sleeps standing in for proofs:
-    returns (start_s, done_s, worker, status) arrays."""
+    returns (start_s, done_s, worker, status) arrays.  With shape (one id per
+    job), jobs of equal shape that have arrived are grouped, up to max_group
+    (whir_serve_simulate_groups)."""
     n = len(arrival_s)
     A = (ctypes.c_double * max(1, n))(*arrival_s)
-    N = (ctypes.c_uint64 * max(1, n))(*need_bytes)
+    N = (ctypes.c_uint64 * max(1, n))(*[int(x) for x in need_bytes])
     D = (ctypes.c_double * max(1, n))(*duration_s)
     S = (ctypes.c_double * max(1, n))()
     E = (ctypes.c_double * max(1, n))()
     Wk = np.zeros(max(1, n), np.int32)
     St = np.zeros(max(1, n), np.int32)
-    _check(lib().whir_serve_simulate(A, N, D, n, workers, budget_bytes, S, E,
-                                     Wk.ctypes.data_as(i32p), St.ctypes.data_as(i32p)))
+    if shape is None:
+        _check(lib().whir_serve_simulate(A, N, D, n, workers, budget_bytes, S, E,
+                                         Wk.ctypes.data_as(i32p), St.ctypes.data_as(i32p)))
+    else:
+        sh = np.ascontiguousarray(shape, np.int32)
+        _check(lib().whir_serve_simulate_groups(A, N, D, sh.ctypes.data_as(i32p), max_group, n,
+                                                workers, budget_bytes, S, E,
+                                                Wk.ctypes.data_as(i32p), St.ctypes.data_as(i32p)))
     return np.array(S[:n]), np.array(E[:n]), Wk[:n], St[:n]
 
 

@@ -1,6 +1,8 @@
 // Job runner for batched and served proving (see batch.h).
 #include "batch.h"
 
+#include "batch_prover.h"
+
 #include <algorithm>
 #include <condition_variable>
 #include <memory>
@@ -16,9 +18,9 @@ struct Admission::Sync {
 
 Admission::Admission(const std::vector<double> &arrival, const std::vector<size_t> &need,
                      size_t budget, const std::vector<size_t> &held, bool honor_arrival,
-                     Clock::time_point t0)
-    : arrival_(arrival), need_(need), budget_(budget), honor_(honor_arrival), t0_(t0),
-      held_(held), sync_(new Sync) {
+                     Clock::time_point t0, const Grouping *grouping)
+    : taken_(arrival.size(), 0), grouping_(grouping), arrival_(arrival), need_(need),
+      budget_(budget), honor_(honor_arrival), t0_(t0), held_(held), sync_(new Sync) {
   order_.resize(arrival.size());
   for (size_t i = 0; i < order_.size(); i++) order_[i] = i;
   // ties keep submission order
@@ -30,11 +32,19 @@ Admission::Admission(const std::vector<double> &arrival, const std::vector<size_
 
 Admission::~Admission() { delete sync_; }
 
-int Admission::take(int worker, bool *too_big) {
+size_t Admission::grow_of(int worker, const std::vector<int> &group) const {
+  if (grouping_ && grouping_->grow) return grouping_->grow(worker, group);
+  // buffers only grow: the worker ends up holding max(held, need)
+  const size_t nd = need_[group[0]];
+  return nd > held_[worker] ? nd - held_[worker] : 0;
+}
+
+std::vector<int> Admission::take(int worker, bool *too_big) {
   std::unique_lock<std::mutex> lock(sync_->mu);
   *too_big = false;
   for (;;) {
-    if (head_ >= order_.size()) return -1;
+    while (head_ < order_.size() && taken_[order_[head_]]) head_++;
+    if (head_ >= order_.size()) return {};
     size_t j = order_[head_];
     if (honor_) {
       auto due = t0_ + std::chrono::duration_cast<Clock::duration>(
@@ -45,20 +55,37 @@ int Admission::take(int worker, bool *too_big) {
       }
     }
     if (need_[j] > budget_) {  // can never run: hand it out to be failed
+      taken_[j] = 1;
       head_++;
       *too_big = true;
       sync_->cv.notify_all();
-      return (int)j;
+      return {(int)j};
     }
-    // buffers only grow: the worker ends up holding max(held, need)
-    size_t grow = need_[j] > held_[worker] ? need_[j] - held_[worker] : 0;
-    if (total_ + grow <= budget_) {
-      head_++;
-      held_[worker] += grow;
-      total_ += grow;
-      peak_ = std::max(peak_, total_);
-      sync_->cv.notify_all();
-      return (int)j;
+    std::vector<int> group{(int)j};
+    if (grouping_) {
+      const int mx = grouping_->max_group(j);
+      const auto now = Clock::now();
+      for (size_t q = head_ + 1; q < order_.size() && (int)group.size() < mx; q++) {
+        const size_t c = order_[q];
+        if (taken_[c] || need_[c] > budget_) continue;
+        if (honor_ && now < t0_ + std::chrono::duration_cast<Clock::duration>(
+                                      std::chrono::duration<double>(arrival_[c])))
+          break;  // arrival order: no later job has arrived either
+        if (grouping_->compatible(j, c)) group.push_back((int)c);
+      }
+    }
+    for (;;) {
+      const size_t grow = grow_of(worker, group);
+      if (total_ + grow <= budget_) {
+        for (int g : group) taken_[g] = 1;
+        held_[worker] += grow;
+        total_ += grow;
+        peak_ = std::max(peak_, total_);
+        sync_->cv.notify_all();
+        return group;
+      }
+      if (group.size() == 1) break;
+      group.resize(group.size() / 2);
     }
     sync_->cv.wait(lock);  // a release may free enough
   }
@@ -76,8 +103,9 @@ RunStats run_jobs(std::vector<Job> &jobs, std::vector<void *> &states, std::vect
                   size_t budget, bool honor_arrival,
                   const std::function<size_t(const Params &)> &need,
                   const std::function<void *(int worker)> &make_worker,
-                  const std::function<size_t(void *state, Job &job)> &exec,
-                  const std::function<size_t(void *state)> &prepare) {
+                  const std::function<size_t(void *state, std::vector<Job *> &group)> &exec,
+                  const std::function<size_t(void *state)> &prepare,
+                  const Grouping *grouping) {
   const int workers = (int)states.size();
   if (workers < 1 || held.size() != states.size()) throw WhirError(-1, "at least one worker");
   std::vector<double> arr(jobs.size());
@@ -91,7 +119,7 @@ RunStats run_jobs(std::vector<Job> &jobs, std::vector<void *> &states, std::vect
   auto secs = [&] {
     return std::chrono::duration<double>(Admission::Clock::now() - t0).count();
   };
-  Admission adm(arr, nd, budget, held, honor_arrival, t0);
+  Admission adm(arr, nd, budget, held, honor_arrival, t0, grouping);
   std::vector<std::thread> th;
   std::vector<std::string> start_err(workers);
   for (int w = 0; w < workers; w++) {
@@ -114,32 +142,42 @@ RunStats run_jobs(std::vector<Job> &jobs, std::vector<void *> &states, std::vect
       }
       for (;;) {
         bool too_big = false;
-        int j = adm.take(w, &too_big);
-        if (j < 0) break;
-        Job &job = jobs[j];
-        job.worker = w;
-        job.start = secs();
+        std::vector<int> taken = adm.take(w, &too_big);
+        if (taken.empty()) break;
+        std::vector<Job *> group;
+        const double start = secs();
+        for (int j : taken) {
+          group.push_back(&jobs[j]);
+          jobs[j].worker = w;
+          jobs[j].start = start;
+        }
         size_t now_held = adm.held()[w];
+        int status = 0;
+        std::string error;
         if (!state) {
-          job.status = -5;
-          job.error = "worker could not start: " + start_err[w];
+          status = -5;
+          error = "worker could not start: " + start_err[w];
           now_held = 0;
         } else if (too_big) {
-          job.status = -4;
-          job.error = "job needs more device memory than the budget";
+          status = -4;
+          error = "job needs more device memory than the budget";
         } else {
           try {
-            now_held = exec(state, job);
-            job.status = 0;
+            now_held = exec(state, group);
           } catch (const WhirError &e) {
-            job.status = e.code;
-            job.error = e.what();
+            status = e.code;
+            error = e.what();
           } catch (const std::exception &e) {
-            job.status = -5;
-            job.error = e.what();
+            status = -5;
+            error = e.what();
           }
         }
-        job.done = secs();
+        const double done = secs();
+        for (Job *job : group) {
+          job->status = status;
+          job->error = error;
+          job->done = done;
+        }
         adm.release(w, now_held);
       }
     });
@@ -156,7 +194,18 @@ namespace {
 struct GpuWorker {
   std::unique_ptr<Context> ctx;
   std::unique_ptr<Prover> prover;
+  std::unique_ptr<BatchProver> group_prover;  // lock-step groups, made on first use
+  size_t bytes() const {
+    return (prover ? prover->device_bytes() : 0) + (group_prover ? group_prover->device_bytes() : 0);
+  }
 };
+bool same_shape(const Job &a, const Job &b) {
+  const Params &p = a.params, &q = b.params;
+  return p.k == q.k && p.folding == q.folding && p.rate == q.rate &&
+         p.initial_reduction == q.initial_reduction && p.soundness == q.soundness &&
+         p.security_level == q.security_level && a.n_claims == b.n_claims &&
+         a.commit_only == b.commit_only && a.on_device == b.on_device;
+}
 }  // namespace
 
 struct Server::Lock {
@@ -228,16 +277,39 @@ RunStats Server::run(std::vector<Job> &jobs, bool honor_arrival) {
         w->prover->reserve();
       }
       cuda_check(cudaStreamSynchronize(w->ctx->stream()), "sync");
-      return w->prover->device_bytes();
+      return w->bytes();
     };
     std::vector<Job> none;
     run_jobs(none, states_, held_, budget_, false, need, make, nullptr, prepare);
   }
-  auto exec = [device](void *state, Job &job) -> size_t {
+  const int host_threads = (int)std::min(16u, std::max(1u, std::thread::hardware_concurrency()));
+  auto exec = [device, host_threads](void *state, std::vector<Job *> &group) -> size_t {
     cuda_check(cudaSetDevice(device), "cudaSetDevice");
     auto *w = static_cast<GpuWorker *>(state);
+    const Job &head = *group[0];
     // large jobs set the tail latency: their blocks go first on the device
-    w->ctx->set_high_priority(job.params.k >= Server::kPriorityK);
+    w->ctx->set_high_priority(head.params.k >= Server::kPriorityK);
+    if (group.size() > 1) {  // lock step: every pass of the group in one launch
+      if (!w->group_prover)
+        w->group_prover.reset(new BatchProver(w->ctx.get(), head.params, host_threads));
+      else
+        w->group_prover->set_params(head.params);
+      std::vector<Transcript> ts(group.size());
+      std::vector<Transcript *> tp;
+      std::vector<const uint32_t *> polys;
+      for (size_t i = 0; i < group.size(); i++) {
+        tp.push_back(&ts[i]);
+        polys.push_back(group[i]->poly);
+      }
+      w->group_prover->prove(tp, polys, head.on_device, head.commit_only ? 0 : head.n_claims,
+                             head.commit_only);
+      for (size_t i = 0; i < group.size(); i++) {
+        group[i]->checkpoint = ts[i].draw_fe();
+        group[i]->proof = ts[i].bytes();
+      }
+      return w->bytes();
+    }
+    Job &job = *group[0];
     if (!w->prover) w->prover.reset(new Prover(w->ctx.get(), job.params));
     else w->prover->set_params(job.params);
     Transcript ts;
@@ -250,9 +322,32 @@ RunStats Server::run(std::vector<Job> &jobs, bool honor_arrival) {
     }
     job.checkpoint = ts.draw_fe();
     job.proof = ts.bytes();
-    return w->prover->device_bytes();
+    return w->bytes();
   };
-  return run_jobs(jobs, states_, held_, budget_, honor_arrival, need, make, exec);
+  // lock-step groups: jobs of one shape, at most lockstep_ of them, at most
+  // 2^kGroupLog evaluations in all, and no more than the batched kernels take
+  Grouping grouping;
+  std::vector<int> group_cap(jobs.size(), 1);
+  for (size_t j = 0; j < jobs.size(); j++) {
+    const int by_size = jobs[j].params.k >= kGroupLog ? 1 : 1 << (kGroupLog - jobs[j].params.k);
+    group_cap[j] = std::max(1, std::min({lockstep_, by_size, BatchProver::max_batch(jobs[j].params)}));
+  }
+  grouping.compatible = [&jobs](size_t h, size_t j) { return same_shape(jobs[h], jobs[j]); };
+  grouping.max_group = [&group_cap](size_t h) { return group_cap[h]; };
+  std::vector<void *> &states = states_;
+  grouping.grow = [&jobs, &states](int worker, const std::vector<int> &group) -> size_t {
+    const auto *w = static_cast<const GpuWorker *>(states[worker]);
+    const Params &p = jobs[group[0]].params;
+    if (group.size() == 1) {
+      const size_t need = Prover::workspace_bytes(p), have = w && w->prover ? w->prover->device_bytes() : 0;
+      return need > have ? need - have : 0;
+    }
+    const size_t need = BatchProver::workspace_bytes(p, (int)group.size());
+    const size_t have = w && w->group_prover ? w->group_prover->device_bytes() : 0;
+    return need > have ? need - have : 0;
+  };
+  return run_jobs(jobs, states_, held_, budget_, honor_arrival, need, make, exec, nullptr,
+                  lockstep_ > 1 ? &grouping : nullptr);
 }
 
 }  // namespace whir

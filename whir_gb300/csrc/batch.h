@@ -38,28 +38,45 @@ struct Job {
   int worker = -1;
 };
 
+// Lock-step groups: a worker that takes the job at the head of the queue
+// also takes later jobs that have arrived and are compatible with it (the
+// same shape), up to max_group(head), to prove them together.  grow(worker,
+// group) is the device bytes that worker would add to run the group; it is
+// called on the worker's own thread with the admission lock held.
+struct Grouping {
+  std::function<bool(size_t head, size_t job)> compatible;
+  std::function<int(size_t head)> max_group;
+  std::function<size_t(int worker, const std::vector<int> &group)> grow;
+};
+
 // Release order and memory gate, independent of how a job is executed.
 class Admission {
  public:
   using Clock = std::chrono::steady_clock;
-  // need[j]: device bytes a worker holds while running job j; held[w]: bytes
-  // worker w already holds
+  // need[j]: device bytes a worker holds while running job j alone; held[w]:
+  // bytes worker w already holds
   Admission(const std::vector<double> &arrival, const std::vector<size_t> &need, size_t budget,
-            const std::vector<size_t> &held, bool honor_arrival, Clock::time_point t0);
+            const std::vector<size_t> &held, bool honor_arrival, Clock::time_point t0,
+            const Grouping *grouping = nullptr);
   ~Admission();
   Admission(const Admission &) = delete;
   Admission &operator=(const Admission &) = delete;
   // Blocks until the next job (in arrival order) may start on `worker`;
-  // returns its index, or -1 when every job has been handed out.  A job whose
-  // need alone exceeds the budget is returned with *too_big set.
-  int take(int worker, bool *too_big);
+  // returns it with the jobs grouped with it (the head first), or an empty
+  // list when every job has been handed out.  A job whose need alone exceeds
+  // the budget is returned alone with *too_big set.  A group that does not
+  // fit the budget is halved until it does (down to the head alone).
+  std::vector<int> take(int worker, bool *too_big);
   // the worker finished its job and now holds `held` device bytes
   void release(int worker, size_t held);
   size_t peak_bytes() const { return peak_; }
   const std::vector<size_t> &held() const { return held_; }
 
  private:
+  size_t grow_of(int worker, const std::vector<int> &group) const;
   std::vector<size_t> order_;  // job indices by arrival
+  std::vector<char> taken_;    // handed out (possibly ahead of the head, in a group)
+  const Grouping *grouping_;
   std::vector<double> arrival_;
   std::vector<size_t> need_;
   size_t budget_;
@@ -78,8 +95,9 @@ struct RunStats {
 };
 
 // Runs `jobs` on one host thread per entry of `states` (a worker's persistent
-// state, created on first use by make_worker on its own thread).  exec(state,
-// job) does the work and returns the device bytes the worker holds
+// state, created on first use by make_worker on its own thread).
+// exec(state, group) does the work of a group of jobs (one job unless
+// grouping is given) and returns the device bytes the worker holds
 // afterwards.  held[w] (in/out) is what worker w holds across runs.
 // prepare (optional) runs once on each worker thread before it takes jobs
 // and returns the device bytes the worker then holds.
@@ -87,8 +105,9 @@ RunStats run_jobs(std::vector<Job> &jobs, std::vector<void *> &states, std::vect
                   size_t budget, bool honor_arrival,
                   const std::function<size_t(const Params &)> &need,
                   const std::function<void *(int worker)> &make_worker,
-                  const std::function<size_t(void *state, Job &job)> &exec,
-                  const std::function<size_t(void *state)> &prepare = nullptr);
+                  const std::function<size_t(void *state, std::vector<Job *> &group)> &exec,
+                  const std::function<size_t(void *state)> &prepare = nullptr,
+                  const Grouping *grouping = nullptr);
 
 // A pool of GPU workers on one device, kept between runs: each worker's
 // stream, pinned staging and prover buffers stay allocated, so a run starts
@@ -101,12 +120,19 @@ class Server {
   Server &operator=(const Server &) = delete;
   RunStats run(std::vector<Job> &jobs, bool honor_arrival);
   int workers() const { return (int)states_.size(); }
+  // Lock-step groups of same-shape jobs (BatchProver): at most max_group
+  // jobs per group; 1 proves every job alone; 0 restores the default.
+  void set_lockstep(int max_group) { lockstep_ = max_group > 0 ? max_group : kLockstepDefault; }
+  static constexpr int kLockstepDefault = 256;
+  // a group holds at most 2^kGroupLog evaluations in all
+  static constexpr int kGroupLog = 26;
   // jobs of at least 2^kPriorityK evaluations run on high-priority streams
   static constexpr int kPriorityK = 22;
 
  private:
   int device_;
   size_t budget_;
+  int lockstep_ = kLockstepDefault;
   std::vector<void *> states_;
   std::vector<size_t> held_;
   struct Lock;

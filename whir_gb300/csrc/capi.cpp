@@ -664,6 +664,12 @@ int whir_server_run(whir_server *s, whir_job *jobs, int n_jobs, int honor_arriva
   run_on(s->s, jobs, n_jobs, stats, honor_arrival != 0);
   API_END
 }
+int whir_server_set_lockstep(whir_server *s, int max_group) {
+  API_BEGIN
+  need(s != nullptr && max_group >= 0, "bad argument");
+  s->s.set_lockstep(max_group);
+  API_END
+}
 int whir_server_free(whir_server *s) {
   API_BEGIN
   delete s;
@@ -703,10 +709,13 @@ int whir_proof_bytes_max(const whir_params *params, int n_claims, uint64_t *byte
   API_END
 }
 
-int whir_serve_simulate(const double *arrival_s, const uint64_t *need_b, const double *duration_s,
-                        int n_jobs, int n_workers, uint64_t budget, double *start_s,
-                        double *done_s, int32_t *worker, int32_t *status) {
-  API_BEGIN
+// whir_serve's scheduler with host sleeps for proofs; shape (optional):
+// jobs of equal shape id may be grouped, up to max_group per group, a group
+// holding its size times one job's bytes and taking the head job's time
+static void simulate(const double *arrival_s, const uint64_t *need_b, const double *duration_s,
+                     const int32_t *shape, int max_group, int n_jobs, int n_workers,
+                     uint64_t budget, double *start_s, double *done_s, int32_t *worker,
+                     int32_t *status) {
   need(n_jobs >= 0 && n_workers >= 1 && n_workers <= 256, "bad sizes");
   need(n_jobs == 0 || (arrival_s && need_b && duration_s && start_s && done_s && worker && status),
        "null argument");
@@ -721,15 +730,25 @@ int whir_serve_simulate(const double *arrival_s, const uint64_t *need_b, const d
   auto needf = [&](const whir::Params &p) { return nb[p.k]; };
   // a worker's buffers only grow, as a prover's do
   auto make = [](int) -> void * { return new size_t(0); };
-  auto exec = [&](void *state, whir::Job &j) -> size_t {
-    std::this_thread::sleep_for(std::chrono::duration<double>(duration_s[j.params.k]));
+  auto exec = [&](void *state, std::vector<whir::Job *> &group) -> size_t {
+    const int h = group[0]->params.k;
+    std::this_thread::sleep_for(std::chrono::duration<double>(duration_s[h]));
     size_t *held = static_cast<size_t *>(state);
-    *held = std::max(*held, nb[j.params.k]);
+    *held = std::max(*held, nb[h] * group.size());
     return *held;
   };
   std::vector<void *> states(n_workers, nullptr);
   std::vector<size_t> held(n_workers, 0);
-  whir::run_jobs(js, states, held, budget, true, needf, make, exec);
+  whir::Grouping grouping;
+  grouping.compatible = [&](size_t h, size_t j) { return shape[h] == shape[j]; };
+  grouping.max_group = [&](size_t) { return max_group; };
+  grouping.grow = [&](int w, const std::vector<int> &group) -> size_t {
+    const size_t have = states[w] ? *static_cast<size_t *>(states[w]) : 0;
+    const size_t want = nb[group[0]] * group.size();
+    return want > have ? want - have : 0;
+  };
+  whir::run_jobs(js, states, held, budget, true, needf, make, exec, nullptr,
+                 shape && max_group > 1 ? &grouping : nullptr);
   for (void *st : states) delete static_cast<size_t *>(st);
   for (int i = 0; i < n_jobs; i++) {
     start_s[i] = js[i].start;
@@ -737,6 +756,25 @@ int whir_serve_simulate(const double *arrival_s, const uint64_t *need_b, const d
     worker[i] = js[i].worker;
     status[i] = js[i].status == 0 ? WHIR_OK : js[i].status == -4 ? WHIR_ERR_CAPACITY : WHIR_ERR_INTERNAL;
   }
+}
+
+int whir_serve_simulate(const double *arrival_s, const uint64_t *need_b, const double *duration_s,
+                        int n_jobs, int n_workers, uint64_t budget, double *start_s,
+                        double *done_s, int32_t *worker, int32_t *status) {
+  API_BEGIN
+  simulate(arrival_s, need_b, duration_s, nullptr, 1, n_jobs, n_workers, budget, start_s, done_s,
+           worker, status);
+  API_END
+}
+
+int whir_serve_simulate_groups(const double *arrival_s, const uint64_t *need_b,
+                               const double *duration_s, const int32_t *shape, int max_group,
+                               int n_jobs, int n_workers, uint64_t budget, double *start_s,
+                               double *done_s, int32_t *worker, int32_t *status) {
+  API_BEGIN
+  need(max_group >= 1 && (shape || n_jobs == 0), "bad grouping");
+  simulate(arrival_s, need_b, duration_s, shape, max_group, n_jobs, n_workers, budget, start_s,
+           done_s, worker, status);
   API_END
 }
 
