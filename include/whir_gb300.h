@@ -125,6 +125,31 @@ WHIR_API int whir_combine_pows(whir_ctx *ctx, uint32_t *weights, int k, const ui
 WHIR_API int whir_combine_pows_scaled(whir_ctx *ctx, uint32_t *weights, int k, const uint32_t *vars,
                              int n, const uint32_t *scales);
 
+/* The code part of SumcheckProver::fold_with_code (sumcheck/prover.rs:400-561)
+ * on its own, as the reference's test_fold_with_code (prover.rs:598-768)
+ * exercises it: for queries idx[0..n) of a base codeword (device, 2^k_data
+ * rows of 2^folding words) with scales s_i (n ext), the per-query recursion
+ * g from the rows' evaluations at eq(rs) (rs: folding ext), folded round by
+ * round with r[0..folding-1) (ext); out[8 j .. 8 j + 8) = round j's (c0, c2)
+ * of the pow claims, out[8 folding .. + 4) = sum_i s_i g(0, idx_i) (the
+ * round-0 sum term). */
+WHIR_API int whir_fold_code_rounds(whir_ctx *ctx, const uint32_t *codeword, int k_data,
+                                   int folding, const size_t *idx, int n,
+                                   const uint32_t *scales, const uint32_t *rs, const uint32_t *r,
+                                   uint32_t *out);
+
+/* Debug mode of the single-instance prover, process-wide, off by default.
+ * Bit 0: the reference's debug-build invariants, checked on the device's
+ * results: after the expression build, every sumcheck round of fold and
+ * fold_with_code, <poly, weights> equals the claimed sum
+ * (crates/whir/src/sumcheck/prover.rs:346,558, expr.rs:68), and every opened
+ * Merkle path hashes to its root (crates/merkle/src/poseidon_packed.rs:158-230);
+ * a failure ends the proof with WHIR_ERR_ARG and a "debug check" message.
+ * The checks add a reduction per round; proofs are unchanged.  Bit 1: NVTX
+ * ranges around the prover's phases, named like the reference's tracing
+ * spans (whir.rs:19-314, sumcheck/prover.rs:184-497). */
+WHIR_API int whir_debug_set(unsigned flags);
+
 /* Poseidon2KoalaBear<width>::permute_mut on the host (width 16 or 24), with
  * the constants of new_from_rng_128(&mut rng(1000)) used by the harness
  * (crates/whir/src/test.rs:195-196). */

@@ -140,6 +140,10 @@ _SIGS = {
                                                   ctypes.c_uint64,
                                                   ctypes.POINTER(ctypes.c_double),
                                                   ctypes.POINTER(ctypes.c_double), i32p, i32p]),
+    "whir_fold_code_rounds": (ctypes.c_int, [vp, vp, ctypes.c_int, ctypes.c_int,
+                                             ctypes.POINTER(ctypes.c_size_t), ctypes.c_int, u32p,
+                                             u32p, u32p, u32p]),
+    "whir_debug_set": (ctypes.c_int, [ctypes.c_uint]),
     "whir_counters": (ctypes.c_int, [vp, ctypes.POINTER(ctypes.c_uint64),
                                      ctypes.POINTER(ctypes.c_uint64),
                                      ctypes.POINTER(ctypes.c_uint64)]),
@@ -496,6 +500,29 @@ def prove_harness(ctx, params, polys, poly_k, groups, whir=None):
     w.prove(t, polys, poly_k, groups)
     cp = t.draw_base()
     return t.finalize(), cp
+
+
+def fold_code_rounds(ctx, dev_codeword, k_data, folding, idx, scales, rs, r):
+    """whir_fold_code_rounds: per round (c0, c2) of fold_with_code's pow claims
+    (folding x 8 words) and the round-0 sum term (4 words)."""
+    n = len(idx)
+    ix = (ctypes.c_size_t * max(1, n))(*[int(i) for i in idx])
+    sc, sp = _u32(scales)
+    rsa, rsp = _u32(rs)
+    ra, rp = _u32(r if len(r) else np.zeros(4, np.uint32))
+    out = np.zeros(8 * folding + 4, np.uint32)
+    _check(lib().whir_fold_code_rounds(ctx.h, dev_codeword.ptr, k_data, folding, ix, n, sp, rsp,
+                                       rp, out.ctypes.data_as(u32p)))
+    return out
+
+
+DEBUG_CHECKS, DEBUG_NVTX = 1, 2
+
+
+def debug_set(flags):
+    """whir_debug_set: DEBUG_CHECKS (the reference's debug invariants) and/or
+    DEBUG_NVTX (NVTX ranges); 0 turns the debug mode off."""
+    _check(lib().whir_debug_set(flags))
 
 
 def batch_max(params):

@@ -18,6 +18,7 @@
 #include "poseidon2_host.h"
 #include "batch.h"
 #include "batch_prover.h"
+#include "debug.h"
 #include "prover.h"
 #include "tune.h"
 #include "verifier.h"
@@ -427,6 +428,81 @@ int whir_combine_pows_scaled(whir_ctx *ctx, uint32_t *weights, int k, const uint
   std::vector<E4> sc(n);
   for (int i = 0; i < n; i++) sc[i] = ext_in(scales + 4 * i);
   combine_pows_impl(ctx, weights, k, vars, n, sc);
+  API_END
+}
+
+int whir_fold_code_rounds(whir_ctx *ctx, const uint32_t *codeword, int k_data, int folding,
+                          const size_t *idx, int n, const uint32_t *scales, const uint32_t *rs,
+                          const uint32_t *r, uint32_t *out) {
+  API_BEGIN
+  need(ctx && codeword && out && rs && (r || folding <= 1), "null argument");
+  need(folding >= 1 && folding <= 8 && k_data >= folding && k_data <= 24, "bad shape");
+  need(n >= 1 && idx && scales, "no queries");
+  const int d = folding, lS = k_data - d;
+  const size_t S = (size_t)1 << lS, T = (size_t)1 << d;
+  for (int i = 0; i < n; i++) need(idx[i] < ((size_t)1 << k_data), "index out of range");
+  whir::gpu::Point rsp = point_in(rs, d);
+  std::vector<E4> rr(d > 1 ? d - 1 : 0);
+  for (int i = 0; i + 1 < d; i++) rr[i] = ext_in(r + 4 * i);
+  // device state (Prover's fold_with_code layout): G | scales | idx | ws | tw | B | wd | rows
+  const size_t un = (size_t)n;
+  std::vector<uint32_t> hrows(un * T), hidx(un), hwd(T);
+  std::vector<E4> hsc(un);
+  for (size_t i = 0; i < un; i++) {
+    hidx[i] = (uint32_t)idx[i];
+    hsc[i] = ext_in(scales + 4 * i);
+    for (size_t t = 0; t < T; t++) hrows[i * T + t] = (uint32_t)((idx[i] & (S - 1)) + t * S);
+  }
+  whir::gpu::CodeState cs;
+  cs.n = n;
+  cs.d = d;
+  cs.k_data = k_data;
+  cs.omega = whir::two_adic_generator(k_data);
+  cs.winv = kb::inv(cs.omega);
+  cs.two_inv = kb::inv(kb::from_canonical(2));
+  const uint32_t wdv = kb::pow(cs.winv, S);
+  hwd[0] = kb::ONE;
+  for (size_t t = 1; t < T; t++) hwd[t] = kb::mul(hwd[t - 1], wdv);
+  const size_t words = 4 * un * T + 4 * un + 5 * un + T + un * T;
+  ctx->scratch.reserve(4 * words + 64);
+  uint32_t *base = ctx->scratch.as<uint32_t>();
+  cs.G = reinterpret_cast<E4 *>(base);
+  cs.scales = reinterpret_cast<E4 *>(base + 4 * un * T);
+  uint32_t *u = base + 4 * un * T + 4 * un;
+  cs.idx = u;
+  cs.ws = u + un;
+  cs.tw = u + 2 * un;
+  cs.B = u + 3 * un;
+  uint32_t *dwd = u + 4 * un, *drows = dwd + T;
+  cs.wd = dwd;
+  cudaStream_t st = ctx->ctx.stream();
+  whir::cuda_check(cudaMemcpyAsync(const_cast<uint32_t *>(cs.idx), hidx.data(), 4 * un,
+                                   cudaMemcpyHostToDevice, st), "h2d");
+  whir::cuda_check(cudaMemcpyAsync(cs.scales, hsc.data(), 16 * un, cudaMemcpyHostToDevice, st), "h2d");
+  whir::cuda_check(cudaMemcpyAsync(dwd, hwd.data(), 4 * T, cudaMemcpyHostToDevice, st), "h2d");
+  whir::cuda_check(cudaMemcpyAsync(drows, hrows.data(), 4 * un * T, cudaMemcpyHostToDevice, st),
+                   "h2d");
+  // G_0: the 2^d rows of each query's recursion at eq(rs) (prover.rs:497-506)
+  whir::cuda_check(whir::gpu::row_evals(codeword, (int)T, drows, (int)(un * T), rsp, cs.G, st),
+                   "row_evals");
+  unsigned long long *a = acc_buf(ctx, 12);
+  for (int round = 0; round < d; round++) {
+    whir::cuda_check(whir::gpu::code_round(cs, round, round ? rr[round - 1] : kb::e_zero(), a, st),
+                     "code_round");
+    uint32_t got[12];
+    read_acc(ctx, a, 12, got);
+    memcpy(out + 8 * round, got, 32);
+    if (round == 0) memcpy(out + 8 * d, got + 8, 16);
+    whir::cuda_check(cudaMemsetAsync(a, 0, 8 * 12, st), "memset");
+  }
+  ctx->ctx.sync();
+  API_END
+}
+
+int whir_debug_set(unsigned flags) {
+  API_BEGIN
+  need((flags & ~3u) == 0, "unknown debug flags");
+  whir::set_debug(flags);
   API_END
 }
 

@@ -1,0 +1,40 @@
+// Debug mode of the provers, off by default (whir_debug_set): the
+// reference's debug-build invariants checked on the device's results, and
+// NVTX ranges named like the reference's tracing spans so that a profiler
+// timeline lines up with them.
+#pragma once
+#include <nvtx3/nvToolsExt.h>
+
+namespace whir {
+
+enum DebugFlags : unsigned {
+  // after every sumcheck round and expression build: <poly, weights> equals
+  // the running claimed sum (crates/whir/src/sumcheck/prover.rs:346,558,
+  // expr.rs:68); every opened Merkle path hashes to its root
+  // (crates/merkle/src/poseidon_packed.rs:158-230)
+  DEBUG_CHECKS = 1u,
+  // NVTX ranges around the prover's phases (crates/whir/src/whir.rs:19-314,
+  // crates/whir/src/sumcheck/prover.rs:184-497)
+  DEBUG_NVTX = 2u,
+};
+void set_debug(unsigned flags);
+unsigned debug_flags();
+inline bool debug_checks() { return (debug_flags() & DEBUG_CHECKS) != 0; }
+
+// an NVTX range for the lifetime of the object while DEBUG_NVTX is set
+class Span {
+ public:
+  explicit Span(const char *name) : on_((debug_flags() & DEBUG_NVTX) != 0) {
+    if (on_) nvtxRangePushA(name);
+  }
+  ~Span() {
+    if (on_) nvtxRangePop();
+  }
+  Span(const Span &) = delete;
+  Span &operator=(const Span &) = delete;
+
+ private:
+  bool on_;
+};
+
+}  // namespace whir

@@ -153,6 +153,9 @@ cudaError_t sumcheck_round(const kb::E4 *p_in, const kb::E4 *w_in, size_t n_in, 
 cudaError_t eval_ext(const kb::E4 *poly, int k, const kb::E4 *eq_lo, int s_lo,
                      const kb::E4 *eq_hi, unsigned long long *acc, cudaStream_t st,
                      const Publish &pub = Publish());
+// <a, b> of two extension arrays of n elements -> acc u64[4] (debug checks)
+cudaError_t dot_ext(const kb::E4 *a, const kb::E4 *b, size_t n, unsigned long long *acc,
+                    cudaStream_t st, const Publish &pub = Publish());
 // fold_with_code's per-query state on the device (see code_round_kernel)
 struct CodeState {
   const uint32_t *idx;  // n query indexes

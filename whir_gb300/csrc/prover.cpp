@@ -1,12 +1,15 @@
 // GPU WHIR prover host orchestration (see prover.h).
 #include "prover.h"
+#include "debug.h"
 #include "host_math.h"
 #include "svo_host.h"
+#include "verifier.h"
 
 #include <math.h>
 #include <string.h>
 
 #include <algorithm>
+#include <atomic>
 #include <chrono>
 #include <functional>
 #include <map>
@@ -73,6 +76,10 @@ uint32_t two_adic_generator(int bits) {
   for (int i = bits; i < 24; i++) g = mul(g, g);
   return g;
 }
+
+static std::atomic<unsigned> g_debug{0};
+void set_debug(unsigned flags) { g_debug.store(flags, std::memory_order_relaxed); }
+unsigned debug_flags() { return g_debug.load(std::memory_order_relaxed); }
 
 void cuda_check(cudaError_t e, const char *what) {
   if (e != cudaSuccess)
@@ -251,13 +258,17 @@ void Context::count_copy(size_t bytes, int kind) {
 // ---------------- encode + commit ----------------
 void encode_commit(Context &ctx, const uint32_t *src, int k, int rate, int folding, int dim,
                    uint32_t *codeword, uint32_t *scratch, uint32_t *nodes, DeviceTree *out) {
+  Span span(dim == 1 ? "commit_base" : "commit_ext");  // whir.rs:19, 38
   cudaStream_t st = ctx.stream();
   int log_h = k + rate - folding;
   size_t width = (size_t)dim << folding, h_in = (size_t)1 << (k - folding);
   size_t rows = (size_t)1 << log_h;
-  ctx.prof_begin(Context::K_DFT);
-  cuda_check(gpu::dft_batch(src, h_in, width, log_h, codeword, scratch, st), "dft_batch");
-  ctx.prof_end(Context::K_DFT, 4.0 * (double)(h_in * width + rows * width));
+  {
+    Span dft(dim == 1 ? "dft-base" : "dft-ext");  // whir.rs:33, 58
+    ctx.prof_begin(Context::K_DFT);
+    cuda_check(gpu::dft_batch(src, h_in, width, log_h, codeword, scratch, st), "dft_batch");
+    ctx.prof_end(Context::K_DFT, 4.0 * (double)(h_in * width + rows * width));
+  }
   ctx.prof_begin(Context::K_LEAF);
   cuda_check(gpu::hash_rows(codeword, rows, (int)width, nodes, st), "hash_rows");
   ctx.prof_end(Context::K_LEAF, 4.0 * (double)(rows * width + rows * 8));
@@ -450,6 +461,10 @@ struct Prover::Impl {
   size_t args_off = 0, defer_off = 0;
   struct PendingHint {
     size_t ts_off, pin_off, words;
+    // the opening's tree, for the debug check of its path
+    uint32_t root[8];
+    size_t index;
+    int log_h, row_len;
   };
   std::vector<PendingHint> pending_hints;
   // claims
@@ -540,10 +555,28 @@ struct Prover::Impl {
                "eq_tables");
   }
   void fill_pending_hints(Transcript &ts) {
-    for (auto &h : pending_hints)
-      ts.hint_fill(h.ts_off, reinterpret_cast<const uint32_t *>(defer_pin.data()) + h.pin_off, h.words);
+    for (auto &h : pending_hints) {
+      const uint32_t *w = reinterpret_cast<const uint32_t *>(defer_pin.data()) + h.pin_off;
+      // MerkleTree::query's debug self-check (poseidon_packed.rs:158-230)
+      if (debug_checks() &&
+          !merkle_path_ok(h.root, h.index, w, (size_t)h.row_len, w + h.row_len, h.log_h))
+        throw WhirError(-5, "debug check: an opened Merkle path does not hash to its root");
+      ts.hint_fill(h.ts_off, w, h.words);
+    }
     pending_hints.clear();
     defer_off = 0;
+  }
+  // Expression::prod == sum (prover.rs:346,558, expr.rs:68): the device
+  // arrays' inner product against the running claimed sum, in debug mode
+  void check_sum(const char *where) {
+    if (!debug_checks()) return;
+    flush();
+    unsigned long long *a = acc.as<unsigned long long>();
+    cuda_check(gpu::dot_ext(P(), W(), (size_t)1 << kc, a, st(), publish(4)), "dot");
+    const unsigned long long *h = published();
+    wait_published();
+    if (!e_eq(reduce_acc(h), sum))
+      throw WhirError(-5, std::string("debug check: <poly, weights> != sum after ") + where);
   }
   // pinned space (in words) for device->host results read after a later sync
   size_t defer_alloc(size_t words, Transcript &ts) {
@@ -625,6 +658,7 @@ struct Prover::Impl {
 
   // ---- write_virtual_eval (prover.rs:232-277) ----
   void write_virtual_eval(Transcript &ts) {
+    Span span("write_virtual_eval");  // sumcheck/prover.rs:231
     VirtClaim v;
     v.point.resize(p.k);
     expand(v.point.data(), p.k, ts.draw_ext());
@@ -766,6 +800,7 @@ struct Prover::Impl {
 
   // ---- new_prover (prover.rs:280-354) incl. expression (185-229) ----
   void new_prover(Transcript &ts) {
+    Span span("new_prover");  // sumcheck/prover.rs:279
     alpha = ts.draw_ext();
     auto order = claims_layout_order();
     int n = (int)claims.size();
@@ -823,6 +858,7 @@ struct Prover::Impl {
       a = e_mul(a, alpha);
     }
     for (auto &kv : groups) add_eqs(W() + kv.first.first, kv.first.second, kv.second.first, kv.second.second);
+    check_sum("new_prover");
   }
 
   // ---- queries (MerkleTree::query, poseidon_packed.rs:145-233) ----
@@ -857,12 +893,16 @@ struct Prover::Impl {
                  "gather");
     }
     ctx->count_copy(4 * per * n, cudaMemcpyDeviceToHost);
-    for (int i = 0; i < n; i++)
-      pending_hints.push_back(PendingHint{ts.hint_reserve(per), off + per * i, per});
+    for (int i = 0; i < n; i++) {
+      PendingHint h{ts.hint_reserve(per), off + per * i, per, {}, idx[i], t.log_h, t.row_len};
+      memcpy(h.root, t.root, 32);
+      pending_hints.push_back(h);
+    }
     return off;
   }
 
   std::vector<size_t> stir_indexes(Transcript &ts, int bits, int n) {  // whir.rs:64-77
+    Span span("stir_indexes");  // whir.rs:63
     std::vector<size_t> v(n);
     for (int i = 0; i < n; i++) v[i] = ts.draw_bits(bits);
     std::sort(v.begin(), v.end());
@@ -878,6 +918,7 @@ struct Prover::Impl {
   std::vector<E4> fold(Transcript &ts, const std::vector<std::vector<E4>> &eq_pts,
                        const std::vector<E4> &eq_evals, const std::vector<uint32_t> &vars,
                        size_t rows_off, size_t per, int row_len, const std::vector<E4> &point) {
+    Span span("fold");  // sumcheck/prover.rs:377
     alpha = ts.draw_ext();
     flush();
     std::vector<E4> sc;
@@ -911,6 +952,7 @@ struct Prover::Impl {
       sum = extrapolate012(c0, e_sub(sum, c0), c2, r);
       out.push_back(r);
       rs.push_back(r);
+      check_sum("a fold round");
     }
     (void)row_len;
     return out;
@@ -919,6 +961,7 @@ struct Prover::Impl {
   // ---- fold_with_code (prover.rs:400-561) ----
   std::vector<E4> fold_with_code(Transcript &ts, const std::vector<std::vector<E4>> &eq_pts,
                                  const std::vector<E4> &eq_evals, const std::vector<size_t> &idx) {
+    Span span("fold_with_code");  // sumcheck/prover.rs:399
     int d = p.folding;
     alpha = ts.draw_ext();
     int k_data = t0.log_h;
@@ -1009,6 +1052,7 @@ struct Prover::Impl {
     cuda_check(gpu::code_finish(cs, rc.back(), st()), "code_finish");
     flush();
     add_pows_dev(cs.ws, cs.scales, n);  // combine_pows_scaled (combine.rs:441-468)
+    check_sum("fold_with_code");
     for (auto &r : rc) rs.push_back(r);
     return rc;
   }
@@ -1018,13 +1062,17 @@ struct Prover::Impl {
     pending_hints.clear();
     defer_off = 0;
     int n_ood = n_ood_queries(p.soundness, p.security_level, p.k, p.rate, EXT_BITS);
-    for (int i = 0; i < n_ood; i++) write_virtual_eval(ts);
+    {
+      Span span("ood claims");  // whir.rs:187
+      for (int i = 0; i < n_ood; i++) write_virtual_eval(ts);
+    }
     new_prover(ts);
     int n_rounds, final_rounds;
     number_of_rounds(p.folding, p.k, &n_rounds, &final_rounds);
     cur_tree = -1;
     std::vector<E4> round_point;
     for (int round = 0; round < n_rounds; round++) {
+      Span round_span("round");  // whir.rs:206
       int kfd, this_rate, prev_rate;
       round_params(round, &kfd, &this_rate, &prev_rate);
       flush();
@@ -1036,6 +1084,7 @@ struct Prover::Impl {
       int n_o = n_ood_queries(p.soundness, p.security_level, kc, this_rate, EXT_BITS);
       std::vector<std::vector<E4>> pts;
       std::vector<E4> evs;
+      Span ood_span("ood claims in round");  // whir.rs:224
       for (int i = 0; i < n_o; i++) {
         std::vector<E4> pt(kc);
         expand(pt.data(), kc, ts.draw_ext());
@@ -1045,6 +1094,7 @@ struct Prover::Impl {
         evs.push_back(e);
       }
       int n_s = n_stir_queries(p.soundness, p.security_level, prev_rate);
+      Span stir_span("stir claims");  // whir.rs:250
       std::vector<size_t> idx = stir_indexes(ts, kfd, n_s);
       std::vector<E4> rnew;
       if (round == 0) {
@@ -1062,6 +1112,7 @@ struct Prover::Impl {
       round_point = rnew;
       cur_tree = slot;
     }
+    Span final_span("final");  // whir.rs:314
     flush();
     size_t nf = (size_t)1 << kc;
     E4 *hf = (E4 *)ctx->pinned(16 * nf);

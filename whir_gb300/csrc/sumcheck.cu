@@ -841,6 +841,32 @@ cudaError_t eval_ext(const E4 *poly, int k, const E4 *eq_lo, int s_lo, const E4 
   return eval_ext_batch(poly, k, eq_lo, s_lo, eq_hi, 0, 1, acc, st, pub);
 }
 
+// <poly, weights> = sum_i poly[i] weights[i] (Expression::prod, the debug
+// invariant of crates/whir/src/sumcheck/expr.rs:68) -> acc u64[4]
+template <bool VEC>
+__global__ void __launch_bounds__(256) dot_ext_kernel(const E4 *__restrict__ a,
+                                                     const E4 *__restrict__ b, size_t n,
+                                                     unsigned long long *acc, Publish pub) {
+  E4 s = kb::e_zero();
+  for (size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x; i < n;
+       i += (size_t)gridDim.x * blockDim.x)
+    s = kb::e_add(s, kb::e_mul(ld_e4<VEC>(a + i), ld_e4<VEC>(b + i)));
+  E4 v[1] = {s};
+  block_acc<1>(v, acc, acc, pub);
+}
+
+cudaError_t dot_ext(const E4 *a, const E4 *b, size_t n, unsigned long long *acc, cudaStream_t st,
+                    const Publish &pub) {
+  size_t g = (n + 255) / 256;
+  unsigned grid = (unsigned)(g < 152 * 4 ? (g ? g : 1) : 152 * 4);
+  if (aligned16(a) && aligned16(b))
+    dot_ext_kernel<true><<<grid, 256, 0, st>>>(a, b, n, acc, pub);
+  else
+    dot_ext_kernel<false><<<grid, 256, 0, st>>>(a, b, n, acc, pub);
+  count_launches(1);
+  return cudaGetLastError();
+}
+
 // Batched: instance y = blockIdx.y evaluates rows idx[off[y] .. off[y+1])
 // of its own codeword, which is interleaved with the others' (row r of
 // instance y is row r batch + y of rows), at its own rs (rs_b[y ks ..]).

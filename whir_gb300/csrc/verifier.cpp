@@ -60,6 +60,27 @@ bool open_path(TranscriptReader &ts, const uint32_t root[8], size_t index, size_
   return !ts.failed() && memcmp(acc, root, 32) == 0;
 }
 
+}  // namespace
+
+bool merkle_path_ok(const uint32_t root[8], size_t index, const uint32_t *row, size_t row_len,
+                    const uint32_t *siblings, int log_h) {
+  if (log_h < 0 || log_h > 40 || index >= ((size_t)1 << log_h)) return false;
+  uint32_t acc[8];
+  hash_leaf(row, row_len, acc);
+  size_t idx = index;
+  for (int l = 0; l < log_h; l++) {
+    uint32_t nxt[8];
+    const size_t mid = (size_t)1 << (log_h - l - 1);
+    if (idx >= mid) compress(siblings + 8 * l, acc, nxt);
+    else compress(acc, siblings + 8 * l, nxt);
+    memcpy(acc, nxt, 32);
+    idx &= mid - 1;
+  }
+  return memcmp(acc, root, 32) == 0;
+}
+
+namespace {
+
 // whir.rs:64-77: n sample_bits draws, sorted and deduplicated
 std::vector<size_t> stir_indexes(TranscriptReader &ts, int bits, int n) {
   std::vector<size_t> v(n);

@@ -28,4 +28,10 @@ VerifyResult verify(const Params &p, const std::vector<int> &poly_k,
                     const std::vector<std::vector<int>> &groups, const uint8_t *proof, size_t len,
                     uint32_t *checkpoint);
 
+// The path check of MerkleTree::verify (crates/merkle/src/poseidon_packed.rs:235-257,
+// poseidon.rs:22-41) over words already read: the opened row (row_len words)
+// hashed as a leaf, then log_h sibling digests bottom-up, must give root.
+bool merkle_path_ok(const uint32_t root[8], size_t index, const uint32_t *row, size_t row_len,
+                    const uint32_t *siblings, int log_h);
+
 }  // namespace whir
