@@ -272,7 +272,7 @@ WHIR_API int whir_server_run(whir_server *s, whir_job *jobs, int n_jobs, int hon
  * same shape (parameters, claim count, commit-only, input memory) that have
  * arrived, and proves them together as whir_prove_batch does, every pass of
  * the group in one launch.  max_group bounds a group (1: every job alone;
- * 0: the default, 256); a group also holds at most 2^26 evaluations in all
+ * 0: the default, 64); a group also holds at most 2^26 evaluations in all
  * and shrinks to fit the device budget.  Proof bytes do not change. */
 WHIR_API int whir_server_set_lockstep(whir_server *s, int max_group);
 WHIR_API int whir_server_free(whir_server *s);

@@ -57,6 +57,7 @@ def _bind(L):
         "wo_fe_from_u32": (c.c_uint32, [c.c_uint32]),
         "wo_fe_to_u32": (c.c_uint32, [c.c_uint32]),
         "wo_fe_mul": (c.c_uint32, [c.c_uint32, c.c_uint32]),
+        "wo_set_packed": (None, [c.c_int]),
         "wo_fe_add": (c.c_uint32, [c.c_uint32, c.c_uint32]),
         "wo_fe_inv": (c.c_uint32, [c.c_uint32]),
         "wo_ext_mul": (None, [u32p, u32p, u32p]),
@@ -269,3 +270,9 @@ def verify(params, poly_ks, groups, proof):
     cp = np.zeros(1, np.uint32)
     rc = lib().wo_verify(ctypes.byref(prm), ctypes.byref(cl), proof, len(proof), ptr(cp))
     return rc, int(cp[0])
+
+
+def set_packed(on):
+    """Merkle hashing through the lane-packed permutation (the timed baseline);
+    the results are the same as the scalar path's."""
+    lib().wo_set_packed(1 if on else 0)

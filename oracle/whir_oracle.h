@@ -124,6 +124,10 @@ int wo_verify(const wo_params *prm, const wo_claims *cl, const uint8_t *proof,
 /* threads used by the hot loops (OpenMP); 1 when built without OpenMP */
 int wo_threads(void);
 void wo_set_threads(int n);
+/* nonzero: Merkle trees hash WO_LANES leaves / nodes per call through the
+ * lane-packed permutation (the timed baseline); 0 (default): the scalar
+ * permutation.  Same results either way. */
+void wo_set_packed(int on);
 
 #pragma GCC visibility pop
 

@@ -86,6 +86,12 @@ const wo_p2 *p2_get(int width);
 void p2_permute(const wo_p2 *p, fe *state);
 void hash_leaf(const fe *in, size_t n, fe out[8]);
 void compress2(const fe l[8], const fe r[8], fe out[8]);
+/* lane-packed hashing for the timed baseline (wo_packed.c): WO_LANES states
+ * per call, the same results as hash_leaf / compress2 */
+#define WO_LANES 8
+int wo_packed(void);
+void hash_leaves_packed(const fe *rows, size_t row_len, size_t r0, int n, fe *out);
+void compress_nodes_packed(const fe *src, size_t half, size_t i0, int n, fe *dst);
 
 /* ---- challenger + transcript (crates/transcript/src/poseidon.rs) ---- */
 typedef struct {

@@ -183,16 +183,17 @@ void dft_batch(const fe *in, size_t h_in, size_t width, int log_h, fe *out) {
   fe g = fe_two_adic(log_h);
   tw[0] = WO_ONE;
   for (size_t i = 1; i < h / 2; i++) tw[i] = fe_mul(tw[i - 1], g);
+  /* bit-reversed positions, shared by every column */
+  uint32_t *rev = malloc(h * sizeof(uint32_t));
+  rev[0] = 0;
+  for (size_t i = 1; i < h; i++) rev[i] = (rev[i >> 1] >> 1) | ((uint32_t)(i & 1) << (log_h - 1));
 #pragma omp parallel
   {
     fe *a = malloc(h * sizeof(fe));
 #pragma omp for schedule(dynamic)
     for (long long c = 0; c < (long long)width; c++) {
-      for (size_t i = 0; i < h; i++) {
-        size_t r = 0;
-        for (int b = 0; b < log_h; b++) r |= ((i >> b) & 1) << (log_h - 1 - b);
-        a[r] = i < h_in ? in[i * width + c] : 0;
-      }
+      memset(a, 0, h * sizeof(fe));
+      for (size_t i = 0; i < h_in; i++) a[rev[i]] = in[i * width + c];
       for (int s = 1; s <= log_h; s++) {
         size_t m = (size_t)1 << s, half = m / 2, step = h / m;
         for (size_t blk = 0; blk < h; blk += m)
@@ -206,6 +207,7 @@ void dft_batch(const fe *in, size_t h_in, size_t width, int log_h, fe *out) {
     }
     free(a);
   }
+  free(rev);
   free(tw);
 }
 void wo_dft_batch(const uint32_t *in, size_t h_in, size_t width, int log_h_out,
@@ -227,6 +229,23 @@ void tree_build(wo_tree *t, const fe *rows, int log_h, size_t row_len) {
   t->row_len = row_len;
   t->rows = rows;
   t->nodes = malloc((2 * h - 1) * 8 * sizeof(fe));
+  if (wo_packed()) {  /* the timed baseline: WO_LANES leaves / nodes per call */
+#pragma omp parallel for schedule(static)
+    for (long long i = 0; i < (long long)h; i += WO_LANES)
+      hash_leaves_packed(rows, row_len, (size_t)i,
+                         (int)((long long)h - i < WO_LANES ? (long long)h - i : WO_LANES),
+                         t->nodes + (size_t)i * 8);
+    for (int l = 0; l < log_h; l++) {
+      size_t n = h >> l, half = n / 2;
+      fe *src = t->nodes + level_off(log_h, l), *dst = t->nodes + level_off(log_h, l + 1);
+#pragma omp parallel for schedule(static)
+      for (long long i = 0; i < (long long)half; i += WO_LANES)
+        compress_nodes_packed(src, half, (size_t)i,
+                              (int)((long long)half - i < WO_LANES ? (long long)half - i : WO_LANES),
+                              dst);
+    }
+    return;
+  }
 #pragma omp parallel for schedule(static)
   for (long long i = 0; i < (long long)h; i++)
     hash_leaf(rows + (size_t)i * row_len, row_len, t->nodes + (size_t)i * 8);

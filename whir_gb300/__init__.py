@@ -553,18 +553,18 @@ def prove_batch(ctx, params, polys, claims=1, commit_only=False):
             keep.append(a)
             ptrs[i] = a.ctypes.data
     cap = 64 if commit_only else proof_bound(p, claims)
-    buf = ctypes.create_string_buffer(cap * max(1, n))
+    buf = np.empty(cap * max(1, n), np.uint8)  # filled by the library up to each length
     lens = (ctypes.c_size_t * max(1, n))()
     cps = np.zeros(max(1, n), np.uint32)
     _check(lib().whir_prove_batch(ctx.h, ctypes.byref(p), ptrs, 1 if on_device else 0, n,
-                                  0 if commit_only else claims, 1 if commit_only else 0, buf, cap,
-                                  lens, cps.ctypes.data_as(u32p)))
-    raw = buf.raw  # one copy of the whole buffer
+                                  0 if commit_only else claims, 1 if commit_only else 0,
+                                  ctypes.cast(buf.ctypes.data, ctypes.c_char_p), cap, lens,
+                                  cps.ctypes.data_as(u32p)))
     out = []
     for i in range(n):
         if lens[i] > cap:
             raise WhirError("proof longer than its buffer")
-        out.append((raw[i * cap:i * cap + lens[i]], int(cps[i])))
+        out.append((buf[i * cap:i * cap + lens[i]].tobytes(), int(cps[i])))
     return out
 
 

@@ -302,11 +302,10 @@ RunStats Server::run(std::vector<Job> &jobs, bool honor_arrival) {
         polys.push_back(group[i]->poly);
       }
       w->group_prover->prove(tp, polys, head.on_device, head.commit_only ? 0 : head.n_claims,
-                             head.commit_only);
-      for (size_t i = 0; i < group.size(); i++) {
-        group[i]->checkpoint = ts[i].draw_fe();
-        group[i]->proof = ts[i].bytes();
-      }
+                             head.commit_only, [&](int i) {
+                               group[i]->checkpoint = ts[i].draw_fe();
+                               group[i]->proof = ts[i].bytes();
+                             });
       return w->bytes();
     }
     Job &job = *group[0];

@@ -123,7 +123,7 @@ class Server {
   // Lock-step groups of same-shape jobs (BatchProver): at most max_group
   // jobs per group; 1 proves every job alone; 0 restores the default.
   void set_lockstep(int max_group) { lockstep_ = max_group > 0 ? max_group : kLockstepDefault; }
-  static constexpr int kLockstepDefault = 256;
+  static constexpr int kLockstepDefault = 64;
   // a group holds at most 2^kGroupLog evaluations in all
   static constexpr int kGroupLog = 26;
   // jobs of at least 2^kPriorityK evaluations run on high-priority streams

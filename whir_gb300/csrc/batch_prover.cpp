@@ -14,6 +14,7 @@
 
 #include <algorithm>
 #include <atomic>
+#include <chrono>
 #include <condition_variable>
 #include <exception>
 #include <mutex>
@@ -28,15 +29,19 @@ using kb::E4;
 using namespace kb;
 
 // ---------------- host pool ----------------
+// Helpers wait for work by spinning on the generation counter for a short
+// while (a round trip's host work arrives every few tens of microseconds,
+// and a condition-variable wake-up of 15 threads costs about as much), then
+// sleep on the condition variable.
 struct HostPool::State {
   std::mutex mu;
-  std::condition_variable cv, done_cv;
+  std::condition_variable cv;
   const std::function<void(int)> *fn = nullptr;
   int n = 0;
   std::atomic<int> next{0};
-  int active = 0;  // helpers not yet finished with the current generation
-  unsigned long gen = 0;
-  bool stop = false;
+  std::atomic<int> active{0};  // helpers not yet finished with the current generation
+  std::atomic<unsigned long> gen{0};
+  std::atomic<bool> stop{false};
   std::exception_ptr err;
   std::vector<std::thread> th;
   void work() {
@@ -58,15 +63,20 @@ HostPool::HostPool(int threads) : s_(new State), threads_(std::max(1, threads)) 
     s_->th.emplace_back([s = s_] {
       unsigned long seen = 0;
       for (;;) {
-        {
-          std::unique_lock<std::mutex> l(s->mu);
-          s->cv.wait(l, [&] { return s->stop || s->gen != seen; });
-          if (s->stop) return;
-          seen = s->gen;
+        auto t0 = std::chrono::steady_clock::now();
+        unsigned spins = 0;
+        while (s->gen.load(std::memory_order_acquire) == seen && !s->stop.load()) {
+          if ((++spins & 255) == 0 &&
+              std::chrono::steady_clock::now() - t0 > std::chrono::microseconds(200)) {
+            std::unique_lock<std::mutex> l(s->mu);
+            s->cv.wait(l, [&] { return s->stop.load() || s->gen.load() != seen; });
+          }
+          std::this_thread::yield();
         }
+        if (s->stop.load()) return;
+        seen = s->gen.load(std::memory_order_acquire);
         s->work();
-        std::lock_guard<std::mutex> l(s->mu);
-        if (--s->active == 0) s->done_cv.notify_all();
+        s->active.fetch_sub(1, std::memory_order_acq_rel);
       }
     });
 }
@@ -74,7 +84,7 @@ HostPool::HostPool(int threads) : s_(new State), threads_(std::max(1, threads)) 
 HostPool::~HostPool() {
   {
     std::lock_guard<std::mutex> l(s_->mu);
-    s_->stop = true;
+    s_->stop.store(true);
   }
   s_->cv.notify_all();
   for (auto &t : s_->th) t.join();
@@ -93,15 +103,16 @@ void HostPool::run(int n, const std::function<void(int)> &fn) {
     s_->n = n;
     s_->next.store(0);
     s_->err = nullptr;
-    s_->active = threads_ - 1;
-    s_->gen++;
+    s_->active.store(threads_ - 1);
+    s_->gen.fetch_add(1, std::memory_order_acq_rel);
   }
   s_->cv.notify_all();
   s_->work();
+  // every helper has left this generation's work before fn goes out of scope
+  while (s_->active.load(std::memory_order_acquire) != 0) std::this_thread::yield();
   std::exception_ptr err;
   {
-    std::unique_lock<std::mutex> l(s_->mu);
-    s_->done_cv.wait(l, [&] { return s_->active == 0; });
+    std::lock_guard<std::mutex> l(s_->mu);
     err = s_->err;
   }
   if (err) std::rethrow_exception(err);
@@ -810,13 +821,13 @@ struct BatchProver::Impl {
     uint32_t *hr = stage_host<uint32_t>(ro);
     int *hf = stage_host<int>(fo);
     E4 *hrs = stage_host<E4>(rso);
-    for (int b = 0; b < B; b++) {
+    par([&](int b) {
       hf[b] = (int)(qoff[b] * T);
       for (size_t i = 0; i < in[b].idx.size(); i++)
         for (size_t t = 0; t < T; t++)
           hr[(qoff[b] + i) * T + t] = (uint32_t)((in[b].idx[i] & (S - 1)) + t * S);
       std::copy(in[b].rs.begin(), in[b].rs.end(), hrs + (size_t)b * ks);
-    }
+    });
     hf[B] = (int)(n * T);
     stage_upload();
     if ((int)in[0].rs.size() != ks) throw WhirError(-5, "fold_with_code after the SVO rounds only");
@@ -952,7 +963,8 @@ struct BatchProver::Impl {
   }
 
   void prove(const std::vector<Transcript *> &ts, const std::vector<const uint32_t *> &polys,
-             bool on_device, int n_claims, bool commit_only) {
+             bool on_device, int n_claims, bool commit_only,
+             const std::function<void(int)> &finish) {
     B = (int)ts.size();
     if (B < 1 || polys.size() != ts.size()) throw WhirError(-1, "batch of no instances");
     if (B > BatchProver::max_batch(p)) throw WhirError(-1, "batch too large for these parameters");
@@ -965,6 +977,8 @@ struct BatchProver::Impl {
     }
     stage_off = stage_copied = 0;
     defer_off = 0;
+    const size_t cap = commit_only ? 64 : proof_bytes_max(p, n_claims) + 64;
+    par([&](int b) { in[b].ts->reserve(cap); });
     // reductions publish and re-zero their accumulators; start from zero
     cuda_check(cudaMemsetAsync(acc.as<void>(), 0, acc.bytes(), st()), "memset");
     const size_t n = (size_t)1 << p.k;
@@ -973,7 +987,10 @@ struct BatchProver::Impl {
                             on_device ? cudaMemcpyDeviceToDevice : cudaMemcpyHostToDevice),
                  "poly copy");
     encode_commit(stacked.as<uint32_t>(), p.k, p.rate, 1, cw0.as<uint32_t>(), tree0.as<uint32_t>(), &t0);
-    if (commit_only) return;
+    if (commit_only) {
+      if (finish) par(finish);
+      return;
+    }
     for (int c = 0; c < n_claims; c++) {  // the harness's claim groups (test.rs:225-231)
       par([&](int b) {
         in[b].pt.resize(p.k);
@@ -988,6 +1005,7 @@ struct BatchProver::Impl {
       });
     }
     open();
+    if (finish) par(finish);
   }
 };
 
@@ -1007,8 +1025,8 @@ void BatchProver::reserve(int batch) { m_->reserve(batch, 16); }
 size_t BatchProver::device_bytes() const { return m_->device_bytes(); }
 void BatchProver::prove(const std::vector<Transcript *> &ts,
                         const std::vector<const uint32_t *> &polys, bool on_device, int n_claims,
-                        bool commit_only) {
-  m_->prove(ts, polys, on_device, n_claims, commit_only);
+                        bool commit_only, const std::function<void(int)> &finish) {
+  m_->prove(ts, polys, on_device, n_claims, commit_only, finish);
 }
 
 }  // namespace whir

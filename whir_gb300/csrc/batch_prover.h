@@ -49,8 +49,11 @@ class BatchProver {
   // memory), then n_claims times draw one expanded point and write the
   // evaluation, then open; commit_only stops after the root.  ts[b] are the
   // instances' transcripts (fresh).  1 <= ts.size() <= max_batch(params).
+  // finish (optional) runs once per instance on the host pool after its
+  // proof is complete (the caller's read-out of ts[b]).
   void prove(const std::vector<Transcript *> &ts, const std::vector<const uint32_t *> &polys,
-             bool on_device, int n_claims, bool commit_only);
+             bool on_device, int n_claims, bool commit_only,
+             const std::function<void(int)> &finish = nullptr);
   // grow the device buffers for `batch` instances of the current parameters
   void reserve(int batch);
   size_t device_bytes() const;

@@ -666,13 +666,14 @@ int whir_prove_batch(whir_ctx *ctx, const whir_params *params, const uint32_t *c
   std::vector<whir::Transcript *> tp(batch);
   std::vector<const uint32_t *> pp(polys, polys + batch);
   for (int b = 0; b < batch; b++) tp[b] = &ts[b];
-  ctx->batch->prove(tp, pp, on_device != 0, n_claims, commit_only != 0);
-  for (int b = 0; b < batch; b++) {
+  // each instance's read-out runs on the prover's host pool
+  ctx->batch->prove(tp, pp, on_device != 0, n_claims, commit_only != 0, [&](int b) {
     checkpoints[b] = ts[b].draw_fe();
     const std::vector<uint8_t> &bytes = ts[b].bytes();
     proof_len[b] = bytes.size();
-    if (proof_cap) memcpy(proofs + (size_t)b * proof_cap, bytes.data(), std::min(proof_cap, bytes.size()));
-  }
+    if (proof_cap)
+      memcpy(proofs + (size_t)b * proof_cap, bytes.data(), std::min(proof_cap, bytes.size()));
+  });
   API_END
 }
 

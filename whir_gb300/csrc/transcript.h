@@ -59,6 +59,8 @@ class Transcript {
   uint32_t draw_fe() { return ch_.sample(); }
   size_t draw_bits(int bits) { return ch_.sample_bits(bits); }
   const std::vector<uint8_t> &bytes() const { return bytes_; }
+  // room for a proof of up to n bytes without reallocating
+  void reserve(size_t n) { bytes_.reserve(n); }
 
  private:
   void put(uint32_t v) {
