@@ -29,17 +29,20 @@ using kb::E4;
 using namespace kb;
 
 // ---------------- host pool ----------------
-// Helpers wait for work by spinning on the generation counter for a short
-// while (a round trip's host work arrives every few tens of microseconds,
-// and a condition-variable wake-up of 15 threads costs about as much), then
-// sleep on the condition variable.
+// A run wakes only as many helpers as its work needs (run's `parts`).  A
+// helper that took part spins on the generation counter for a short while
+// before sleeping on the condition variable (a round trip's host work comes
+// every few tens of microseconds, and waking sleeping threads costs about as
+// much); helpers that were not needed go straight back to sleep, so that
+// many small groups proving side by side do not keep the host cores busy.
 struct HostPool::State {
   std::mutex mu;
   std::condition_variable cv;
   const std::function<void(int)> *fn = nullptr;
   int n = 0;
+  int helpers = 0;  // helpers taking part in the current generation
   std::atomic<int> next{0};
-  std::atomic<int> active{0};  // helpers not yet finished with the current generation
+  std::atomic<int> active{0};  // taking part and not yet finished
   std::atomic<unsigned long> gen{0};
   std::atomic<bool> stop{false};
   std::exception_ptr err;
@@ -60,21 +63,30 @@ struct HostPool::State {
 
 HostPool::HostPool(int threads) : s_(new State), threads_(std::max(1, threads)) {
   for (int t = 1; t < threads_; t++)
-    s_->th.emplace_back([s = s_] {
+    s_->th.emplace_back([s = s_, t] {
       unsigned long seen = 0;
+      bool spin = false;  // took part in the last generation
       for (;;) {
-        auto t0 = std::chrono::steady_clock::now();
-        unsigned spins = 0;
-        while (s->gen.load(std::memory_order_acquire) == seen && !s->stop.load()) {
-          if ((++spins & 255) == 0 &&
-              std::chrono::steady_clock::now() - t0 > std::chrono::microseconds(200)) {
-            std::unique_lock<std::mutex> l(s->mu);
-            s->cv.wait(l, [&] { return s->stop.load() || s->gen.load() != seen; });
+        if (spin) {
+          auto t0 = std::chrono::steady_clock::now();
+          unsigned spins = 0;
+          while (s->gen.load(std::memory_order_acquire) == seen && !s->stop.load()) {
+            if ((++spins & 63) == 0 &&
+                std::chrono::steady_clock::now() - t0 > std::chrono::microseconds(50))
+              break;
+            std::this_thread::yield();
           }
-          std::this_thread::yield();
         }
-        if (s->stop.load()) return;
-        seen = s->gen.load(std::memory_order_acquire);
+        int helpers;
+        {
+          std::unique_lock<std::mutex> l(s->mu);
+          s->cv.wait(l, [&] { return s->stop.load() || s->gen.load() != seen; });
+          if (s->stop.load()) return;
+          seen = s->gen.load();
+          helpers = s->helpers;
+        }
+        spin = t <= helpers;
+        if (!spin) continue;
         s->work();
         s->active.fetch_sub(1, std::memory_order_acq_rel);
       }
@@ -91,9 +103,10 @@ HostPool::~HostPool() {
   delete s_;
 }
 
-void HostPool::run(int n, const std::function<void(int)> &fn) {
+void HostPool::run(int n, const std::function<void(int)> &fn, int parts) {
   if (n <= 0) return;
-  if (threads_ == 1 || n == 1) {
+  const int helpers = std::min({threads_, std::max(1, parts), n}) - 1;
+  if (helpers <= 0) {
     for (int i = 0; i < n; i++) fn(i);
     return;
   }
@@ -101,9 +114,10 @@ void HostPool::run(int n, const std::function<void(int)> &fn) {
     std::lock_guard<std::mutex> l(s_->mu);
     s_->fn = &fn;
     s_->n = n;
+    s_->helpers = helpers;
     s_->next.store(0);
     s_->err = nullptr;
-    s_->active.store(threads_ - 1);
+    s_->active.store(helpers);
     s_->gen.fetch_add(1, std::memory_order_acq_rel);
   }
   s_->cv.notify_all();
@@ -258,7 +272,8 @@ struct BatchProver::Impl {
   Impl(Context *c, const Params &pp, int threads) : ctx(c), p(pp), ks(pp.folding), pool(threads) {}
 
   cudaStream_t st() const { return ctx->stream(); }
-  void par(const std::function<void(int)> &fn) { pool.run(B, fn); }
+  // per-instance host work on the pool: one thread per 8 instances
+  void par(const std::function<void(int)> &fn) { pool.run(B, fn, (B + 7) / 8); }
 
   // ---- staging ----
   size_t stage_alloc(size_t bytes) {

@@ -19,16 +19,17 @@
 
 namespace whir {
 
-// A small pool of host threads for per-instance work: run(n, fn) calls
-// fn(0) .. fn(n-1) across the pool and the calling thread, and returns when
-// all are done (rethrowing the first exception).
+// A small pool of host threads for per-instance work: run(n, fn, parts)
+// calls fn(0) .. fn(n-1) on at most `parts` threads (the calling thread and
+// pool helpers), and returns when all are done (rethrowing the first
+// exception).
 class HostPool {
  public:
   explicit HostPool(int threads);
   ~HostPool();
   HostPool(const HostPool &) = delete;
   HostPool &operator=(const HostPool &) = delete;
-  void run(int n, const std::function<void(int)> &fn);
+  void run(int n, const std::function<void(int)> &fn, int parts);
   int threads() const { return threads_; }
 
  private:
