@@ -43,3 +43,49 @@ def test_single_rank_is_a_no_op():
     import bench
     assert bench.max_over_ranks(1.5, 1, "cpu") == 1.5
     assert bench.replica_throughput(1, 30, 0.5) == 60
+
+
+def _prove_rank(rank, world, port, out):
+    # each replica proves its own polynomials (the oracle stands in for the
+    # GPU prover on the CPU), times them, and the job is accounted as
+    # bench.py accounts it: the slowest rank's time, every rank's proofs
+    import time
+    os.environ.update(MASTER_ADDR="127.0.0.1", MASTER_PORT=str(port))
+    dist.init_process_group("gloo", rank=rank, world_size=world)
+    try:
+        import bench
+        from oracle import oracle as O
+        O.lib().wo_set_threads(1)
+        params, steps = (10, 4, 1, 1, 1, 100), 3
+        dist.barrier()
+        t0 = time.perf_counter()
+        proofs = [O.prove(params, [O.rand_fe(100 * rank + s, 1 << 10)], [10], [[0]])
+                  for s in range(steps)]
+        el = time.perf_counter() - t0
+        slowest = bench.max_over_ranks(el, world, "cpu")
+        # every rank's proofs reach rank 0 (a replica's proofs are its own)
+        gathered = [None] * world
+        dist.all_gather_object(gathered, [p[0] for p in proofs])
+        out[rank] = (el, slowest, bench.replica_throughput(world, steps, slowest), gathered)
+    finally:
+        dist.destroy_process_group()
+
+
+def test_two_replicas_prove_independently():
+    world = 2
+    out = mp.Manager().dict()
+    mp.spawn(_prove_rank, args=(world, _free_port(), out), nprocs=world, join=True)
+    from oracle import oracle as O
+    els = [out[r][0] for r in range(world)]
+    for r in range(world):
+        el, slowest, value, gathered = out[r]
+        assert slowest == pytest.approx(max(els))
+        assert value == pytest.approx(world * 3 / max(els))
+        # the same proofs on every rank, and each is the oracle's for its seed
+        assert gathered == out[0][3]
+    for rank in range(world):
+        for s in range(3):
+            want = O.prove((10, 4, 1, 1, 1, 100), [O.rand_fe(100 * rank + s, 1 << 10)], [10],
+                           [[0]])[0]
+            assert out[0][3][rank][s] == want
+    assert out[0][3][0][0] != out[0][3][1][0]  # the replicas' work differs
