@@ -53,7 +53,7 @@ NCU_TRAFFIC_K = 24
 # k = 22 proof, the ncu summary of the leaf hash in profiles/).  With one warp
 # instruction issued per cycle on each of the 4 sub-partitions of each SM,
 # the issue-bound rate is SMs * 4 * 32 * clock / this.
-LEAF_INSTR_PER_PERM24 = 8576
+LEAF_INSTR_PER_PERM24 = 8539
 GB300_SMS = 152
 
 
@@ -431,6 +431,20 @@ def run_batched(W, args, device):
                 "k22_proof_kernel_ms": t22, "k16_proof_kernel_ms_in_group_of_256": t16 / 256,
                 "note": "272 proofs in 16 x the kernel time of one k=22 proof alone"},
             "peak_device_gb": peak / 2 ** 30, "bit_exact_vs_plain": same(a, b)}
+
+        # the small proofs of the mix alone: 256 at k=16
+        mk = lambda: [job(16, 2, 2) for _ in range(256)]
+        a, b = mk(), mk()
+        srv.run(a)
+        sa = min(srv.run(mk())[0] for _ in range(3))
+        a = mk()
+        srv.run(a)
+        one.run(b)
+        sb, _ = one.run(b)
+        out["batched_small"] = {
+            "workload": "256 proofs at k=16, rate 1/4, folding 4, 2 claims each",
+            "proofs_per_s": len(a) / sa, "plain_loop_proofs_per_s": len(b) / sb,
+            "speedup": sb / sa, "bit_exact_vs_plain": same(a, b)}
 
         # cfg: served Poisson stream, an arrival-rate sweep
         sweep = []
