@@ -272,8 +272,8 @@ struct BatchProver::Impl {
   Impl(Context *c, const Params &pp, int threads) : ctx(c), p(pp), ks(pp.folding), pool(threads) {}
 
   cudaStream_t st() const { return ctx->stream(); }
-  // per-instance host work on the pool: one thread per 8 instances
-  void par(const std::function<void(int)> &fn) { pool.run(B, fn, (B + 7) / 8); }
+  // per-instance host work on the pool: one thread per 4 instances
+  void par(const std::function<void(int)> &fn) { pool.run(B, fn, (B + 3) / 4); }
 
   // ---- staging ----
   size_t stage_alloc(size_t bytes) {
