@@ -6,6 +6,8 @@ import ctypes
 import os
 import re
 
+import pytest
+
 ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
 
 
@@ -46,3 +48,15 @@ def test_every_entry_point_has_a_ctypes_signature():
     # the allocation-free entry point is bound by its own test with its signature
     missing = declared - set(W._SIGS) - {"whir_compress_hi_noalloc"}
     assert not missing, sorted(missing)
+
+
+def test_batch_limits_follow_the_dft_indexing():
+    # a lock-step group's batched codewords must fit the DFT's 2^16-word rows
+    # and 32-bit word indexing (no GPU needed: parameter arithmetic only)
+    import whir_gb300 as W
+    assert W.batch_max((16, 4, 2, 1, 1, 100)) == 1023   # extension rows of 64 words
+    assert W.batch_max((22, 4, 2, 1, 1, 100)) == 127    # round 0: 2^19 rows x 64 words
+    assert W.batch_max((10, 4, 1, 1, 1, 100)) == 1024   # no extension round
+    assert W.batch_max((24, 4, 2, 1, 1, 100)) >= 1
+    with pytest.raises(W.WhirError):
+        W.batch_max((3, 4, 1, 1, 1, 100))               # k below the folding
