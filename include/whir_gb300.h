@@ -40,7 +40,7 @@ extern "C" {
 #define WHIR_ERR_ARG (-1)      /* invalid argument or parameters */
 #define WHIR_ERR_CUDA (-2)     /* CUDA runtime error */
 #define WHIR_ERR_NOMEM (-3)    /* device or host allocation failed */
-#define WHIR_ERR_CAPACITY (-4) /* caller buffer too small */
+#define WHIR_ERR_CAPACITY (-4) /* caller buffer too small, or a job beyond the device budget */
 #define WHIR_ERR_INTERNAL (-5)
 
 typedef struct whir_ctx whir_ctx;

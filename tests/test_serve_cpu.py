@@ -173,3 +173,23 @@ def test_groups_keep_heads_in_arrival_order():
         starts.setdefault(round(s[j], 4), []).append(j)
     heads = sorted(min(g) for g in starts.values())
     assert (np.diff([s[h] for h in heads]) >= -1e-4).all()
+
+
+def test_job_that_no_idle_worker_can_hold_fails_instead_of_waiting():
+    # two workers each keep 60 units after their first jobs (buffers only
+    # grow); a later job needing 80 fits the budget of 130 alone, but on
+    # either worker it would add 20 to 120: with nothing running no release
+    # can make room, so it fails with the capacity status instead of waiting
+    s, e, wk, st = W.serve_simulate([0.0, 0.0, 0.05], [60, 60, 80], [0.02, 0.02, 0.01], 2, 130)
+    assert list(st[:2]) == [0, 0]
+    assert st[2] == -4   # WHIR_ERR_CAPACITY
+    assert e[2] < 1.0
+
+
+def test_job_waits_for_the_worker_that_can_hold_it():
+    # the same budget, but one worker keeps 80 units: a second 80-unit job
+    # must wait for that worker (adding nothing there) and succeed
+    s, e, wk, st = W.serve_simulate([0.0, 0.0], [80, 80], [0.03, 0.01], 2, 100)
+    assert (st == 0).all()
+    assert wk[0] == wk[1]
+    assert s[1] >= e[0] - 1e-3

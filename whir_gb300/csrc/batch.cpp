@@ -20,7 +20,8 @@ Admission::Admission(const std::vector<double> &arrival, const std::vector<size_
                      size_t budget, const std::vector<size_t> &held, bool honor_arrival,
                      Clock::time_point t0, const Grouping *grouping)
     : taken_(arrival.size(), 0), grouping_(grouping), arrival_(arrival), need_(need),
-      budget_(budget), honor_(honor_arrival), t0_(t0), held_(held), sync_(new Sync) {
+      budget_(budget), honor_(honor_arrival), t0_(t0), held_(held), blocked_(held.size(), 0),
+      sync_(new Sync) {
   order_.resize(arrival.size());
   for (size_t i = 0; i < order_.size(); i++) order_[i] = i;
   // ties keep submission order
@@ -58,6 +59,7 @@ std::vector<int> Admission::take(int worker, bool *too_big) {
       taken_[j] = 1;
       head_++;
       *too_big = true;
+      running_++;
       sync_->cv.notify_all();
       return {(int)j};
     }
@@ -81,18 +83,46 @@ std::vector<int> Admission::take(int worker, bool *too_big) {
         held_[worker] += grow;
         total_ += grow;
         peak_ = std::max(peak_, total_);
+        running_++;
         sync_->cv.notify_all();
         return group;
       }
       if (group.size() == 1) break;
       group.resize(group.size() / 2);
     }
-    sync_->cv.wait(lock);  // a release may free enough
+    // The head does not fit beside what the other workers hold.  A release
+    // may free enough; but when nothing runs and every worker has found it
+    // does not fit, no release will come: fail it instead of waiting.
+    if (blocked_head_ != j) {
+      std::fill(blocked_.begin(), blocked_.end(), 0);
+      blocked_head_ = j;
+    }
+    blocked_[worker] = 1;
+    if (running_ == 0 && std::all_of(blocked_.begin(), blocked_.end(), [](char b) { return b; })) {
+      taken_[j] = 1;
+      head_++;
+      *too_big = true;
+      running_++;
+      sync_->cv.notify_all();
+      return {(int)j};
+    }
+    sync_->cv.wait(lock);
   }
 }
 
 void Admission::release(int worker, size_t held) {
   std::lock_guard<std::mutex> lock(sync_->mu);
+  running_--;
+  update_held(worker, held);
+}
+
+void Admission::set_held(int worker, size_t held) {
+  std::lock_guard<std::mutex> lock(sync_->mu);
+  update_held(worker, held);
+}
+
+void Admission::update_held(int worker, size_t held) {
+  blocked_head_ = (size_t)-1;  // the holdings changed: every worker looks again
   total_ = total_ - held_[worker] + held;
   held_[worker] = held;
   peak_ = std::max(peak_, total_);
@@ -134,7 +164,7 @@ RunStats run_jobs(std::vector<Job> &jobs, std::vector<void *> &states, std::vect
       void *state = states[w];
       if (state && prepare) {
         try {
-          adm.release(w, prepare(state));
+          adm.set_held(w, prepare(state));
         } catch (const std::exception &e) {
           start_err[w] = e.what();
           state = nullptr;  // its jobs fail with the reason
@@ -160,7 +190,8 @@ RunStats run_jobs(std::vector<Job> &jobs, std::vector<void *> &states, std::vect
           now_held = 0;
         } else if (too_big) {
           status = -4;
-          error = "job needs more device memory than the budget";
+          error = "job does not fit the device budget (alone, or beside the buffers the idle "
+                  "workers keep)";
         } else {
           try {
             now_held = exec(state, group);

@@ -64,16 +64,21 @@ class Admission {
   // Blocks until the next job (in arrival order) may start on `worker`;
   // returns it with the jobs grouped with it (the head first), or an empty
   // list when every job has been handed out.  A job whose need alone exceeds
-  // the budget is returned alone with *too_big set.  A group that does not
+  // the budget is returned alone with *too_big set, and so is a job that no
+  // idle worker can hold next to what the others keep while nothing runs
+  // (buffers only grow, so waiting would never end).  A group that does not
   // fit the budget is halved until it does (down to the head alone).
   std::vector<int> take(int worker, bool *too_big);
   // the worker finished its job and now holds `held` device bytes
   void release(int worker, size_t held);
+  // the worker (taking no job) now holds `held` device bytes
+  void set_held(int worker, size_t held);
   size_t peak_bytes() const { return peak_; }
   const std::vector<size_t> &held() const { return held_; }
 
  private:
   size_t grow_of(int worker, const std::vector<int> &group) const;
+  void update_held(int worker, size_t held);  // with the lock held
   std::vector<size_t> order_;  // job indices by arrival
   std::vector<char> taken_;    // handed out (possibly ahead of the head, in a group)
   const Grouping *grouping_;
@@ -85,6 +90,9 @@ class Admission {
   size_t head_ = 0;
   std::vector<size_t> held_;  // bytes held per worker
   size_t total_ = 0, peak_ = 0;
+  size_t running_ = 0;           // groups handed out and not yet released
+  std::vector<char> blocked_;    // workers that found the head job does not fit
+  size_t blocked_head_ = (size_t)-1;
   struct Sync;
   Sync *sync_;
 };
