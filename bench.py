@@ -468,6 +468,24 @@ def run_batched(W, args, device):
                                  "p99_ms": _pct(lb, 99)},
                 "throughput_ratio": sb / sa,
                 "peak_device_gb": peak / 2 ** 30, "bit_exact_vs_plain": same(a, b)})
+        # GPU time of the saturated stream's jobs, each proved alone: the
+        # summed single-proof kernel time of the 400 jobs (lock-step groups
+        # can beat it for the small shapes; the large ones fill the GPU alone)
+        kt = {}
+        kctx = W.Context(device)
+        try:
+            for (kk, r, c) in sorted(set(spec)):
+                pk = params_of(kk, r)
+                W.prove_harness(kctx, pk, [pool[kk][1]], [kk], [[0]] * c)
+                kt[(kk, r, c)] = kernel_ms(W, kctx, lambda: W.prove_harness(
+                    kctx, pk, [pool[kk][1]], [kk], [[0]] * c))
+        finally:
+            kctx.close()
+        gpu_s = sum(kt[x] for x in spec) * 1e-3
+        sweep[-1]["gpu_time_of_jobs_alone"] = {
+            "proofs_per_s": len(spec) / gpu_s,
+            "frac": sweep[-1]["proofs_per_s"] / (len(spec) / gpu_s),
+            "note": "jobs / summed kernel time of each job proved alone"}
         # the knee: the lowest rate at which the serial loop no longer keeps up
         knee = next((s["arrivals_per_s"] for s in sweep
                      if s["serial_plain"]["proofs_per_s"] < 0.9 * s["arrivals_per_s"]), None)
@@ -479,7 +497,8 @@ def run_batched(W, args, device):
             "saturated": {"arrivals_per_s": top["arrivals_per_s"],
                           "proofs_per_s": top["proofs_per_s"],
                           "serial_plain_proofs_per_s": top["serial_plain"]["proofs_per_s"],
-                          "throughput_ratio": top["throughput_ratio"]},
+                          "throughput_ratio": top["throughput_ratio"],
+                          "gpu_time_of_jobs_alone": top["gpu_time_of_jobs_alone"]},
             "bit_exact_vs_plain": all(s["bit_exact_vs_plain"] for s in sweep)}
     finally:
         srv.close()
