@@ -53,7 +53,7 @@ NCU_TRAFFIC_K = 24
 # k = 22 proof, the ncu summary of the leaf hash in profiles/).  With one warp
 # instruction issued per cycle on each of the 4 sub-partitions of each SM,
 # the issue-bound rate is SMs * 4 * 32 * clock / this.
-LEAF_INSTR_PER_PERM24 = 8539
+LEAF_INSTR_PER_PERM24 = 8109
 GB300_SMS = 152
 
 
@@ -177,7 +177,7 @@ def integer_roofline(k, prof, clk):
                            f"count and the kernel's, ncu) at {mhz:.0f} MHz, 152 SMs x 4 issue "
                            f"slots of 32 lanes",
             "note": "the kernel issues fewer instructions than the structural count; the gap "
-                    "to the issue rate is pipe contention (FMA-heavy 80%, ALU 70%, profiles/)"}
+                    "to the issue rate is pipe contention (FMA-heavy 87%, ALU 67%, profiles/)"}
 
 
 def workload_config(k):
