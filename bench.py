@@ -326,6 +326,41 @@ def kernel_ms(W, ctx, fn):
     return sum(ctx.prof_read(klass)[0] for klass in range(4))
 
 
+def run_batched_verify(W, device, params, jobs):
+    import concurrent.futures as cf
+    proofs = [j.proof for j in jobs]
+    want = [(0, j.checkpoint) for j in jobs]
+    groups = [[0]] * 2
+    vctx = W.Context(device)
+    try:
+        got = W.verify_batch(vctx, params, [16], groups, proofs)
+        times = []
+        for _ in range(5):
+            t0 = time.perf_counter()
+            W.verify_batch(vctx, params, [16], groups, proofs)
+            times.append(time.perf_counter() - t0)
+    finally:
+        vctx.close()
+    sub = proofs[:32]
+    t0 = time.perf_counter()
+    alone = [W.verify(params, [16], groups, p) for p in sub]
+    t_one = time.perf_counter() - t0
+    threads = os.cpu_count() or 1
+    with cf.ThreadPoolExecutor(threads) as ex:
+        list(ex.map(lambda p: W.verify(params, [16], groups, p), proofs[:threads]))
+        t0 = time.perf_counter()
+        pooled = list(ex.map(lambda p: W.verify(params, [16], groups, p), proofs))
+        t_pool = time.perf_counter() - t0
+    best = min(times)
+    return {"workload": "the 256 proofs of batched_small verified (k=16, rate 1/4, folding 4, "
+                        "2 claims)",
+            "proofs_per_s": len(proofs) / best, "ms_per_batch": best * 1e3,
+            "host_one_core_proofs_per_s": len(sub) / t_one,
+            f"host_{threads}_threads_proofs_per_s": len(proofs) / t_pool,
+            "speedup_vs_host_threads": (len(proofs) / best) / (len(proofs) / t_pool),
+            "same_as_whir_verify": got == want and alone == want[:32] and pooled == want}
+
+
 def run_batched(W, args, device):
     """Batched and served proving through the persistent worker pool
     (whir_server_*), each against the plain one-worker loop on the same jobs.
@@ -445,6 +480,12 @@ def run_batched(W, args, device):
             "workload": "256 proofs at k=16, rate 1/4, folding 4, 2 claims each",
             "proofs_per_s": len(a) / sa, "plain_loop_proofs_per_s": len(b) / sb,
             "speedup": sb / sa, "bit_exact_vs_plain": same(a, b)}
+
+        # those 256 proofs verified: whir_verify_batch (transcript passes on
+        # host threads, every Merkle opening of every proof in one launch)
+        # against whir_verify one proof at a time, on one core and on a
+        # thread per host core
+        out["batched_verify"] = run_batched_verify(W, device, params_of(16, 2), a)
 
         # cfg: served Poisson stream, an arrival-rate sweep
         sweep = []

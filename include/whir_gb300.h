@@ -147,7 +147,10 @@ WHIR_API int whir_fold_code_rounds(whir_ctx *ctx, const uint32_t *codeword, int 
  * a failure ends the proof with WHIR_ERR_ARG and a "debug check" message.
  * The checks add a reduction per round; proofs are unchanged.  Bit 1: NVTX
  * ranges around the prover's phases, named like the reference's tracing
- * spans (whir.rs:19-314, sumcheck/prover.rs:184-497). */
+ * spans (whir.rs:19-314, sumcheck/prover.rs:184-497).  Bit 2: whir_verify
+ * hashes each Merkle opening where it reads it (Whir::verify's order,
+ * whir.rs:361-522) instead of after reading the whole proof (the order
+ * whir_verify_batch uses); the results are the same either way. */
 WHIR_API int whir_debug_set(unsigned flags);
 
 /* Poseidon2KoalaBear<width>::permute_mut on the host (width 16 or 24), with
@@ -217,7 +220,9 @@ WHIR_API int whir_batch_max(const whir_params *params, int32_t *max_batch);
 
 /* Whir::verify (crates/whir/src/whir.rs:361-522, sumcheck/verifier.rs) on the
  * host: checks a proof of whir_prove with the same parameters, polynomial
- * sizes and claim groups.  *result: 0 accepted; 1 the bytes ran out or held a
+ * sizes and claim groups.  The Merkle openings (hints, which no challenge
+ * depends on) are hashed after the rest of the proof is read; the result is
+ * the first failure in Whir::verify's order all the same.  *result: 0 accepted; 1 the bytes ran out or held a
  * non-canonical word; 2 a Merkle opening failed; 3 a final opening disagrees
  * with the final polynomial; 4 the sumcheck's final claim failed; 5 the round
  * structure does not match.  On acceptance *checkpoint (may be NULL) is the
@@ -226,6 +231,20 @@ WHIR_API int whir_verify(const whir_params *params, const int32_t *poly_k, int n
                          const int32_t *group_n, int n_groups, const int32_t *group_ids,
                          const uint8_t *proof, size_t len, int32_t *result,
                          uint32_t *checkpoint);
+/* Many proofs of one shape (the same parameters, polynomial sizes and claim
+ * groups) checked together: results[b] and checkpoints[b] equal whir_verify's
+ * on proofs[b] (lens[b] bytes) alone.  Each proof's transcript pass runs on
+ * host threads with its Merkle openings deferred (they are hints: no
+ * challenge depends on them), then every opening of every proof is hashed
+ * in one GPU launch on ctx's stream, and a proof's result is its first
+ * failure in whir_verify's order.  No counterpart in the reference, whose
+ * Whir::verify (crates/whir/src/whir.rs:361-522) checks one proof per call.
+ * n_proofs >= 0; the call returns when all results are written. */
+WHIR_API int whir_verify_batch(whir_ctx *ctx, const whir_params *params, const int32_t *poly_k,
+                               int n_polys, const int32_t *group_n, int n_groups,
+                               const int32_t *group_ids, int n_proofs,
+                               const uint8_t *const *proofs, const size_t *lens, int32_t *results,
+                               uint32_t *checkpoints);
 
 /* ---- many proofs on one GPU (batched and served proving).  No
  * counterpart in the reference, whose harness proves one polynomial per call

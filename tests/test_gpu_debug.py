@@ -35,5 +35,5 @@ def test_debug_checks_pass_and_proofs_unchanged(ctx, oracle, debug_on, params, g
 
 def test_debug_flags_are_checked():  # no GPU work
     with pytest.raises(W.WhirError):
-        W.debug_set(4)
+        W.debug_set(8)
     W.debug_set(0)

@@ -113,6 +113,10 @@ _SIGS = {
     "whir_tune_reset": (ctypes.c_int, []),
     "whir_verify": (ctypes.c_int, [ctypes.POINTER(Params), i32p, ctypes.c_int, i32p, ctypes.c_int,
                                    i32p, ctypes.c_char_p, ctypes.c_size_t, i32p, u32p]),
+    "whir_verify_batch": (ctypes.c_int, [vp, ctypes.POINTER(Params), i32p, ctypes.c_int, i32p,
+                                         ctypes.c_int, i32p, ctypes.c_int,
+                                         ctypes.POINTER(ctypes.c_void_p),
+                                         ctypes.POINTER(ctypes.c_size_t), i32p, u32p]),
     "whir_server_new": (ctypes.c_int, [ctypes.c_int, ctypes.c_int, ctypes.c_uint64,
                                        ctypes.POINTER(vp)]),
     "whir_server_run": (ctypes.c_int, [vp, ctypes.POINTER(JobC), ctypes.c_int, ctypes.c_int,
@@ -516,12 +520,13 @@ def fold_code_rounds(ctx, dev_codeword, k_data, folding, idx, scales, rs, r):
     return out
 
 
-DEBUG_CHECKS, DEBUG_NVTX = 1, 2
+DEBUG_CHECKS, DEBUG_NVTX, DEBUG_VERIFY_INLINE = 1, 2, 4
 
 
 def debug_set(flags):
-    """whir_debug_set: DEBUG_CHECKS (the reference's debug invariants) and/or
-    DEBUG_NVTX (NVTX ranges); 0 turns the debug mode off."""
+    """whir_debug_set: DEBUG_CHECKS (the reference's debug invariants),
+    DEBUG_NVTX (NVTX ranges) and/or DEBUG_VERIFY_INLINE (verify hashes each
+    opening where it reads it); 0 turns the debug mode off."""
     _check(lib().whir_debug_set(flags))
 
 
@@ -741,6 +746,29 @@ def verify(params, poly_k, groups, proof):
     _check(lib().whir_verify(ctypes.byref(p), ks, len(poly_k), gn, len(groups), gi, bytes(proof),
                              len(proof), ctypes.byref(res), cp.ctypes.data_as(u32p)))
     return res.value, int(cp[0])
+
+
+def verify_batch(ctx, params, poly_k, groups, proofs):
+    """whir_verify_batch: every proof (bytes) checked against the same
+    parameters, polynomial sizes and claim groups, the Merkle openings of all
+    of them hashed in one GPU launch; returns [(result, checkpoint)] as
+    verify() gives for each proof alone."""
+    p = params if isinstance(params, Params) else Params(*params)
+    ks = (ctypes.c_int32 * len(poly_k))(*poly_k)
+    gn = (ctypes.c_int32 * max(1, len(groups)))(*[len(g) for g in groups])
+    flat = [i for g in groups for i in g]
+    gi = (ctypes.c_int32 * max(1, len(flat)))(*flat)
+    n = len(proofs)
+    bufs = [np.frombuffer(bytes(pr), np.uint8) if len(pr) else np.zeros(1, np.uint8)
+            for pr in proofs]
+    ptrs = (ctypes.c_void_p * max(1, n))(*[b.ctypes.data for b in bufs])
+    lens = (ctypes.c_size_t * max(1, n))(*[len(pr) for pr in proofs])
+    res = np.zeros(max(1, n), np.int32)
+    cps = np.zeros(max(1, n), np.uint32)
+    _check(lib().whir_verify_batch(ctx.h, ctypes.byref(p), ks, len(poly_k), gn, len(groups), gi,
+                                   n, ptrs, lens, res.ctypes.data_as(i32p),
+                                   cps.ctypes.data_as(u32p)))
+    return [(int(res[i]), int(cps[i])) for i in range(n)]
 
 
 def autotune(ctx, log_h_lo, log_h_hi):

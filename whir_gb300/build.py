@@ -19,7 +19,7 @@ LIBDIR = os.path.join(HERE, "_lib")
 LIB = os.path.join(LIBDIR, "libwhir_gb300.so")
 
 CU_SOURCES = ["ntt.cu", "merkle.cu", "sumcheck.cu", "noalloc.cu"]
-CPP_SOURCES = ["poseidon2_host.cpp", "transcript.cpp", "svo_host.cpp", "prover.cpp", "batch_prover.cpp", "batch.cpp", "verifier.cpp", "tune.cpp",
+CPP_SOURCES = ["poseidon2_host.cpp", "transcript.cpp", "svo_host.cpp", "prover.cpp", "batch_prover.cpp", "batch.cpp", "verifier.cpp", "verify_batch.cpp", "tune.cpp",
                "capi.cpp"]
 GENCODE = ["-gencode", "arch=compute_103a,code=sm_103a"]
 

@@ -22,6 +22,7 @@
 #include "prover.h"
 #include "tune.h"
 #include "verifier.h"
+#include "verify_batch.h"
 #include "transcript.h"
 
 using whir::Context;
@@ -37,6 +38,7 @@ struct whir_ctx {
   std::unique_ptr<DeviceBuffer> spare_nodes;
   std::mutex spare_mu;
   std::unique_ptr<whir::BatchProver> batch;  // whir_prove_batch's prover, made on first use
+  std::unique_ptr<whir::BatchVerifier> verifier;  // whir_verify_batch's, made on first use
   explicit whir_ctx(int dev) : ctx(dev) {}
 };
 struct whir_transcript {
@@ -501,7 +503,7 @@ int whir_fold_code_rounds(whir_ctx *ctx, const uint32_t *codeword, int k_data, i
 
 int whir_debug_set(unsigned flags) {
   API_BEGIN
-  need((flags & ~3u) == 0, "unknown debug flags");
+  need((flags & ~7u) == 0, "unknown debug flags");
   whir::set_debug(flags);
   API_END
 }
@@ -855,12 +857,8 @@ int whir_serve_simulate_groups(const double *arrival_s, const uint64_t *need_b,
   API_END
 }
 
-int whir_verify(const whir_params *params, const int32_t *poly_k, int n_polys,
-                const int32_t *group_n, int n_groups, const int32_t *group_ids,
-                const uint8_t *proof, size_t len, int32_t *result, uint32_t *checkpoint) {
-  API_BEGIN
-  need(result != nullptr, "null result");
-  std::vector<int> ks = ks_in(poly_k, n_polys);
+static std::vector<std::vector<int>> groups_in(const int32_t *group_n, int n_groups,
+                                               const int32_t *group_ids) {
   need(n_groups >= 0 && (group_n || !n_groups), "bad claim groups");
   std::vector<std::vector<int>> groups;
   size_t off = 0;
@@ -869,9 +867,46 @@ int whir_verify(const whir_params *params, const int32_t *poly_k, int n_polys,
     groups.emplace_back(group_ids + off, group_ids + off + group_n[g]);
     off += group_n[g];
   }
+  return groups;
+}
+
+int whir_verify(const whir_params *params, const int32_t *poly_k, int n_polys,
+                const int32_t *group_n, int n_groups, const int32_t *group_ids,
+                const uint8_t *proof, size_t len, int32_t *result, uint32_t *checkpoint) {
+  API_BEGIN
+  need(result != nullptr, "null result");
+  std::vector<int> ks = ks_in(poly_k, n_polys);
+  std::vector<std::vector<int>> groups = groups_in(group_n, n_groups, group_ids);
   uint32_t cp = 0;
-  *result = (int32_t)whir::verify(params_in(params), ks, groups, proof, len, &cp);
+  if (whir::debug_flags() & whir::DEBUG_VERIFY_INLINE) {
+    *result = (int32_t)whir::verify(params_in(params), ks, groups, proof, len, &cp);
+  } else {
+    // the transcript pass with the openings deferred, then the openings
+    // hashed here: the same pass structure as whir_verify_batch
+    whir::DeferredPaths d;
+    whir::VerifyResult r = whir::verify(params_in(params), ks, groups, proof, len, &cp, &d);
+    std::vector<uint8_t> ok = whir::deferred_paths_ok(proof, len, d);
+    *result = (int32_t)whir::verify_resolve(r, d, ok.data());
+  }
   if (checkpoint) *checkpoint = *result == 0 ? cp : 0;
+  API_END
+}
+
+int whir_verify_batch(whir_ctx *ctx, const whir_params *params, const int32_t *poly_k,
+                      int n_polys, const int32_t *group_n, int n_groups,
+                      const int32_t *group_ids, int n_proofs, const uint8_t *const *proofs,
+                      const size_t *lens, int32_t *results, uint32_t *checkpoints) {
+  API_BEGIN
+  need(ctx != nullptr, "null context");
+  need(n_proofs >= 0 && (n_proofs == 0 || (proofs && lens && results && checkpoints)),
+       "bad proof list");
+  std::vector<int> ks = ks_in(poly_k, n_polys);
+  std::vector<std::vector<int>> groups = groups_in(group_n, n_groups, group_ids);
+  if (!ctx->verifier)
+    ctx->verifier.reset(new whir::BatchVerifier(
+        &ctx->ctx, (int)std::min(16u, std::max(1u, std::thread::hardware_concurrency()))));
+  ctx->verifier->verify(params_in(params), ks, groups, n_proofs, proofs, lens, results,
+                        checkpoints);
   API_END
 }
 

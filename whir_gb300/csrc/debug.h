@@ -1,7 +1,7 @@
 // Debug mode of the provers, off by default (whir_debug_set): the
-// reference's debug-build invariants checked on the device's results, and
-// NVTX ranges named like the reference's tracing spans so that a profiler
-// timeline lines up with them.
+// reference's debug-build invariants checked on the device's results, NVTX
+// ranges named like the reference's tracing spans so that a profiler
+// timeline lines up with them, and the verifier's inline path order.
 #pragma once
 #include <nvtx3/nvToolsExt.h>
 
@@ -16,6 +16,10 @@ enum DebugFlags : unsigned {
   // NVTX ranges around the prover's phases (crates/whir/src/whir.rs:19-314,
   // crates/whir/src/sumcheck/prover.rs:184-497)
   DEBUG_NVTX = 2u,
+  // whir_verify hashes each Merkle opening where it reads it (the order of
+  // Whir::verify, crates/whir/src/whir.rs:361-522) instead of after the
+  // transcript pass (the order whir_verify_batch uses); the same results
+  DEBUG_VERIFY_INLINE = 4u,
 };
 void set_debug(unsigned flags);
 unsigned debug_flags();

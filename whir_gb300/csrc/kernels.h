@@ -85,6 +85,21 @@ struct IdxArgs {
 cudaError_t gather_openings_val(const uint32_t *rows, int row_len, const uint32_t *nodes,
                                 int log_h, const IdxArgs &a, int n, uint32_t *out,
                                 cudaStream_t st);
+// Merkle path checks of many openings (MerkleTree::verify,
+// crates/merkle/src/poseidon_packed.rs:235-257, path check poseidon.rs:22-41):
+// path i's words start at words[d[i].off]: the row (row_len words, hashed as
+// a leaf), then log_h sibling digests bottom-up, as an opening lies in a
+// proof; its root is roots[8 i .. 8 i + 8).  ok[i] = 1 when the path climbs
+// to its root, else 0.  One thread per path; paths sorted by (row_len,
+// log_h) keep warps uniform.  log_h <= 40.
+struct PathDesc {
+  uint64_t off;
+  uint64_t index;
+  int32_t log_h;
+  int32_t row_len;
+};
+cudaError_t verify_paths(const PathDesc *d, const uint32_t *words, const uint32_t *roots, int n,
+                         uint8_t *ok, cudaStream_t st);
 KB_HD size_t tree_words(int log_h) { return (((size_t)2 << log_h) - 1) * 8; }
 KB_HD size_t level_offset_words(int log_h, int level) {
   return (((size_t)2 << log_h) - ((size_t)2 << (log_h - level))) * 8;

@@ -86,6 +86,65 @@ __global__ void hash_rows_generic(const uint32_t *__restrict__ rows, size_t n_ro
   for (int j = 0; j < 8; j++) digests[i * 8 + j] = s[j];
 }
 
+// One opening per thread: the leaf sponge over the row (16 rate words per
+// permutation, a shorter last chunk overwriting only its words), then one
+// width-16 compression per level with the sibling on the side the index's
+// bit names (halves pairing: at a level of 2m nodes, index i >= m is the
+// right child).
+__global__ void __launch_bounds__(128) verify_paths_kernel(const PathDesc *__restrict__ d,
+                                                           const uint32_t *__restrict__ words,
+                                                           const uint32_t *__restrict__ roots,
+                                                           int n, uint8_t *__restrict__ ok) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  const PathDesc pd = d[i];
+  const uint32_t *w = words + pd.off;
+  uint32_t s[24];
+#pragma unroll
+  for (int j = 0; j < 24; j++) s[j] = 0;
+  for (int pos = 0; pos < pd.row_len; pos += 16) {
+    const int take = pd.row_len - pos < 16 ? pd.row_len - pos : 16;
+#pragma unroll
+    for (int j = 0; j < 16; j++)
+      if (j < take) s[j] = w[pos + j];
+    p2_permute<24>(s);
+  }
+  uint32_t acc[8];
+#pragma unroll
+  for (int j = 0; j < 8; j++) acc[j] = s[j];
+  const uint32_t *sib = w + pd.row_len;
+  uint64_t idx = pd.index;
+  for (int l = 0; l < pd.log_h; l++) {
+    const uint64_t mid = 1ull << (pd.log_h - l - 1);
+    const bool right = idx >= mid;
+    uint32_t t[16];
+#pragma unroll
+    for (int j = 0; j < 8; j++) {
+      const uint32_t a = acc[j], b = sib[8 * l + j];
+      t[j] = right ? b : a;
+      t[8 + j] = right ? a : b;
+    }
+    p2_permute<16>(t);
+#pragma unroll
+    for (int j = 0; j < 8; j++) acc[j] = t[j];
+    idx &= mid - 1;
+  }
+  const uint32_t *root = roots + 8 * (size_t)i;
+  bool good = true;
+#pragma unroll
+  for (int j = 0; j < 8; j++) good &= acc[j] == root[j];
+  ok[i] = good ? 1 : 0;
+}
+
+cudaError_t verify_paths(const PathDesc *d, const uint32_t *words, const uint32_t *roots, int n,
+                         uint8_t *ok, cudaStream_t st) {
+  if (n <= 0) return cudaSuccess;
+  const int T = 128;
+  verify_paths_kernel<<<(unsigned)((n + T - 1) / T), T, 0, st>>>(d, words, roots, n, ok);
+  count_launches(1);
+  return cudaGetLastError();
+}
+
 cudaError_t hash_rows(const uint32_t *rows, size_t n_rows, int row_len, uint32_t *digests,
                       cudaStream_t st) {
   if (n_rows == 0) return cudaSuccess;

@@ -104,6 +104,7 @@ class TranscriptReader {
   size_t draw_bits(int bits) { return ch_.sample_bits(bits); }
   bool failed() const { return err_; }
   size_t remaining() const { return n_ - off_; }
+  size_t offset() const { return off_; }  // bytes read so far
 
  private:
   uint32_t take() {

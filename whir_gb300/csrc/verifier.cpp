@@ -40,10 +40,26 @@ void compress(const uint32_t a[8], const uint32_t b[8], uint32_t out[8]) {
 // MerkleTree::verify (crates/merkle/src/poseidon_packed.rs:235-257, path
 // check :22-41): the leaf words, then the siblings bottom to top (halves
 // pairing: the sibling of index i at a level of 2m nodes is i ^ m).
+// With defer, the path is recorded (as read) instead of hashed.
 bool open_path(TranscriptReader &ts, const uint32_t root[8], size_t index, size_t row_len,
-               int log_h, std::vector<uint32_t> &row) {
+               int log_h, std::vector<uint32_t> &row, DeferredPaths *defer) {
+  const size_t word = ts.offset() / 4;
   row.resize(row_len);
   for (size_t i = 0; i < row_len; i++) row[i] = ts.hint_fe();
+  if (defer) {
+    if (log_h < 0 || log_h > 40 || index >= ((size_t)1 << log_h)) return false;
+    uint32_t w[8];
+    for (int l = 0; l < log_h; l++) ts.hint_digest(w);  // read (and range-checked) only
+    if (ts.failed()) return false;  // ran out mid-path: the transcript failure comes first
+    PathCheck c;
+    c.word = word;
+    c.index = (uint64_t)index;
+    c.log_h = log_h;
+    c.row_len = (int)row_len;
+    memcpy(c.root, root, 32);
+    defer->checks.push_back(c);
+    return true;
+  }
   uint32_t acc[8];
   hash_leaf(row.data(), row_len, acc);
   if (log_h < 0 || log_h > 40 || index >= ((size_t)1 << log_h)) return false;
@@ -135,7 +151,7 @@ E4 reduce_round(TranscriptReader &ts, E4 *sum) {
 
 VerifyResult verify(const Params &p, const std::vector<int> &poly_k,
                     const std::vector<std::vector<int>> &groups, const uint8_t *proof, size_t len,
-                    uint32_t *checkpoint) {
+                    uint32_t *checkpoint, DeferredPaths *defer) {
   using namespace kb;
   if (!proof && len) throw WhirError(-1, "null proof");
   Prover::workspace_bytes(p);  // validates the parameters
@@ -224,10 +240,10 @@ VerifyResult verify(const Params &p, const std::vector<int> &poly_k,
     for (size_t q : idx) {
       E4 e;
       if (round == 0) {
-        if (!open_path(ts, comm, q, row_base, kfd, row)) return ts.failed() ? V_TRANSCRIPT : V_MERKLE;
+        if (!open_path(ts, comm, q, row_base, kfd, row, defer)) return ts.failed() ? V_TRANSCRIPT : V_MERKLE;
         e = eval_base_small(row.data(), f, round_point.data());
       } else {
-        if (!open_path(ts, round_comm, q, row_ext, kfd, row))
+        if (!open_path(ts, round_comm, q, row_ext, kfd, row, defer))
           return ts.failed() ? V_TRANSCRIPT : V_MERKLE;
         e = eval_ext_small(reinterpret_cast<const E4 *>(row.data()), f, round_point.data());
       }
@@ -259,11 +275,11 @@ VerifyResult verify(const Params &p, const std::vector<int> &poly_k,
     for (size_t q : idx) {
       E4 e;
       if (have_round_comm) {
-        if (!open_path(ts, round_comm, q, row_ext, kfd, row))
+        if (!open_path(ts, round_comm, q, row_ext, kfd, row, defer))
           return ts.failed() ? V_TRANSCRIPT : V_MERKLE;
         e = eval_ext_small(reinterpret_cast<const E4 *>(row.data()), f, round_point.data());
       } else {
-        if (!open_path(ts, comm, q, row_base, kfd, row)) return ts.failed() ? V_TRANSCRIPT : V_MERKLE;
+        if (!open_path(ts, comm, q, row_base, kfd, row, defer)) return ts.failed() ? V_TRANSCRIPT : V_MERKLE;
         e = eval_base_small(row.data(), f, round_point.data());
       }
       E4 want = horner(fp.data(), fp.size(), e_from(kb::pow(omega, q)));
@@ -278,6 +294,26 @@ VerifyResult verify(const Params &p, const std::vector<int> &poly_k,
   if (ts.failed()) return V_TRANSCRIPT;
   if (checkpoint) *checkpoint = cp;
   return V_OK;
+}
+
+std::vector<uint8_t> deferred_paths_ok(const uint8_t *proof, size_t len, const DeferredPaths &d) {
+  std::vector<uint8_t> ok(d.checks.size());
+  std::vector<uint32_t> w;
+  for (size_t i = 0; i < d.checks.size(); i++) {
+    const PathCheck &c = d.checks[i];
+    const size_t n = (size_t)c.row_len + 8 * (size_t)c.log_h;
+    if (4 * (c.word + n) > len) throw WhirError(-1, "path outside the proof");
+    w.resize(n);
+    memcpy(w.data(), proof + 4 * c.word, 4 * n);  // little-endian words, as bincode writes them
+    ok[i] = merkle_path_ok(c.root, c.index, w.data(), c.row_len, w.data() + c.row_len, c.log_h);
+  }
+  return ok;
+}
+
+VerifyResult verify_resolve(VerifyResult deferred, const DeferredPaths &d, const uint8_t *path_ok) {
+  for (size_t i = 0; i < d.checks.size(); i++)
+    if (!path_ok[i]) return V_MERKLE;
+  return deferred;
 }
 
 }  // namespace whir
