@@ -63,12 +63,33 @@ inline kb::E4 horner(const kb::E4 *c, size_t n, const kb::E4 &x) {
   for (size_t i = n; i-- > 0;) acc = e_add(e_mul(acc, x), c[i]);
   return acc;
 }
+// the same at a base-field point (an extension times base product is four
+// base products)
+inline kb::E4 horner_base(const kb::E4 *c, size_t n, uint32_t x) {
+  using namespace kb;
+  E4 acc = e_zero();
+  for (size_t i = n; i-- > 0;) acc = e_add(e_scale(acc, x), c[i]);
+  return acc;
+}
 // Point::expand: (v, v^2, v^4, ...) (point.rs:115-124)
 inline void expand(kb::E4 *out, int k, kb::E4 v) {
   for (int i = 0; i < k; i++) {
     out[i] = v;
     v = kb::e_sq(v);
   }
+}
+// <eq, poly> with an eq table already built (eq_host): n entries
+inline kb::E4 dot_eq_ext(const kb::E4 *eq, const kb::E4 *poly, size_t n) {
+  using namespace kb;
+  E4 acc = e_zero();
+  for (size_t i = 0; i < n; i++) acc = e_add(acc, e_mul(eq[i], poly[i]));
+  return acc;
+}
+inline kb::E4 dot_eq_base(const kb::E4 *eq, const uint32_t *poly, size_t n) {
+  using namespace kb;
+  E4 acc = e_zero();
+  for (size_t i = 0; i < n; i++) acc = e_add(acc, e_scale(eq[i], poly[i]));
+  return acc;
 }
 // <eq(z), poly> for a short extension poly of 2^k entries
 inline kb::E4 eval_ext_small(const kb::E4 *poly, int k, const kb::E4 *z) {

@@ -2,6 +2,7 @@
 #include "poseidon2_host.h"
 
 #include <mutex>
+#include <utility>
 
 #include "kb.cuh"
 
@@ -70,6 +71,18 @@ struct ChaCha12 {
   }
 };
 
+// Internal diagonals of p3-koala-bear's Poseidon2 (V in M_I = 1 1^T + diag(V)),
+// entry i = sign * num / 2^log_den.
+constexpr int v16[16][3] = {{-1, 2, 0}, {1, 1, 0},  {1, 2, 0},  {1, 1, 1},
+                            {1, 3, 0},  {1, 4, 0},  {-1, 1, 1}, {-1, 3, 0},
+                            {-1, 4, 0}, {1, 1, 8},  {1, 1, 3},  {1, 1, 24},
+                            {-1, 1, 8}, {-1, 1, 3}, {-1, 1, 4}, {-1, 1, 24}};
+constexpr int v24[24][3] = {{-1, 2, 0}, {1, 1, 0},  {1, 2, 0},  {1, 1, 1},  {1, 3, 0},
+                            {1, 4, 0},  {-1, 1, 1}, {-1, 3, 0}, {-1, 4, 0}, {1, 1, 8},
+                            {1, 1, 2},  {1, 1, 3},  {1, 1, 4},  {1, 1, 5},  {1, 1, 6},
+                            {1, 1, 24}, {-1, 1, 8}, {-1, 1, 3}, {-1, 1, 4}, {-1, 1, 5},
+                            {-1, 1, 6}, {-1, 1, 7}, {-1, 1, 9}, {-1, 1, 24}};
+
 // diag entry sign * num / 2^log_den
 uint32_t diag_value(int sign, uint32_t num, int log_den) {
   uint32_t v = kb::mul(kb::from_canonical(num), kb::inv(kb::pow(kb::from_canonical(2), log_den)));
@@ -77,22 +90,11 @@ uint32_t diag_value(int sign, uint32_t num, int log_den) {
 }
 
 void build(Poseidon2Constants &c, int width) {
-  // Internal diagonals of p3-koala-bear's Poseidon2 (V in M_I = 1 1^T + diag(V)).
-  static const int v16[16][3] = {{-1, 2, 0}, {1, 1, 0},  {1, 2, 0},  {1, 1, 1},
-                                 {1, 3, 0},  {1, 4, 0},  {-1, 1, 1}, {-1, 3, 0},
-                                 {-1, 4, 0}, {1, 1, 8},  {1, 1, 3},  {1, 1, 24},
-                                 {-1, 1, 8}, {-1, 1, 3}, {-1, 1, 4}, {-1, 1, 24}};
-  static const int v24[24][3] = {{-1, 2, 0}, {1, 1, 0},  {1, 2, 0},  {1, 1, 1},  {1, 3, 0},
-                                 {1, 4, 0},  {-1, 1, 1}, {-1, 3, 0}, {-1, 4, 0}, {1, 1, 8},
-                                 {1, 1, 2},  {1, 1, 3},  {1, 1, 4},  {1, 1, 5},  {1, 1, 6},
-                                 {1, 1, 24}, {-1, 1, 8}, {-1, 1, 3}, {-1, 1, 4}, {-1, 1, 5},
-                                 {-1, 1, 6}, {-1, 1, 7}, {-1, 1, 9}, {-1, 1, 24}};
   c.width = width;
   c.rounds_p = width == 16 ? 20 : 23;  // poseidon2_round_numbers_128 for 31-bit p, D = 3
   for (int i = 0; i < width; i++) {
     const int *v = width == 16 ? v16[i] : v24[i];
     c.diag[i] = diag_value(v[0], (uint32_t)v[1], v[2]);
-    c.diag_plain[i] = kb::to_canonical(c.diag[i]);
   }
   ChaCha12 rng(1000);
   for (int r = 0; r < 8; r++)
@@ -100,8 +102,15 @@ void build(Poseidon2Constants &c, int width) {
   for (int r = 0; r < c.rounds_p; r++) c.int_rc[r] = rng.next_field();
 }
 
-// The linear layers in 64-bit lanes with one reduction per output word (the
-// compiler turns % p into a multiply-high and a subtract).
+// x mod p for x < 2^38: 2^31 = 2^24 - 1 (mod p) folds the bits above 31,
+// leaving a value below 2^32 < 3p, then two conditional subtractions.
+inline uint32_t reduce38(uint64_t x) {
+  uint64_t y = (x & 0x7fffffffu) + (x >> 31) * 0x00ffffffull;
+  y = y >= 2ull * kb::P ? y - 2ull * kb::P : y;
+  return (uint32_t)(y >= kb::P ? y - kb::P : y);
+}
+
+// The linear layers in 64-bit lanes with one reduction per output word.
 inline void mat4_wide(uint64_t *x) {
   uint64_t t01 = x[0] + x[1], t23 = x[2] + x[3];
   uint64_t t0123 = t01 + t23;
@@ -112,24 +121,65 @@ inline void mat4_wide(uint64_t *x) {
   uint64_t y2 = t01233 + t23;
   x[0] = y0; x[1] = y1; x[2] = y2; x[3] = y3;
 }
-// light MDS of canonical words: every output below 49 p before its reduction
-void mds_light(uint32_t *s, int w) {
-  uint64_t x[24];
-  for (int i = 0; i < w; i++) x[i] = s[i];
-  for (int i = 0; i < w; i += 4) mat4_wide(x + i);
+// light MDS of canonical words: every output below 49 p < 2^38 before its
+// reduction
+template <int W>
+inline void mds_light(uint32_t *s) {
+  uint64_t x[W];
+  for (int i = 0; i < W; i++) x[i] = s[i];
+  for (int i = 0; i < W; i += 4) mat4_wide(x + i);
   uint64_t sums[4] = {0, 0, 0, 0};
-  for (int i = 0; i < w; i++) sums[i & 3] += x[i];
-  for (int i = 0; i < w; i++) s[i] = (uint32_t)((x[i] + sums[i & 3]) % kb::P);
+  for (int i = 0; i < W; i++) sums[i & 3] += x[i];
+  for (int i = 0; i < W; i++) s[i] = reduce38(x[i] + sums[i & 3]);
 }
-// s_i <- sum + d_i s_i: the Montgomery word times the plain residue d_i is
-// the Montgomery word of the product (below p 2^31 before its reduction)
-void internal_layer(const Poseidon2Constants &c, uint32_t *s) {
-  const int w = c.width;
+// s_i <- sum + d_i s_i with the diagonal's small entries (Montgomery form is
+// linear, so scaling the word scales the element): num in 1..4 as a multiple
+// of x or of p - x; 2^-e as (x + m p) / 2^e with m = -x mod 2^e (exact, since
+// p = 1 mod 2^24), below 2p; every lane below 2^38 before one reduction.
+// Each lane's form is fixed at compile time.
+template <int W, int I>
+inline void internal_lane(uint32_t *s, uint64_t sum) {
+  constexpr int sign = W == 16 ? v16[I][0] : v24[I][0];
+  constexpr int num = W == 16 ? v16[I][1] : v24[I][1];
+  constexpr int e = W == 16 ? v16[I][2] : v24[I][2];
+  const uint64_t x = s[I];
+  uint64_t t;
+  if constexpr (e == 0) {
+    t = sign > 0 ? (uint64_t)num * x : (uint64_t)num * (kb::P - x);
+  } else {
+    const uint64_t m = (0 - x) & ((1ull << e) - 1);
+    const uint64_t y = (x + m * kb::P) >> e;  // < 2p
+    t = sign > 0 ? y : 2ull * kb::P - y;
+  }
+  s[I] = reduce38(sum + t);
+}
+template <int W, int... I>
+inline void internal_lanes(uint32_t *s, uint64_t sum, std::integer_sequence<int, I...>) {
+  (internal_lane<W, I>(s, sum), ...);
+}
+template <int W>
+inline void internal_layer(uint32_t *s) {
   uint64_t total = 0;
-  for (int i = 0; i < w; i++) total += s[i];
-  const uint64_t sum = total % kb::P;
-  for (int i = 0; i < w; i++)
-    s[i] = (uint32_t)((sum + (uint64_t)s[i] * c.diag_plain[i]) % kb::P);
+  for (int i = 0; i < W; i++) total += s[i];
+  internal_lanes<W>(s, reduce38(total), std::make_integer_sequence<int, W>{});
+}
+
+template <int W>
+void permute_w(const Poseidon2Constants &c, uint32_t *s) {
+  using namespace kb;
+  mds_light<W>(s);
+  for (int r = 0; r < 4; r++) {
+    for (int i = 0; i < W; i++) s[i] = cube(add(s[i], c.ext_rc[r][i]));
+    mds_light<W>(s);
+  }
+  for (int r = 0; r < c.rounds_p; r++) {
+    s[0] = cube(add(s[0], c.int_rc[r]));
+    internal_layer<W>(s);
+  }
+  for (int r = 4; r < 8; r++) {
+    for (int i = 0; i < W; i++) s[i] = cube(add(s[i], c.ext_rc[r][i]));
+    mds_light<W>(s);
+  }
 }
 
 }  // namespace
@@ -145,21 +195,8 @@ const Poseidon2Constants &poseidon2_constants(int width) {
 }
 
 void poseidon2_permute_host(const Poseidon2Constants &c, uint32_t *s) {
-  using namespace kb;
-  int w = c.width;
-  mds_light(s, w);
-  for (int r = 0; r < 4; r++) {
-    for (int i = 0; i < w; i++) s[i] = cube(add(s[i], c.ext_rc[r][i]));
-    mds_light(s, w);
-  }
-  for (int r = 0; r < c.rounds_p; r++) {
-    s[0] = cube(add(s[0], c.int_rc[r]));
-    internal_layer(c, s);
-  }
-  for (int r = 4; r < 8; r++) {
-    for (int i = 0; i < w; i++) s[i] = cube(add(s[i], c.ext_rc[r][i]));
-    mds_light(s, w);
-  }
+  if (c.width == 16) permute_w<16>(c, s);
+  else permute_w<24>(c, s);
 }
 
 void std_rng_fill_field(uint64_t seed, uint32_t *out, uint64_t n) {

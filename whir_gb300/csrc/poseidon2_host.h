@@ -16,9 +16,7 @@ struct Poseidon2Constants {
   int rounds_p;
   uint32_t ext_rc[8][24];  // [round][lane], rounds 0..3 initial, 4..7 terminal
   uint32_t int_rc[24];
-  uint32_t diag[24];       // internal matrix 1 1^T + diag(diag)
-  uint32_t diag_plain[24]; // the same entries as plain residues (multiplying a
-                           // Montgomery word by one scales the element)
+  uint32_t diag[24];       // internal matrix 1 1^T + diag(diag), Montgomery form
 };
 
 // Constants for width 16 or 24 (computed once, thread-safe).

@@ -92,6 +92,30 @@ class TranscriptReader {
     for (int i = 0; i < 8; i++) d[i] = read_fe();
   }
   uint32_t hint_fe() { return take(); }
+  // n hint words at once (out == nullptr: read and checked only); the same
+  // words, offset and failure as n hint_fe() calls
+  void hint_words(uint32_t *out, size_t n) {
+    if (n > (n_ - off_) / 4) {
+      for (size_t i = 0; i < n; i++) {
+        const uint32_t v = take();
+        if (out) out[i] = v;
+      }
+      return;
+    }
+    const uint8_t *q = p_ + off_;
+    uint32_t bad = 0;
+    if (out) {
+      for (size_t i = 0; i < n; i++) {
+        const uint32_t v = word_at(q + 4 * i);
+        bad |= (uint32_t)(v >= kb::P);
+        out[i] = v;
+      }
+    } else {
+      for (size_t i = 0; i < n; i++) bad |= (uint32_t)(word_at(q + 4 * i) >= kb::P);
+    }
+    off_ += 4 * n;
+    if (bad) err_ = true;
+  }
   void hint_digest(uint32_t *d) {
     for (int i = 0; i < 8; i++) d[i] = take();
   }
@@ -113,14 +137,17 @@ class TranscriptReader {
       off_ = n_;
       return 0;
     }
-    uint32_t v = (uint32_t)p_[off_] | ((uint32_t)p_[off_ + 1] << 8) |
-                 ((uint32_t)p_[off_ + 2] << 16) | ((uint32_t)p_[off_ + 3] << 24);
+    uint32_t v = word_at(p_ + off_);
     off_ += 4;
     if (v >= kb::P) {
       err_ = true;
       return 0;
     }
     return v;
+  }
+  static uint32_t word_at(const uint8_t *b) {  // little-endian
+    return (uint32_t)b[0] | ((uint32_t)b[1] << 8) | ((uint32_t)b[2] << 16) |
+           ((uint32_t)b[3] << 24);
   }
   const uint8_t *p_;
   size_t n_, off_ = 0;

@@ -45,11 +45,10 @@ bool open_path(TranscriptReader &ts, const uint32_t root[8], size_t index, size_
                int log_h, std::vector<uint32_t> &row, DeferredPaths *defer) {
   const size_t word = ts.offset() / 4;
   row.resize(row_len);
-  for (size_t i = 0; i < row_len; i++) row[i] = ts.hint_fe();
+  ts.hint_words(row.data(), row_len);
   if (defer) {
     if (log_h < 0 || log_h > 40 || index >= ((size_t)1 << log_h)) return false;
-    uint32_t w[8];
-    for (int l = 0; l < log_h; l++) ts.hint_digest(w);  // read (and range-checked) only
+    ts.hint_words(nullptr, 8 * (size_t)log_h);  // read (and range-checked) only
     if (ts.failed()) return false;  // ran out mid-path: the transcript failure comes first
     PathCheck c;
     c.word = word;
@@ -127,13 +126,13 @@ E4 final_value(const FoldingRound &f, const std::vector<E4> &fp, int kp) {
     const E4 *z = f.eq_pts.data() + i * f.kfull;
     w.push_back(e_mul(eval_eq_xy(z, f.rs.data(), nr), eval_ext_small(fp.data(), kp, z + nr)));
   }
+  std::vector<uint32_t> pt(f.kfull);
   for (uint32_t v : f.pow_vars) {
-    std::vector<uint32_t> pt(f.kfull);
     for (int j = 0; j < f.kfull; j++) {
       pt[j] = v;
       v = mul(v, v);
     }
-    E4 e = horner(fp.data(), fp.size(), e_from(pt[nr]));  // eval_univariate
+    E4 e = horner_base(fp.data(), fp.size(), pt[nr]);  // eval_univariate
     w.push_back(e_mul(eval_pow_xy(pt.data(), f.rs.data(), nr), e));
   }
   return horner(w.data(), w.size(), f.alpha);
@@ -218,6 +217,7 @@ VerifyResult verify(const Params &p, const std::vector<int> &poly_k,
   uint32_t round_comm[8];
   bool have_round_comm = false;
   std::vector<uint32_t> row;
+  std::vector<E4> eqr((size_t)1 << f);
   for (int round = 0; round < n_rounds; round++) {
     int kfd, this_rate, prev_rate;
     round_params(p, round, &kfd, &this_rate, &prev_rate);
@@ -237,15 +237,17 @@ VerifyResult verify(const Params &p, const std::vector<int> &poly_k,
     int n_s = n_stir_queries(p.soundness, p.security_level, prev_rate);
     std::vector<size_t> idx = stir_indexes(ts, kfd, n_s);
     uint32_t omega = two_adic_generator(kfd);
+    // eq(round point), shared by every opening of the round
+    eq_host(round_point.data(), f, e_one(), eqr.data());
     for (size_t q : idx) {
       E4 e;
       if (round == 0) {
         if (!open_path(ts, comm, q, row_base, kfd, row, defer)) return ts.failed() ? V_TRANSCRIPT : V_MERKLE;
-        e = eval_base_small(row.data(), f, round_point.data());
+        e = dot_eq_base(eqr.data(), row.data(), eqr.size());
       } else {
         if (!open_path(ts, round_comm, q, row_ext, kfd, row, defer))
           return ts.failed() ? V_TRANSCRIPT : V_MERKLE;
-        e = eval_ext_small(reinterpret_cast<const E4 *>(row.data()), f, round_point.data());
+        e = dot_eq_ext(eqr.data(), reinterpret_cast<const E4 *>(row.data()), eqr.size());
       }
       fn.pow_vars.push_back(kb::pow(omega, q));
       oev.push_back(e);
@@ -272,17 +274,18 @@ VerifyResult verify(const Params &p, const std::vector<int> &poly_k,
     int n_s = n_stir_queries(p.soundness, p.security_level, prev_rate);
     std::vector<size_t> idx = stir_indexes(ts, kfd, n_s);
     uint32_t omega = two_adic_generator(kfd);
+    eq_host(round_point.data(), f, e_one(), eqr.data());
     for (size_t q : idx) {
       E4 e;
       if (have_round_comm) {
         if (!open_path(ts, round_comm, q, row_ext, kfd, row, defer))
           return ts.failed() ? V_TRANSCRIPT : V_MERKLE;
-        e = eval_ext_small(reinterpret_cast<const E4 *>(row.data()), f, round_point.data());
+        e = dot_eq_ext(eqr.data(), reinterpret_cast<const E4 *>(row.data()), eqr.size());
       } else {
         if (!open_path(ts, comm, q, row_base, kfd, row, defer)) return ts.failed() ? V_TRANSCRIPT : V_MERKLE;
-        e = eval_base_small(row.data(), f, round_point.data());
+        e = dot_eq_base(eqr.data(), row.data(), eqr.size());
       }
-      E4 want = horner(fp.data(), fp.size(), e_from(kb::pow(omega, q)));
+      E4 want = horner_base(fp.data(), fp.size(), kb::pow(omega, q));
       if (!e_eq(e, want)) return V_STIR;
     }
   }
