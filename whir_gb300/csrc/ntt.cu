@@ -500,8 +500,10 @@ __device__ __forceinline__ void dif_last_v(const uint4 *tile, const TW &tw, int 
   }
 }
 
-template <int C>
-__global__ void __launch_bounds__(256, 4) dft_tile_v2(const uint32_t *__restrict__ in,
+// MINB: CTAs per SM the registers must allow; tiles of more than 48 KB fit
+// three per SM by shared memory, so they take up to 80 registers a thread
+template <int C, int MINB>
+__global__ void __launch_bounds__(256, MINB) dft_tile_v2(const uint32_t *__restrict__ in,
                                                    uint32_t *__restrict__ out, int S, int lg,
                                                    uint32_t width, uint32_t rows_valid,
                                                    uint32_t a_in, uint32_t b_in, uint32_t a_out,
@@ -550,11 +552,16 @@ static cudaError_t launch_tile_v(const uint32_t *in, uint32_t *out, int S, size_
   int threads = (int)(rows * (C / 4) / 8);
   threads = threads < 32 ? 32 : (threads > 256 ? 256 : threads);
   dim3 grid((unsigned)(width / C), (unsigned)(n_outer >> lg));
-  if (S >= 4)
-    dft_tile_v2<C><<<grid, threads, rows * C * 4, st>>>(in, out, S, lg, (uint32_t)width,
-                                                (uint32_t)rows_valid, (uint32_t)a_in,
-                                                (uint32_t)b_in, (uint32_t)a_out, (uint32_t)b_out,
-                                                pre_log, tw_log, ix);
+  if (S >= 4 && rows * C * 4 > (48u << 10))
+    dft_tile_v2<C, 3><<<grid, threads, rows * C * 4, st>>>(in, out, S, lg, (uint32_t)width,
+                                                   (uint32_t)rows_valid, (uint32_t)a_in,
+                                                   (uint32_t)b_in, (uint32_t)a_out,
+                                                   (uint32_t)b_out, pre_log, tw_log, ix);
+  else if (S >= 4)
+    dft_tile_v2<C, 4><<<grid, threads, rows * C * 4, st>>>(in, out, S, lg, (uint32_t)width,
+                                                   (uint32_t)rows_valid, (uint32_t)a_in,
+                                                   (uint32_t)b_in, (uint32_t)a_out,
+                                                   (uint32_t)b_out, pre_log, tw_log, ix);
   else
     dft_tile_v<C><<<grid, threads, smem, st>>>(in, out, S, lg, (uint32_t)width,
                                                (uint32_t)rows_valid, (uint32_t)a_in, (uint32_t)b_in,
@@ -716,8 +723,10 @@ cudaError_t init_device_tables() {
   if (e == cudaSuccess) e = cudaFuncSetAttribute(dft_tile<1>, cudaFuncAttributeMaxDynamicSharedMemorySize, tile_smem_max(1));
   if (e == cudaSuccess) e = cudaFuncSetAttribute(dft_tile_v<8>, cudaFuncAttributeMaxDynamicSharedMemorySize, tile_smem_max(8));
   if (e == cudaSuccess) e = cudaFuncSetAttribute(dft_tile_v<4>, cudaFuncAttributeMaxDynamicSharedMemorySize, tile_smem_max(4));
-  if (e == cudaSuccess) e = cudaFuncSetAttribute(dft_tile_v2<8>, cudaFuncAttributeMaxDynamicSharedMemorySize, tile_smem_max(8));
-  if (e == cudaSuccess) e = cudaFuncSetAttribute(dft_tile_v2<4>, cudaFuncAttributeMaxDynamicSharedMemorySize, tile_smem_max(4));
+  if (e == cudaSuccess) e = cudaFuncSetAttribute(dft_tile_v2<8, 3>, cudaFuncAttributeMaxDynamicSharedMemorySize, tile_smem_max(8));
+  if (e == cudaSuccess) e = cudaFuncSetAttribute(dft_tile_v2<4, 3>, cudaFuncAttributeMaxDynamicSharedMemorySize, tile_smem_max(4));
+  if (e == cudaSuccess) e = cudaFuncSetAttribute(dft_tile_v2<8, 4>, cudaFuncAttributeMaxDynamicSharedMemorySize, tile_smem_max(8));
+  if (e == cudaSuccess) e = cudaFuncSetAttribute(dft_tile_v2<4, 4>, cudaFuncAttributeMaxDynamicSharedMemorySize, tile_smem_max(4));
   if (e == cudaSuccess) done[dev] = true;
   return e;
 }
