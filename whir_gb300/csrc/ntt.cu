@@ -18,9 +18,12 @@
 // CTA owns 8 columns = 32 bytes of every row it touches).  Zero padding is
 // never materialised: rows >= h_in are read as zero in pass 1.
 #include <atomic>
+#include <type_traits>
 #include <mutex>
 
 #include "kernels.h"
+
+#include <type_traits>
 
 namespace whir {
 namespace gpu {
@@ -274,9 +277,25 @@ __device__ __forceinline__ uint32_t shoup_mul(uint32_t d, uint2 w) {  // d < 2^3
 struct TwShoup {
   const uint2 *t;
   __device__ __forceinline__ uint4 submul(uint4 a, uint4 b, int i) const {
-    uint2 w = t[i];
+    return submul_w(a, b, t[i]);
+  }
+  static __device__ __forceinline__ uint4 submul_w(uint4 a, uint4 b, uint2 w) {
     return make_uint4(shoup_mul(a.x - b.x + kb::P, w), shoup_mul(a.y - b.y + kb::P, w),
                       shoup_mul(a.z - b.z + kb::P, w), shoup_mul(a.w - b.w + kb::P, w));
+  }
+};
+
+// The 7 twiddles of a radix-8 task with block offset j, in the order
+// dif_step_v reads them (entry hh + j + tl q with hh = H >> st): stage 0's
+// four in slots 0..3, stage 1's two in 4..5, stage 2's one in 6.
+struct Tw8 {
+  uint2 w[7];
+  __device__ __forceinline__ void load(const uint2 *t, int H, int j, int q) {
+#pragma unroll
+    for (int tl = 0; tl < 4; tl++) w[tl] = t[H + j + tl * q];
+#pragma unroll
+    for (int tl = 0; tl < 2; tl++) w[4 + tl] = t[(H >> 1) + j + tl * q];
+    w[6] = t[(H >> 2) + j];
   }
 };
 
@@ -290,6 +309,37 @@ __device__ __forceinline__ void dif_step_v(uint4 *tile, const TW &tw, int rows_l
   const int q = 1 << lq;
   const int H = LAST ? (1 << (R - 1)) : (1 << lh);
   const int tasks = (1 << (rows_log - R)) << LV;
+  if constexpr (R == 3 && !LAST && std::is_same<TW, TwShoup>::value) {
+    // every task of a thread has the same block offset j when the block's
+    // task stride is a multiple of q: its 7 twiddles are loaded once
+    if (((blockDim.x >> LV) & (q - 1)) == 0) {
+      Tw8 w8;
+      w8.load(tw.t, H, (threadIdx.x >> LV) & (q - 1), q);
+      for (int task = threadIdx.x; task < tasks; task += blockDim.x) {
+        const int c = task & (V - 1), rest = task >> LV;
+        const int j = rest & (q - 1), blk = rest >> lq;
+        const int base = blk * 2 * H + j;
+        uint4 v[T];
+#pragma unroll
+        for (int t = 0; t < T; t++) v[t] = tile[vrow<C>(base + t * q) * V + c];
+#pragma unroll
+        for (int st = 0; st < R; st++) {
+          const int span = T >> (st + 1);
+#pragma unroll
+          for (int t = 0; t < T; t++) {
+            if (t & span) continue;
+            const int tl = t & (span - 1);
+            uint4 a = v[t], b = v[t + span];
+            v[t] = add4(a, b);
+            v[t + span] = TwShoup::submul_w(a, b, w8.w[(st == 0 ? 0 : st == 1 ? 4 : 6) + tl]);
+          }
+        }
+#pragma unroll
+        for (int t = 0; t < T; t++) tile[vrow<C>(base + t * q) * V + c] = v[t];
+      }
+      return;
+    }
+  }
   for (int task = threadIdx.x; task < tasks; task += blockDim.x) {
     const int c = task & (V - 1), rest = task >> LV;
     const int j = rest & (q - 1), blk = rest >> lq;
@@ -465,6 +515,12 @@ __device__ __forceinline__ void dif_last_v(const uint4 *tile, const TW &tw, int 
   const int n = 1 << S;
   const uint32_t tmask = (1u << tw_log) - 1u;
   const int tasks = (1 << (rows_log - R)) << LV;
+  // the step's only twiddles (entries 3, 5, 6, 7), loaded once per thread
+  uint2 wl[8];
+  wl[3] = tw.t[3];
+  wl[5] = tw.t[5];
+  wl[6] = tw.t[6];
+  wl[7] = tw.t[7];
   for (int task = threadIdx.x; task < tasks; task += blockDim.x) {
     const int c = task & (V - 1), blk = task >> LV;
     const int base = blk * T;
@@ -482,7 +538,7 @@ __device__ __forceinline__ void dif_last_v(const uint4 *tile, const TW &tw, int 
         uint4 a = v[t], b = v[t + span];
         v[t] = add4(a, b);
         if (tl == 0) v[t + span] = sub4(a, b);  // w^0 = 1
-        else v[t + span] = tw.submul(a, b, hh + tl);
+        else v[t + span] = TwShoup::submul_w(a, b, wl[hh + tl]);
       }
     }
 #pragma unroll
@@ -511,7 +567,6 @@ __global__ void __launch_bounds__(256, MINB) dft_tile_v2(const uint32_t *__restr
                                                    const TileIdx ix) {
   constexpr int V = C / 4;
   extern __shared__ uint4 smv[];
-  const int n = 1 << S, rows = n << lg;
   uint4 *tile = smv;
   const TwShoup aux{g_dif2};  // DIF twiddles (global, read through the L1)
   const uint32_t o0 = blockIdx.y << lg;
@@ -519,7 +574,6 @@ __global__ void __launch_bounds__(256, MINB) dft_tile_v2(const uint32_t *__restr
   const uint32_t wv = width / 4;
   const uint4 *in4 = reinterpret_cast<const uint4 *>(in);
   uint4 *out4 = reinterpret_cast<uint4 *>(out);
-  (void)n;
   const int rows_log = S + lg;
   const int r0 = S % 3 == 0 ? 3 : S % 3;
   if (r0 == 1)
