@@ -468,6 +468,16 @@ __device__ __forceinline__ void dif_first_v(uint4 *tile, const TW &tw, int rows_
     const int j = rest & (q - 1), blk = rest >> lq;
     const int base = blk * 2 * H + j;
     uint4 v[T];
+    // the task's rows lie in one sub-transform (T q = 2^S rows), so their
+    // coset pre-twiddles w^(o' i) with i = i0 + t q form a geometric
+    // sequence: two table lookups, then one product per row
+    uint32_t ptw = 0, pstep = 0;
+    if (pre_log) {
+      const uint32_t o = o0 + (uint32_t)(base >> S), i0 = (uint32_t)(base & (n - 1));
+      const uint32_t oo = o >> ix.pre_shift;
+      ptw = root_pow(((oo * i0) & pmask) << (24 - pre_log));
+      pstep = root_pow(((oo * (uint32_t)q) & pmask) << (24 - pre_log));
+    }
 #pragma unroll
     for (int t = 0; t < T; t++) {
       const int r = base + t * q;
@@ -480,11 +490,12 @@ __device__ __forceinline__ void dif_first_v(uint4 *tile, const TW &tw, int rows_
         // theirs stay cached
         if (pre_log) {
           v[t] = __ldg(in4 + row * wv + v0 + c);
-          v[t] = mul4(v[t], root_pow((((o >> ix.pre_shift) * i) & pmask) << (24 - pre_log)));
+          v[t] = mul4(v[t], ptw);
         } else {
           v[t] = __ldcg(in4 + row * wv + v0 + c);
         }
       }
+      if (pre_log && t + 1 < T) ptw = kb::mul(ptw, pstep);
     }
 #pragma unroll
     for (int st = 0; st < R; st++) {
