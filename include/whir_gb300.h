@@ -142,8 +142,11 @@ WHIR_API int whir_fold_code_rounds(whir_ctx *ctx, const uint32_t *codeword, int 
  * Bit 0: the reference's debug-build invariants, checked on the device's
  * results: after the expression build, every sumcheck round of fold and
  * fold_with_code, <poly, weights> equals the claimed sum
- * (crates/whir/src/sumcheck/prover.rs:346,558, expr.rs:68), and every opened
- * Merkle path hashes to its root (crates/merkle/src/poseidon_packed.rs:158-230);
+ * (crates/whir/src/sumcheck/prover.rs:346,558, expr.rs:68), every opened
+ * Merkle path hashes to its root (crates/merkle/src/poseidon_packed.rs:158-230),
+ * and every opened row folded at the round point equals the current
+ * polynomial at its domain point (crates/whir/src/whir.rs:263-264, 287-288,
+ * 331-352; the polynomial is read back once per round, so keep k small);
  * a failure ends the proof with WHIR_ERR_ARG and a "debug check" message.
  * The checks add a reduction per round; proofs are unchanged.  Bit 1: NVTX
  * ranges around the prover's phases, named like the reference's tracing

@@ -3,8 +3,10 @@
 With the reference's debug-build invariants switched on (after the
 expression build and every sumcheck round <poly, weights> equals the claimed
 sum, prover.rs:346,558 and expr.rs:68; every opened Merkle path hashes to its
-root, poseidon_packed.rs:158-230) and NVTX ranges on, proofs must still pass
-every check and equal the oracle's byte for byte.
+root, poseidon_packed.rs:158-230; every opened row folded at the round point
+equals the current polynomial at its domain point, whir.rs:263-264,287-288,
+331-352) and NVTX ranges on, proofs must still pass every check and equal
+the oracle's byte for byte.
 """
 import pytest
 
@@ -25,6 +27,9 @@ def debug_on():
     ((14, 3, 2, 2, 1, 100), [[0]]),
     ((11, 2, 1, 1, 0, 90), [[0], [0], [0]]),
     ((16, 5, 1, 1, 2, 100), [[0]]),
+    ((12, 4, 0, 1, 1, 100), [[0]]),       # rate 1: no STIR queries
+    ((13, 4, 2, 3, 1, 100), [[0], [0]]),  # initial_reduction 3
+    ((9, 4, 1, 1, 1, 100), [[0]]),        # no folding rounds: the final openings on the base tree
 ])
 def test_debug_checks_pass_and_proofs_unchanged(ctx, oracle, debug_on, params, groups):
     k = params[0]

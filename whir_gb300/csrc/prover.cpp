@@ -578,6 +578,42 @@ struct Prover::Impl {
     if (!e_eq(reduce_acc(h), sum))
       throw WhirError(-5, std::string("debug check: <poly, weights> != sum after ") + where);
   }
+  // The reference's debug-build STIR checks (crates/whir/src/whir.rs:263-264,
+  // 287-288, 331-352): every opened row, folded at the round point, equals
+  // the current polynomial evaluated at omega^index (omega of order 2^kfd).
+  // In debug mode only: waits for the gathered rows and reads the polynomial
+  // back (poly_host: the final polynomial, already on the host).
+  void check_stir(const std::vector<size_t> &idx, int kfd, size_t rows_off, size_t per,
+                  int row_len, bool base_rows, const std::vector<E4> &point,
+                  const std::vector<E4> *poly_host) {
+    if (!debug_checks() || idx.empty()) return;
+    if (point.size() > 30 ||
+        ((size_t)1 << point.size()) * (base_rows ? 1 : 4) != (size_t)row_len)
+      throw WhirError(-5, "debug check: the round point does not match the opened rows");
+    sync();
+    std::vector<E4> poly;
+    if (!poly_host) {
+      poly.resize((size_t)1 << kc);
+      E4 *h = (E4 *)ctx->pinned(16 * poly.size());
+      cuda_check(copy_async(*ctx, h, P(), 16 * poly.size(), cudaMemcpyDeviceToHost), "d2h");
+      sync();
+      std::copy(h, h + poly.size(), poly.begin());
+      poly_host = &poly;
+    }
+    const size_t n = (size_t)1 << point.size();
+    std::vector<E4> eq(n);
+    eq_host(point.data(), (int)point.size(), e_one(), eq.data());
+    const uint32_t omega = two_adic_generator(kfd);
+    for (size_t i = 0; i < idx.size(); i++) {
+      const uint32_t *row = defer_ptr(rows_off + per * i);
+      const E4 e = base_rows ? dot_eq_base(eq.data(), row, n)
+                             : dot_eq_ext(eq.data(), reinterpret_cast<const E4 *>(row), n);
+      const E4 want = horner_base(poly_host->data(), poly_host->size(), kb::pow(omega, idx[i]));
+      if (!e_eq(e, want))
+        throw WhirError(-5, "debug check: an opened row does not fold to the polynomial's "
+                            "value at its point");
+    }
+  }
   // pinned space (in words) for device->host results read after a later sync
   size_t defer_alloc(size_t words, Transcript &ts) {
     words = (words + 3) & ~(size_t)3;
@@ -1098,12 +1134,15 @@ struct Prover::Impl {
       std::vector<size_t> idx = stir_indexes(ts, kfd, n_s);
       std::vector<E4> rnew;
       if (round == 0) {
-        query_async(ts, t0, idx);
+        size_t rows_off = query_async(ts, t0, idx);
+        check_stir(idx, kfd, rows_off, (size_t)t0.row_len + 8 * (size_t)t0.log_h, t0.row_len,
+                   true, rs, nullptr);
         rnew = fold_with_code(ts, pts, evs, idx);
       } else {
         const DeviceTree &prev = tr[cur_tree];
         size_t rows_off = query_async(ts, prev, idx);
         size_t per = (size_t)prev.row_len + 8 * (size_t)prev.log_h;
+        check_stir(idx, kfd, rows_off, per, prev.row_len, false, round_point, nullptr);
         uint32_t omega = two_adic_generator(kfd);
         std::vector<uint32_t> vars(idx.size());
         for (size_t i = 0; i < idx.size(); i++) vars[i] = kb::pow(omega, idx[i]);
@@ -1124,8 +1163,11 @@ struct Prover::Impl {
     round_params(n_rounds, &kfd, &this_rate, &prev_rate);
     int n_s = n_stir_queries(p.soundness, p.security_level, prev_rate);
     std::vector<size_t> idx = stir_indexes(ts, kfd, n_s);
-    query_async(ts, cur_tree >= 0 ? tr[cur_tree] : t0, idx);
+    const DeviceTree &last = cur_tree >= 0 ? tr[cur_tree] : t0;
+    size_t rows_off = query_async(ts, last, idx);
     sync();
+    check_stir(idx, kfd, rows_off, (size_t)last.row_len + 8 * (size_t)last.log_h, last.row_len,
+               cur_tree < 0, cur_tree >= 0 ? round_point : rs, &fp);
     fill_pending_hints(ts);
     if (kc != final_rounds) throw WhirError(-1, "final sumcheck size mismatch");
   }
