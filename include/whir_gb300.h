@@ -146,7 +146,9 @@ WHIR_API int whir_fold_code_rounds(whir_ctx *ctx, const uint32_t *codeword, int 
  * Merkle path hashes to its root (crates/merkle/src/poseidon_packed.rs:158-230),
  * and every opened row folded at the round point equals the current
  * polynomial at its domain point (crates/whir/src/whir.rs:263-264, 287-288,
- * 331-352; the polynomial is read back once per round, so keep k small);
+ * 331-352; the polynomial is read back once per round, so keep k small),
+ * and each out-of-domain claim combined over a stacked layout equals the
+ * claim made on the stacked polynomial (sumcheck/prover.rs:257-266);
  * a failure ends the proof with WHIR_ERR_ARG and a "debug check" message.
  * The checks add a reduction per round; proofs are unchanged.  Bit 1: NVTX
  * ranges around the prover's phases, named like the reference's tracing

@@ -5,8 +5,9 @@ expression build and every sumcheck round <poly, weights> equals the claimed
 sum, prover.rs:346,558 and expr.rs:68; every opened Merkle path hashes to its
 root, poseidon_packed.rs:158-230; every opened row folded at the round point
 equals the current polynomial at its domain point, whir.rs:263-264,287-288,
-331-352) and NVTX ranges on, proofs must still pass every check and equal
-the oracle's byte for byte.
+331-352; each virtual claim equals the claim made on the stacked polynomial,
+sumcheck/prover.rs:257-266) and NVTX ranges on, proofs must still pass every
+check and equal the oracle's byte for byte.
 """
 import pytest
 
@@ -36,6 +37,15 @@ def test_debug_checks_pass_and_proofs_unchanged(ctx, oracle, debug_on, params, g
     poly = oracle.rand_fe(77 + k, 1 << k)
     proof, cp = W.prove_harness(ctx, params, [poly], [k], groups)
     assert (proof, cp) == oracle.prove(params, [poly], [k], groups)
+
+
+def test_debug_checks_on_a_stacked_layout(ctx, oracle, debug_on):
+    # five polynomials of three sizes stacked with selector bits: the virtual
+    # claims also equal the claims made on the stacked polynomial directly
+    params, ks, groups = (10, 3, 1, 1, 1, 32), [8, 6, 6, 8, 5], [[0, 3], [1, 2], [4], [3]]
+    polys = [oracle.rand_fe(40 + i, 1 << k) for i, k in enumerate(ks)]
+    got = W.prove_harness(ctx, params, polys, ks, groups)
+    assert got == oracle.prove(params, polys, ks, groups)
 
 
 def test_debug_flags_are_checked():  # no GPU work

@@ -13,7 +13,9 @@ enum DebugFlags : unsigned {
   // expr.rs:68); every opened Merkle path hashes to its root
   // (crates/merkle/src/poseidon_packed.rs:158-230); every opened row folded at
   // the round point equals the polynomial at its domain point
-  // (crates/whir/src/whir.rs:263-264, 287-288, 331-352)
+  // (crates/whir/src/whir.rs:263-264, 287-288, 331-352); each out-of-domain
+  // claim equals the claim made on the stacked polynomial
+  // (crates/whir/src/sumcheck/prover.rs:257-266)
   DEBUG_CHECKS = 1u,
   // NVTX ranges around the prover's phases (crates/whir/src/whir.rs:19-314,
   // crates/whir/src/sumcheck/prover.rs:184-497)

@@ -710,6 +710,21 @@ struct Prover::Impl {
       v.eval = e_add(v.eval, e_mul(weight, c.eval));
       svo.accumulate(v.acc, c, weight, ks);
     }
+    // the debug-build check of ProverLayout::write_virtual_eval
+    // (crates/whir/src/sumcheck/prover.rs:257-266): the same claim made
+    // directly on the stacked polynomial gives the same evaluation and SVO
+    // accumulators
+    if (debug_checks()) {
+      SvoClaim d;
+      svo_claim(d, stacked.as<uint32_t>(), p.k, v.point.data());
+      std::vector<E4> acc2(acc_size(), e_zero());
+      svo.accumulate(acc2, d, e_one(), ks);
+      bool same = e_eq(d.eval, v.eval);
+      for (size_t i = 0; same && i < acc2.size(); i++) same = e_eq(acc2[i], v.acc[i]);
+      if (!same)
+        throw WhirError(-5, "debug check: the virtual claim differs from the claim on the "
+                            "stacked polynomial");
+    }
     ts.write_ext(v.eval);
     virt.push_back(std::move(v));
   }
