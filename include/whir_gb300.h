@@ -311,7 +311,11 @@ WHIR_API int whir_workspace_bytes(const whir_params *params, uint64_t *bytes);
 WHIR_API int whir_proof_bytes_max(const whir_params *params, int n_claims, uint64_t *bytes);
 /* The admission order of whir_serve with a stand-in for the GPU: job j
  * occupies a worker for duration_s[j] seconds (a host sleep) and holds
- * need[j] bytes.  Host only, for testing the scheduling. */
+ * need[j] bytes.  A negative duration injects a failure: the job fails
+ * (status WHIR_ERR_INTERNAL) after |duration_s[j]| seconds with its worker's
+ * buffers grown for it, as a proof that hits a transcript or I/O error
+ * would; the worker goes on with later jobs.  Host only, for testing the
+ * scheduling. */
 WHIR_API int whir_serve_simulate(const double *arrival_s, const uint64_t *need,
                                  const double *duration_s, int n_jobs, int n_workers,
                                  uint64_t device_budget, double *start_s, double *done_s,

@@ -193,3 +193,51 @@ def test_job_waits_for_the_worker_that_can_hold_it():
     assert (st == 0).all()
     assert wk[0] == wk[1]
     assert s[1] >= e[0] - 1e-3
+
+
+INTERNAL = -5  # WHIR_ERR_INTERNAL
+
+
+def test_failed_proof_fails_only_its_job():
+    # job 2 fails 5 ms into its proof (a transcript or I/O error, injected by
+    # a negative duration); the other jobs finish, and its worker goes on
+    # with later jobs
+    n = 10
+    dur = [0.005] * n
+    dur[2] = -0.005
+    s, e, wk, st = W.serve_simulate([0.0] * n, [10] * n, dur, 2, 10 ** 9)
+    assert st[2] == INTERNAL
+    assert all(st[j] == 0 for j in range(n) if j != 2)
+    assert e[2] >= s[2] + 0.005 - 1e-4
+    assert any(wk[j] == wk[2] and s[j] >= e[2] - 1e-4 for j in range(3, n))
+
+
+def test_failed_proof_keeps_its_buffers_in_the_budget():
+    # worker buffers only grow, and a proof that fails has grown its
+    # worker's buffers first (admission reserved them when it handed the
+    # job out): job 0 (need 60) fails on one worker, which then holds 60;
+    # with a budget of 100 a second 60-byte job cannot start on the other
+    # worker beside it, so every later job runs where the 60 bytes already are
+    n = 5
+    need = [60] * n
+    dur = [0.004] * n
+    dur[0] = -0.004
+    s, e, wk, st = W.serve_simulate([0.0] * n, need, dur, 2, 100)
+    assert st[0] == INTERNAL
+    assert all(st[j] == 0 for j in range(1, n))
+    assert len(set(wk)) == 1
+    assert max(held_at_starts(s, need, wk, 2)) <= 100
+
+
+def test_failures_in_groups():
+    # a group's proof fails: every job of the group reports it, the next
+    # group of the same shape proves
+    n = 8
+    shape = [1] * n
+    dur = [0.004] * n
+    dur[0] = -0.004  # the head of the first group
+    s, e, wk, st = W.serve_simulate([0.0] * n, [5] * n, dur, 1, 10 ** 9, shape=shape,
+                                    max_group=4)
+    assert list(st[:4]) == [INTERNAL] * 4
+    assert (st[4:] == 0).all()
+

@@ -713,7 +713,8 @@ def serve_simulate(arrival_s, need_bytes, duration_s, workers, budget_bytes, sha
     """Admission order of whir_serve with host sleeps standing in for proofs:
     returns (start_s, done_s, worker, status) arrays.  With shape (one id per
     job), jobs of equal shape that have arrived are grouped, up to max_group
-    (whir_serve_simulate_groups)."""
+    (whir_serve_simulate_groups).  A negative duration injects a proof that
+    fails after |duration| seconds (status WHIR_ERR_INTERNAL)."""
     n = len(arrival_s)
     A = (ctypes.c_double * max(1, n))(*arrival_s)
     N = (ctypes.c_uint64 * max(1, n))(*[int(x) for x in need_bytes])

@@ -135,7 +135,8 @@ RunStats run_jobs(std::vector<Job> &jobs, std::vector<void *> &states, std::vect
                   const std::function<void *(int worker)> &make_worker,
                   const std::function<size_t(void *state, std::vector<Job *> &group)> &exec,
                   const std::function<size_t(void *state)> &prepare,
-                  const Grouping *grouping) {
+                  const Grouping *grouping,
+                  const std::function<size_t(void *state)> &held_of) {
   const int workers = (int)states.size();
   if (workers < 1 || held.size() != states.size()) throw WhirError(-1, "at least one worker");
   std::vector<double> arr(jobs.size());
@@ -193,15 +194,19 @@ RunStats run_jobs(std::vector<Job> &jobs, std::vector<void *> &states, std::vect
           error = "job does not fit the device budget (alone, or beside the buffers the idle "
                   "workers keep)";
         } else {
+          bool failed = false;
           try {
             now_held = exec(state, group);
           } catch (const WhirError &e) {
             status = e.code;
             error = e.what();
+            failed = true;
           } catch (const std::exception &e) {
             status = -5;
             error = e.what();
+            failed = true;
           }
+          if (failed && held_of) now_held = std::max(now_held, held_of(state));
         }
         const double done = secs();
         for (Job *job : group) {
@@ -376,8 +381,10 @@ RunStats Server::run(std::vector<Job> &jobs, bool honor_arrival) {
     const size_t have = w && w->group_prover ? w->group_prover->device_bytes() : 0;
     return need > have ? need - have : 0;
   };
+  // after a failed proof: what the worker's buffers hold now
+  auto held_of = [](void *state) -> size_t { return static_cast<GpuWorker *>(state)->bytes(); };
   return run_jobs(jobs, states_, held_, budget_, honor_arrival, need, make, exec, nullptr,
-                  lockstep_ > 1 ? &grouping : nullptr);
+                  lockstep_ > 1 ? &grouping : nullptr, held_of);
 }
 
 }  // namespace whir

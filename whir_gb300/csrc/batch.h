@@ -108,14 +108,18 @@ struct RunStats {
 // grouping is given) and returns the device bytes the worker holds
 // afterwards.  held[w] (in/out) is what worker w holds across runs.
 // prepare (optional) runs once on each worker thread before it takes jobs
-// and returns the device bytes the worker then holds.
+// and returns the device bytes the worker then holds.  When exec throws, the
+// group's jobs fail with the error and the worker goes on with later jobs;
+// held_of (optional) then gives what the worker holds (a proof that failed
+// may have grown its buffers first), else its holding before the group.
 RunStats run_jobs(std::vector<Job> &jobs, std::vector<void *> &states, std::vector<size_t> &held,
                   size_t budget, bool honor_arrival,
                   const std::function<size_t(const Params &)> &need,
                   const std::function<void *(int worker)> &make_worker,
                   const std::function<size_t(void *state, std::vector<Job *> &group)> &exec,
                   const std::function<size_t(void *state)> &prepare = nullptr,
-                  const Grouping *grouping = nullptr);
+                  const Grouping *grouping = nullptr,
+                  const std::function<size_t(void *state)> &held_of = nullptr);
 
 // A pool of GPU workers on one device, kept between runs: each worker's
 // stream, pinned staging and prover buffers stay allocated, so a run starts

@@ -5,6 +5,7 @@
 #include <string.h>
 
 #include <algorithm>
+#include <cmath>
 #include <chrono>
 #include <memory>
 #include <mutex>
@@ -790,7 +791,9 @@ int whir_proof_bytes_max(const whir_params *params, int n_claims, uint64_t *byte
 
 // whir_serve's scheduler with host sleeps for proofs; shape (optional):
 // jobs of equal shape id may be grouped, up to max_group per group, a group
-// holding its size times one job's bytes and taking the head job's time
+// holding its size times one job's bytes and taking the head job's time.  A
+// negative duration is a proof that fails after |duration| seconds (a
+// transcript or I/O error), its worker's buffers already grown for it.
 static void simulate(const double *arrival_s, const uint64_t *need_b, const double *duration_s,
                      const int32_t *shape, int max_group, int n_jobs, int n_workers,
                      uint64_t budget, double *start_s, double *done_s, int32_t *worker,
@@ -801,7 +804,7 @@ static void simulate(const double *arrival_s, const uint64_t *need_b, const doub
   std::vector<whir::Job> js(n_jobs);
   std::vector<size_t> nb(n_jobs);
   for (int i = 0; i < n_jobs; i++) {
-    need(duration_s[i] >= 0 && duration_s[i] <= 10, "duration out of range");
+    need(duration_s[i] >= -10 && duration_s[i] <= 10, "duration out of range");
     js[i].arrival = arrival_s[i];
     js[i].params.k = i;  // carries the job index to need()
     nb[i] = (size_t)need_b[i];
@@ -811,11 +814,13 @@ static void simulate(const double *arrival_s, const uint64_t *need_b, const doub
   auto make = [](int) -> void * { return new size_t(0); };
   auto exec = [&](void *state, std::vector<whir::Job *> &group) -> size_t {
     const int h = group[0]->params.k;
-    std::this_thread::sleep_for(std::chrono::duration<double>(duration_s[h]));
     size_t *held = static_cast<size_t *>(state);
     *held = std::max(*held, nb[h] * group.size());
+    std::this_thread::sleep_for(std::chrono::duration<double>(std::fabs(duration_s[h])));
+    if (duration_s[h] < 0) throw whir::WhirError(-5, "injected failure");
     return *held;
   };
+  auto held_of = [](void *state) -> size_t { return *static_cast<size_t *>(state); };
   std::vector<void *> states(n_workers, nullptr);
   std::vector<size_t> held(n_workers, 0);
   whir::Grouping grouping;
@@ -827,7 +832,7 @@ static void simulate(const double *arrival_s, const uint64_t *need_b, const doub
     return want > have ? want - have : 0;
   };
   whir::run_jobs(js, states, held, budget, true, needf, make, exec, nullptr,
-                 shape && max_group > 1 ? &grouping : nullptr);
+                 shape && max_group > 1 ? &grouping : nullptr, held_of);
   for (void *st : states) delete static_cast<size_t *>(st);
   for (int i = 0; i < n_jobs; i++) {
     start_s[i] = js[i].start;
