@@ -634,10 +634,22 @@ static int groups_ok(const wo_claims *cl) {
   return 1;
 }
 
+/* every stacked polynomial has at least `folding` variables: the
+ * reference's expression build fixes the low `folding` variables of each
+ * (compress_stacked, crates/whir/src/sumcheck/prover.rs:211-222, asserts
+ * rs.k() <= k_poly with rs.k() = folding, whir.rs:184), and its claims split
+ * off that many (SvoPoint::new, svo.rs:64-69, asserts k_svo <= point.k()) */
+static int sizes_ok(const wo_params *prm, const wo_claims *cl) {
+  if (cl->n_polys < 1) return 0;
+  for (int i = 0; i < cl->n_polys; i++)
+    if (cl->poly_k[i] < prm->folding) return 0;
+  return 1;
+}
+
 int wo_prove(const wo_params *prm, const wo_claims *cl, const uint32_t *polys, uint8_t *proof,
              size_t cap, size_t *len, uint32_t *checkpoint) {
   if (!stir_counts_ok(prm)) return -1;  /* parameters the reference cannot run */
-  if (!groups_ok(cl)) return -1;
+  if (!groups_ok(cl) || !sizes_ok(prm, cl)) return -1;
   wo_ts ts;
   ts_writer(&ts, proof, cap);
   prover_layout L;
@@ -725,7 +737,7 @@ static int reduce_round(wo_ts *ts, ext *sum, ext *r) {
 
 int wo_verify(const wo_params *p, const wo_claims *cl, const uint8_t *proof, size_t len,
               uint32_t *checkpoint) {
-  if (!stir_counts_ok(p) || !groups_ok(cl)) return -1;
+  if (!stir_counts_ok(p) || !groups_ok(cl) || !sizes_ok(p, cl)) return -1;
   wo_ts ts;
   ts_reader(&ts, proof, len);
   int rc = 0;

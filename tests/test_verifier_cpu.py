@@ -168,6 +168,24 @@ def test_rejects_random_and_corrupted_bytes(oracle, params, ks, groups):
         assert W.verify(params, ks, groups, b)[0] != 0
 
 
+@pytest.mark.parametrize("params,ks,groups", [
+    ((5, 4, 0, 3, 1, 64), [2, 4], [[0], [1], [1]]),
+    ((6, 5, 2, 1, 0, 32), [3, 5], [[1]]),
+    ((6, 4, 2, 2, 1, 64), [3, 5, 4], []),        # no claim on the small one
+])
+def test_polynomials_smaller_than_the_folding_are_refused(oracle, params, ks, groups):
+    # the reference's expression build fixes the low `folding` variables of
+    # every stacked polynomial (compress_stacked asserts it,
+    # crates/whir/src/sumcheck/prover.rs:216), so it cannot run such a
+    # statement; the oracle and the library refuse it before any work
+    polys = [oracle.rand_fe(1 + i, 1 << k) for i, k in enumerate(ks)]
+    with pytest.raises(RuntimeError):
+        oracle.prove(params, polys, ks, groups)
+    assert oracle.verify(params, ks, groups, b"\0" * 64)[0] == -1
+    with pytest.raises(W.WhirError):
+        W.verify(params, ks, groups, b"\0" * 64)
+
+
 def test_claim_group_of_mixed_sizes_is_refused(oracle):
     # one point per group, expanded to its first polynomial's size: every
     # member must have that size (library and oracle refuse alike)

@@ -308,6 +308,12 @@ std::vector<LayEntry> stack_layout(const std::vector<int> &pk, int k_expect, int
   while (((size_t)1 << k) < total) k++;
   if (k != k_expect) throw WhirError(-1, "stacked layout size does not match params.k");
   if (k < folding) throw WhirError(-1, "k smaller than folding");
+  // the reference's expression build fixes the low `folding` variables of
+  // every stacked polynomial (compress_stacked, sumcheck/prover.rs:211-222,
+  // asserts rs.k() <= k_poly with rs.k() = folding, whir.rs:184)
+  for (int i = 0; i < n; i++)
+    if (pk[i] < folding)
+      throw WhirError(-1, "a stacked polynomial has fewer variables than the folding factor");
   std::vector<LayEntry> lay(n);
   size_t off = 0;
   for (int t = 0; t < n; t++) {
