@@ -198,3 +198,50 @@ def test_claim_group_of_mixed_sizes_is_refused(oracle):
         W.verify(params, ks, [[0, 1]], b"\0" * 64)
     proof, cp = oracle.prove(params, polys, ks, [[1, 2], [0]])
     assert W.verify(params, ks, [[1, 2], [0]], proof) == (0, cp)
+
+
+def _random_statement(rng):
+    # as tests/test_gpu_random_shapes.py draws them (folding 1-6, rates 0-3,
+    # the three soundness modes, stacked layouts of mixed sizes)
+    f = int(rng.integers(1, 7))
+    k = int(rng.integers(f + 1, 13))
+    rate = int(rng.integers(0, 4))
+    params = (k, f, rate, int(rng.integers(1, rate + f + 1)), int(rng.integers(0, 3)),
+              int(rng.choice([32, 64, 100])))
+    ks, room = [], 1 << k
+    for _ in range(int(rng.integers(1, 5))):
+        kp = int(rng.integers(max(f, k - 3), k + 1))
+        if (1 << kp) <= room:
+            ks.append(kp)
+            room -= 1 << kp
+    groups = []
+    for _ in range(int(rng.integers(0, 4))):
+        kp = ks[int(rng.integers(0, len(ks)))]
+        same = [i for i, x in enumerate(ks) if x == kp]
+        groups.append(sorted(int(i) for i in rng.choice(same, size=int(rng.integers(1, len(same) + 1)),
+                                                         replace=False)))
+    return params, ks, groups
+
+
+@pytest.mark.parametrize("seed", range(16))
+def test_random_statements_both_verifiers_agree(oracle, seed):
+    # the library's verifier accepts the oracle's proof of a random statement
+    # with the oracle's checkpoint, and accepts or rejects corrupted copies
+    # exactly when the oracle's own verifier does
+    rng = np.random.default_rng(5000 + seed)
+    params, ks, groups = _random_statement(rng)
+    polys = [oracle.rand_fe(seed * 8 + i, 1 << kp) for i, kp in enumerate(ks)]
+    try:
+        proof, cp = oracle.prove(params, polys, ks, groups)
+    except RuntimeError:
+        with pytest.raises(W.WhirError):
+            W.verify(params, ks, groups, b"\0" * 64)
+        return
+    assert W.verify(params, ks, groups, proof) == (0, cp)
+    assert oracle.verify(params, ks, groups, proof) == (0, cp)
+    for _ in range(12):
+        bad = bytearray(proof)
+        bad[int(rng.integers(0, len(bad)))] ^= 1 << int(rng.integers(0, 7))
+        mine = W.verify(params, ks, groups, bytes(bad))[0]
+        theirs = oracle.verify(params, ks, groups, bytes(bad))[0]
+        assert (mine == 0) == (theirs == 0), (params, ks, groups)
