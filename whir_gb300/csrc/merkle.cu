@@ -7,6 +7,7 @@
 #include <atomic>
 
 #include "kernels.h"
+#include "launch.cuh"
 #include "p2_device.cuh"
 #include "poseidon2_host.h"
 
@@ -43,6 +44,7 @@ template <int ROW>
 __global__ void __launch_bounds__(128) hash_rows_fixed(const uint32_t *__restrict__ rows,
                                                        size_t n_rows,
                                                        uint32_t *__restrict__ digests) {
+  pdl_wait();
   size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= n_rows) return;
   const uint4 *src = reinterpret_cast<const uint4 *>(rows + i * ROW);
@@ -70,6 +72,7 @@ __global__ void __launch_bounds__(128) hash_rows_fixed(const uint32_t *__restric
 // its lanes and is permuted; an empty trailing chunk is not.
 __global__ void hash_rows_generic(const uint32_t *__restrict__ rows, size_t n_rows, int row_len,
                                   uint32_t *__restrict__ digests) {
+  pdl_wait();
   size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= n_rows) return;
   const uint32_t *src = rows + i * row_len;
@@ -95,6 +98,7 @@ __global__ void __launch_bounds__(128) verify_paths_kernel(const PathDesc *__res
                                                            const uint32_t *__restrict__ words,
                                                            const uint32_t *__restrict__ roots,
                                                            int n, uint8_t *__restrict__ ok) {
+  pdl_wait();
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= n) return;
   const PathDesc pd = d[i];
@@ -140,7 +144,7 @@ cudaError_t verify_paths(const PathDesc *d, const uint32_t *words, const uint32_
                          uint8_t *ok, cudaStream_t st) {
   if (n <= 0) return cudaSuccess;
   const int T = 128;
-  verify_paths_kernel<<<(unsigned)((n + T - 1) / T), T, 0, st>>>(d, words, roots, n, ok);
+  launch(verify_paths_kernel, (unsigned)((n + T - 1) / T), T, 0, st, d, words, roots, n, ok);
   count_launches(1);
   return cudaGetLastError();
 }
@@ -153,12 +157,12 @@ cudaError_t hash_rows(const uint32_t *rows, size_t n_rows, int row_len, uint32_t
   // the fixed-width kernels use 16-byte vector loads and stores
   bool aligned = (((uintptr_t)rows | (uintptr_t)digests) & 15) == 0;
   switch (aligned ? row_len : 0) {
-    case 16: hash_rows_fixed<16><<<grid, T, 0, st>>>(rows, n_rows, digests); break;
-    case 32: hash_rows_fixed<32><<<grid, T, 0, st>>>(rows, n_rows, digests); break;
-    case 64: hash_rows_fixed<64><<<grid, T, 0, st>>>(rows, n_rows, digests); break;
-    case 128: hash_rows_fixed<128><<<grid, T, 0, st>>>(rows, n_rows, digests); break;
-    case 256: hash_rows_fixed<256><<<grid, T, 0, st>>>(rows, n_rows, digests); break;
-    default: hash_rows_generic<<<grid, T, 0, st>>>(rows, n_rows, row_len, digests);
+    case 16: launch(hash_rows_fixed<16>, grid, T, 0, st, rows, n_rows, digests); break;
+    case 32: launch(hash_rows_fixed<32>, grid, T, 0, st, rows, n_rows, digests); break;
+    case 64: launch(hash_rows_fixed<64>, grid, T, 0, st, rows, n_rows, digests); break;
+    case 128: launch(hash_rows_fixed<128>, grid, T, 0, st, rows, n_rows, digests); break;
+    case 256: launch(hash_rows_fixed<256>, grid, T, 0, st, rows, n_rows, digests); break;
+    default: launch(hash_rows_generic, grid, T, 0, st, rows, n_rows, row_len, digests);
   }
   count_launches(1);
   return cudaGetLastError();
@@ -166,6 +170,7 @@ cudaError_t hash_rows(const uint32_t *rows, size_t n_rows, int row_len, uint32_t
 
 __global__ void __launch_bounds__(128) compress_level(const uint32_t *__restrict__ src,
                                                       uint32_t *__restrict__ dst, size_t half) {
+  pdl_wait();
   size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= half) return;
   const uint4 *a = reinterpret_cast<const uint4 *>(src + i * 8);
@@ -269,6 +274,7 @@ __global__ void __launch_bounds__(1024) tree_subtrees(uint32_t *__restrict__ nod
                                                      int l0, int steps, uint32_t *host_root,
                                                      unsigned int *flag, unsigned int seq,
                                                      unsigned batch) {
+  pdl_wait();
   extern __shared__ uint4 sm[];  // 2 uint4 per node of this CTA's share
   __shared__ uint32_t kc[8 * 16 + 20];
   for (int i = threadIdx.x; i < 8 * 16 + 20; i += blockDim.x) kc[i] = c_p2_16[i];
@@ -349,8 +355,8 @@ static cudaError_t launch_subtrees(uint32_t *nodes, int log_h, int l0, int log_g
   if (steps <= 0) return cudaSuccess;
   int n = 1 << steps;  // nodes per CTA at level l0
   int threads = 2 * n < 32 ? 32 : 2 * n;  // a quad per node made at the first step
-  tree_subtrees<<<1u << log_g, threads, (size_t)n * 32, st>>>(nodes, log_h, l0, steps,
-                                                              host_root, flag, seq, 1u);
+  launch(tree_subtrees, 1u << log_g, threads, (size_t)n * 32, st, nodes, log_h, l0, steps,
+         host_root, flag, seq, 1u);
   count_launches(1);
   return cudaGetLastError();
 }
@@ -363,8 +369,9 @@ cudaError_t build_tree(uint32_t *nodes, int log_h, cudaStream_t st, uint32_t *ho
   int l = 0;
   for (; l < log_h && ((size_t)1 << (log_h - l)) / 2 >= ((size_t)1 << tune.wide_log); l++) {
     size_t half = ((size_t)1 << (log_h - l)) / 2;
-    compress_level<<<(unsigned)((half + T - 1) / T), T, 0, st>>>(
-        nodes + level_offset_words(log_h, l), nodes + level_offset_words(log_h, l + 1), half);
+    launch(compress_level, (unsigned)((half + T - 1) / T), T, 0, st,
+           nodes + level_offset_words(log_h, l), nodes + level_offset_words(log_h, l + 1),
+           half);
     count_launches(1);
   }
   // remaining S = log_h - l steps (S <= wide_log): G = 2^((S + split)/2)
@@ -388,9 +395,9 @@ cudaError_t build_tree_batch(uint32_t *nodes, int log_h, int batch, cudaStream_t
   int l = 0;
   for (; l < log_h && (B << (log_h - l)) / 2 >= ((size_t)1 << 15); l++) {
     size_t half = (B << (log_h - l)) / 2;
-    compress_level<<<(unsigned)((half + T - 1) / T), T, 0, st>>>(
-        nodes + B * level_offset_words(log_h, l), nodes + B * level_offset_words(log_h, l + 1),
-        half);
+    launch(compress_level, (unsigned)((half + T - 1) / T), T, 0, st,
+           nodes + B * level_offset_words(log_h, l),
+           nodes + B * level_offset_words(log_h, l + 1), half);
     count_launches(1);
   }
   const int S = log_h - l;
@@ -405,8 +412,8 @@ cudaError_t build_tree_batch(uint32_t *nodes, int log_h, int batch, cudaStream_t
     const size_t G = B << (i == 0 ? g : 0);
     const int n = 1 << steps;
     const int threads = 2 * n < 32 ? 32 : 2 * n;
-    tree_subtrees<<<(unsigned)G, threads, (size_t)n * 32, st>>>(nodes, log_h, l0, steps, nullptr,
-                                                               nullptr, 0, (unsigned)batch);
+    launch(tree_subtrees, (unsigned)G, threads, (size_t)n * 32, st, nodes, log_h, l0, steps,
+           nullptr, nullptr, 0, (unsigned)batch);
     count_launches(1);
   }
   return cudaGetLastError();
@@ -417,6 +424,7 @@ __global__ void gather_openings_batch_kernel(const uint32_t *__restrict__ rows, 
                                              unsigned batch, const uint32_t *__restrict__ idx,
                                              const int *__restrict__ inst, int n,
                                              uint32_t *__restrict__ out) {
+  pdl_wait();
   const int q = blockIdx.x;
   if (q >= n) return;
   const size_t b = (size_t)inst[q], r = idx[q];
@@ -437,8 +445,8 @@ cudaError_t gather_openings_batch(const uint32_t *rows, int row_len, const uint3
                                   int n, uint32_t *out, cudaStream_t st) {
   if (n == 0) return cudaSuccess;
   if (batch < 1) return cudaErrorInvalidValue;
-  gather_openings_batch_kernel<<<n, 128, 0, st>>>(rows, row_len, nodes, log_h, (unsigned)batch,
-                                                  idx, inst, n, out);
+  launch(gather_openings_batch_kernel, n, 128, 0, st, rows, row_len, nodes, log_h, (unsigned)batch,
+         idx, inst, n, out);
   count_launches(1);
   return cudaGetLastError();
 }
@@ -448,6 +456,7 @@ cudaError_t gather_openings_batch(const uint32_t *rows, int row_len, const uint3
 template <class T>
 __global__ void interleave_kernel(const T *__restrict__ src, size_t rows, size_t w, size_t batch,
                                   T *__restrict__ dst) {
+  pdl_wait();
   const size_t total = rows * w * batch;
   for (size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x; i < total;
        i += (size_t)gridDim.x * blockDim.x) {
@@ -467,11 +476,10 @@ cudaError_t interleave_rows(const uint32_t *src, size_t rows, size_t w, int batc
   const size_t g = (items + T - 1) / T;
   const unsigned grid = (unsigned)(g < 152 * 32 ? g : 152 * 32);
   if (vec)
-    interleave_kernel<uint4><<<grid, T, 0, st>>>(reinterpret_cast<const uint4 *>(src), rows,
-                                                 w / 4, (size_t)batch,
-                                                 reinterpret_cast<uint4 *>(dst));
+    launch(interleave_kernel<uint4>, grid, T, 0, st, reinterpret_cast<const uint4 *>(src), rows,
+           w / 4, (size_t)batch, reinterpret_cast<uint4 *>(dst));
   else
-    interleave_kernel<uint32_t><<<grid, T, 0, st>>>(src, rows, w, (size_t)batch, dst);
+    launch(interleave_kernel<uint32_t>, grid, T, 0, st, src, rows, w, (size_t)batch, dst);
   count_launches(1);
   return cudaGetLastError();
 }
@@ -496,6 +504,7 @@ __global__ void gather_openings_kernel(const uint32_t *__restrict__ rows, int ro
                                        const uint32_t *__restrict__ nodes, int log_h,
                                        const uint32_t *__restrict__ idx, int n,
                                        uint32_t *__restrict__ out) {
+  pdl_wait();
   int q = blockIdx.x;
   if (q >= n) return;
   gather_one(rows, row_len, nodes, log_h, idx[q], q, out);
@@ -505,6 +514,7 @@ __global__ void gather_openings_val_kernel(const uint32_t *__restrict__ rows, in
                                            const uint32_t *__restrict__ nodes, int log_h,
                                            const __grid_constant__ IdxArgs a, int n,
                                            uint32_t *__restrict__ out) {
+  pdl_wait();
   int q = blockIdx.x;
   if (q >= n) return;
   gather_one(rows, row_len, nodes, log_h, a.idx[q], q, out);
@@ -515,7 +525,7 @@ cudaError_t gather_openings_val(const uint32_t *rows, int row_len, const uint32_
                                 cudaStream_t st) {
   if (n == 0) return cudaSuccess;
   if (n > IdxArgs::N) return cudaErrorInvalidValue;
-  gather_openings_val_kernel<<<n, 128, 0, st>>>(rows, row_len, nodes, log_h, a, n, out);
+  launch(gather_openings_val_kernel, n, 128, 0, st, rows, row_len, nodes, log_h, a, n, out);
   count_launches(1);
   return cudaGetLastError();
 }
@@ -523,7 +533,7 @@ cudaError_t gather_openings_val(const uint32_t *rows, int row_len, const uint32_
 cudaError_t gather_openings(const uint32_t *rows, int row_len, const uint32_t *nodes, int log_h,
                             const uint32_t *idx, int n, uint32_t *out, cudaStream_t st) {
   if (n == 0) return cudaSuccess;
-  gather_openings_kernel<<<n, 128, 0, st>>>(rows, row_len, nodes, log_h, idx, n, out);
+  launch(gather_openings_kernel, n, 128, 0, st, rows, row_len, nodes, log_h, idx, n, out);
   count_launches(1);
   return cudaGetLastError();
 }

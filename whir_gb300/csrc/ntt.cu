@@ -22,6 +22,7 @@
 #include <mutex>
 
 #include "kernels.h"
+#include "launch.cuh"
 
 #include <type_traits>
 
@@ -168,6 +169,7 @@ __global__ void __launch_bounds__(256) dft_tile(const uint32_t *__restrict__ in,
                                                 uint32_t width, uint32_t rows_valid,
                                                 uint32_t a_in, uint32_t b_in, uint32_t a_out,
                                                 uint32_t b_out, int pre_log, int tw_log) {
+  pdl_wait();
   extern __shared__ uint32_t sm[];
   const int n = 1 << S, rows = n << lg;
   uint32_t *tile = sm;
@@ -382,6 +384,7 @@ __global__ void __launch_bounds__(256) dft_tile_v(const uint32_t *__restrict__ i
                                                   uint32_t width, uint32_t rows_valid,
                                                   uint32_t a_in, uint32_t b_in, uint32_t a_out,
                                                   uint32_t b_out, int pre_log, int tw_log) {
+  pdl_wait();
   constexpr int V = C / 4, LV = V == 2 ? 1 : 0;
   extern __shared__ uint4 smv[];
   const int n = 1 << S, rows = n << lg;
@@ -576,6 +579,7 @@ __global__ void __launch_bounds__(256, MINB) dft_tile_v2(const uint32_t *__restr
                                                    uint32_t a_in, uint32_t b_in, uint32_t a_out,
                                                    uint32_t b_out, int pre_log, int tw_log,
                                                    const TileIdx ix) {
+  pdl_wait();
   constexpr int V = C / 4;
   extern __shared__ uint4 smv[];
   uint4 *tile = smv;
@@ -618,19 +622,17 @@ static cudaError_t launch_tile_v(const uint32_t *in, uint32_t *out, int S, size_
   threads = threads < 32 ? 32 : (threads > 256 ? 256 : threads);
   dim3 grid((unsigned)(width / C), (unsigned)(n_outer >> lg));
   if (S >= 4 && rows * C * 4 > (48u << 10))
-    dft_tile_v2<C, 3><<<grid, threads, rows * C * 4, st>>>(in, out, S, lg, (uint32_t)width,
-                                                   (uint32_t)rows_valid, (uint32_t)a_in,
-                                                   (uint32_t)b_in, (uint32_t)a_out,
-                                                   (uint32_t)b_out, pre_log, tw_log, ix);
+    launch(dft_tile_v2<C, 3>, grid, threads, rows * C * 4, st, in, out, S, lg, (uint32_t)width,
+           (uint32_t)rows_valid, (uint32_t)a_in, (uint32_t)b_in, (uint32_t)a_out,
+           (uint32_t)b_out, pre_log, tw_log, ix);
   else if (S >= 4)
-    dft_tile_v2<C, 4><<<grid, threads, rows * C * 4, st>>>(in, out, S, lg, (uint32_t)width,
-                                                   (uint32_t)rows_valid, (uint32_t)a_in,
-                                                   (uint32_t)b_in, (uint32_t)a_out,
-                                                   (uint32_t)b_out, pre_log, tw_log, ix);
+    launch(dft_tile_v2<C, 4>, grid, threads, rows * C * 4, st, in, out, S, lg, (uint32_t)width,
+           (uint32_t)rows_valid, (uint32_t)a_in, (uint32_t)b_in, (uint32_t)a_out,
+           (uint32_t)b_out, pre_log, tw_log, ix);
   else
-    dft_tile_v<C><<<grid, threads, smem, st>>>(in, out, S, lg, (uint32_t)width,
-                                               (uint32_t)rows_valid, (uint32_t)a_in, (uint32_t)b_in,
-                                               (uint32_t)a_out, (uint32_t)b_out, pre_log, tw_log);
+    launch(dft_tile_v<C>, grid, threads, smem, st, in, out, S, lg, (uint32_t)width,
+           (uint32_t)rows_valid, (uint32_t)a_in, (uint32_t)b_in, (uint32_t)a_out,
+           (uint32_t)b_out, pre_log, tw_log);
   count_launches(1);
   return cudaGetLastError();
 }
@@ -648,9 +650,9 @@ static cudaError_t launch_tile(const uint32_t *in, uint32_t *out, int S, size_t 
   int threads = (int)(rows * C / 8);
   threads = threads < 32 ? 32 : (threads > 256 ? 256 : threads);
   dim3 grid((unsigned)(width / C), (unsigned)(n_outer >> lg));
-  dft_tile<C><<<grid, threads, smem, st>>>(in, out, S, lg, (uint32_t)width, (uint32_t)rows_valid,
-                                           (uint32_t)a_in, (uint32_t)b_in, (uint32_t)a_out,
-                                           (uint32_t)b_out, pre_log, tw_log);
+  launch(dft_tile<C>, grid, threads, smem, st, in, out, S, lg, (uint32_t)width,
+         (uint32_t)rows_valid, (uint32_t)a_in, (uint32_t)b_in, (uint32_t)a_out, (uint32_t)b_out,
+         pre_log, tw_log);
   count_launches(1);
   return cudaGetLastError();
 }

@@ -9,6 +9,7 @@
 // same field element, which is why the results match the CPU restatement
 // bit for bit.
 #include "kernels.h"
+#include "launch.cuh"
 
 namespace whir {
 namespace gpu {
@@ -71,6 +72,7 @@ __device__ __forceinline__ void publish_if_last(unsigned long long *acc, const P
 // eq table entries over z[off .. off+nv) times scale: entry b selects z_i
 // when bit i of b is set, 1 - z_i otherwise (Point::eq, point.rs:110-126).
 __global__ void eq_entries(Point z, int off, int nv, E4 scale, E4 *out) {
+  pdl_wait();
   size_t b = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (b >= ((size_t)1 << nv)) return;
   E4 acc = scale;
@@ -86,6 +88,7 @@ __global__ void eq_entries(Point z, int off, int nv, E4 scale, E4 *out) {
 // stored back to back as add_eq expects.
 __global__ void eq_tables_kernel(const E4 *__restrict__ pts, const E4 *__restrict__ scales, int k,
                                  int s, E4 *__restrict__ out) {
+  pdl_wait();
   const int t = blockIdx.y;
   const size_t nlo = (size_t)1 << s, per = nlo + ((size_t)1 << (k - s));
   size_t x = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
@@ -112,7 +115,7 @@ cudaError_t eq_tables(const E4 *pts, const E4 *scales, int n, int k, int s, E4 *
   if (s < 0 || s > k || n > 65535) return cudaErrorInvalidValue;
   size_t per = ((size_t)1 << s) + ((size_t)1 << (k - s));
   dim3 grid((unsigned)((per + 127) / 128), (unsigned)n);
-  eq_tables_kernel<<<grid, 128, 0, st>>>(pts, scales, k, s, out);
+  launch(eq_tables_kernel, grid, 128, 0, st, pts, scales, k, s, out);
   count_launches(1);
   return cudaGetLastError();
 }
@@ -121,6 +124,7 @@ cudaError_t eq_tables(const E4 *pts, const E4 *scales, int n, int k, int s, E4 *
 // (no upload on the stream)
 __global__ void eq_tables_val_kernel(const __grid_constant__ EqArgs a, int k, int s,
                                      E4 *__restrict__ out) {
+  pdl_wait();
   const int t = blockIdx.y;
   const size_t nlo = (size_t)1 << s, per = nlo + ((size_t)1 << (k - s));
   size_t x = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
@@ -146,7 +150,7 @@ cudaError_t eq_tables_val(const EqArgs &a, int n, int k, int s, E4 *out, cudaStr
   if (n > EqArgs::N || k > EqArgs::K || s < 0 || s > k) return cudaErrorInvalidValue;
   size_t per = ((size_t)1 << s) + ((size_t)1 << (k - s));
   dim3 grid((unsigned)((per + 127) / 128), (unsigned)n);
-  eq_tables_val_kernel<<<grid, 128, 0, st>>>(a, k, s, out);
+  launch(eq_tables_val_kernel, grid, 128, 0, st, a, k, s, out);
   count_launches(1);
   return cudaGetLastError();
 }
@@ -154,7 +158,7 @@ cudaError_t eq_tables_val(const EqArgs &a, int n, int k, int s, E4 *out, cudaStr
 static cudaError_t eq_part(const Point &z, int off, int nv, E4 scale, E4 *out, cudaStream_t st) {
   size_t n = (size_t)1 << nv;
   unsigned T = 256, G = (unsigned)((n + T - 1) / T);
-  eq_entries<<<G, T, 0, st>>>(z, off, nv, scale, out);
+  launch(eq_entries, G, T, 0, st, z, off, nv, scale, out);
   count_launches(1);
   return cudaGetLastError();
 }
@@ -167,6 +171,7 @@ cudaError_t eq_split(const Point &z, int s, E4 scale, E4 *lo, E4 *hi, cudaStream
 }
 
 __global__ void eq_join(const E4 *lo, const E4 *hi, int s, size_t n, E4 *out) {
+  pdl_wait();
   size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= n) return;
   out[i] = kb::e_mul(lo[i & (((size_t)1 << s) - 1)], hi[i >> s]);
@@ -178,7 +183,7 @@ cudaError_t eq_full(const Point &z, E4 scale, E4 *out, E4 *tmp, cudaStream_t st)
   cudaError_t e = eq_split(z, s, scale, lo, hi, st);
   if (e != cudaSuccess) return e;
   size_t n = (size_t)1 << z.k;
-  eq_join<<<(unsigned)((n + 255) / 256), 256, 0, st>>>(lo, hi, s, n, out);
+  launch(eq_join, (unsigned)((n + 255) / 256), 256, 0, st, lo, hi, s, n, out);
   count_launches(1);
   return cudaGetLastError();
 }
@@ -215,6 +220,7 @@ __global__ void __launch_bounds__(CH_T, 4) compress_hi_kernel(const uint32_t *__
                                                               const E4 *__restrict__ eq_hi,
                                                               unsigned long long *acc,
                                                               Publish pub, HiStrides sd) {
+  pdl_wait();
   extern __shared__ unsigned char smraw[];
   poly += blockIdx.y * sd.poly;
   eq_lo += blockIdx.y * sd.tab;
@@ -284,6 +290,7 @@ __device__ __forceinline__ unsigned long long ch_fold(unsigned long long x) {
 __global__ void __launch_bounds__(CH_T, 3) compress_hi_pipe_kernel(
     const uint32_t *__restrict__ poly, int k, int ks, const E4 *__restrict__ eq_lo, int s_lo,
     const E4 *__restrict__ eq_hi, unsigned long long *acc, Publish pub, HiStrides sd) {
+  pdl_wait();
   extern __shared__ unsigned char smraw[];
   poly += blockIdx.y * sd.poly;
   eq_lo += blockIdx.y * sd.tab;
@@ -371,9 +378,10 @@ cudaError_t compress_hi_batch(const uint32_t *poly, int k, int ks, const E4 *eq_
   size_t smem = ((size_t)1 << s_lo) * sizeof(E4) + ((size_t)4 << ks) * 8;
   if (((size_t)1 << (ks + s_lo)) == 16 * (size_t)CH_T) {
     grid.x = (unsigned)(n_hi < per3 ? n_hi : per3);
-    compress_hi_pipe_kernel<<<grid, CH_T, smem, st>>>(poly, k, ks, eq_lo, s_lo, eq_hi, acc, pub, sd);
+    launch(compress_hi_pipe_kernel, grid, CH_T, smem, st, poly, k, ks, eq_lo, s_lo, eq_hi, acc,
+           pub, sd);
   } else {
-    compress_hi_kernel<<<grid, CH_T, smem, st>>>(poly, k, ks, eq_lo, s_lo, eq_hi, acc, pub, sd);
+    launch(compress_hi_kernel, grid, CH_T, smem, st, poly, k, ks, eq_lo, s_lo, eq_hi, acc, pub, sd);
   }
   count_launches(1);
   return cudaGetLastError();
@@ -386,6 +394,7 @@ template <bool VEC>
 __global__ void compress_lo_kernel(const uint32_t *__restrict__ poly, int ks, size_t n_out,
                                    Point rs, const E4 *__restrict__ rs_b, size_t poly_stride,
                                    E4 *__restrict__ out) {
+  pdl_wait();
   __shared__ E4 eq[256];
   const int W = 1 << ks;
   poly += blockIdx.y * poly_stride;
@@ -429,9 +438,9 @@ static cudaError_t compress_lo_launch(const uint32_t *poly, int k, int ks, const
   const bool vec = ks >= 2 && aligned16(poly) && aligned16(out) &&
                    (batch == 1 || poly_stride % 4 == 0);
   if (vec)
-    compress_lo_kernel<true><<<grid, T, 0, st>>>(poly, ks, n_out, rs, rs_b, poly_stride, out);
+    launch(compress_lo_kernel<true>, grid, T, 0, st, poly, ks, n_out, rs, rs_b, poly_stride, out);
   else
-    compress_lo_kernel<false><<<grid, T, 0, st>>>(poly, ks, n_out, rs, rs_b, poly_stride, out);
+    launch(compress_lo_kernel<false>, grid, T, 0, st, poly, ks, n_out, rs, rs_b, poly_stride, out);
   count_launches(1);
   return cudaGetLastError();
 }
@@ -453,6 +462,7 @@ cudaError_t compress_lo_batch(const uint32_t *poly, int k, int ks, const E4 *rs_
 template <bool VEC>
 __global__ void add_eq_kernel(E4 *w, size_t n, int s, size_t n_lo, size_t n_hi,
                               const E4 *__restrict__ tables, int n_tables) {
+  pdl_wait();
   w += blockIdx.y * n;
   tables += blockIdx.y * (size_t)n_tables * (n_lo + n_hi);
   for (size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x; i < n;
@@ -476,11 +486,11 @@ cudaError_t add_eq_batch(E4 *w, int k, const E4 *tables, int n_tables, int batch
   size_t g = (n + T - 1) / T, cap = ((size_t)152 * 16 + batch - 1) / batch;
   dim3 grid((unsigned)(g < cap ? g : cap), (unsigned)batch);
   if (aligned16(w) && aligned16(tables))
-    add_eq_kernel<true><<<grid, T, 0, st>>>(w, n, s, (size_t)1 << s, (size_t)1 << (k - s),
-                                            tables, n_tables);
+    launch(add_eq_kernel<true>, grid, T, 0, st, w, n, s, (size_t)1 << s, (size_t)1 << (k - s),
+           tables, n_tables);
   else
-    add_eq_kernel<false><<<grid, T, 0, st>>>(w, n, s, (size_t)1 << s, (size_t)1 << (k - s),
-                                             tables, n_tables);
+    launch(add_eq_kernel<false>, grid, T, 0, st, w, n, s, (size_t)1 << s, (size_t)1 << (k - s),
+           tables, n_tables);
   count_launches(1);
   return cudaGetLastError();
 }
@@ -493,6 +503,7 @@ cudaError_t add_eq(E4 *w, int k, const E4 *tables, int n_tables, cudaStream_t st
 // 2^(k-s) powers of var^(2^s), built by one thread per entry.
 __global__ void pow_tables_kernel(const uint32_t *__restrict__ vars, int n, int s, int k,
                                   uint32_t *__restrict__ tab) {
+  pdl_wait();
   const size_t nlo = (size_t)1 << s, per = nlo + ((size_t)1 << (k - s));
   size_t x = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (x >= (size_t)n * per) return;
@@ -575,12 +586,14 @@ struct ScaleVal {
 template <bool VEC>
 __global__ void add_pows_kernel(E4 *__restrict__ w, size_t n_out, int s, int n,
                                 const uint32_t *__restrict__ tab, const E4 *__restrict__ scales) {
+  pdl_wait();
   add_pows_body<VEC>(w, n_out, s, n, tab, ScalePtr{scales});
 }
 
 // the same two passes with the variables and scales passed by value
 __global__ void pow_tables_val_kernel(const __grid_constant__ PowArgs a, int n, int s, int k,
                                       uint32_t *__restrict__ tab) {
+  pdl_wait();
   const size_t nlo = (size_t)1 << s, per = nlo + ((size_t)1 << (k - s));
   size_t x = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (x >= (size_t)n * per) return;
@@ -592,6 +605,7 @@ template <bool VEC>
 __global__ void add_pows_val_kernel(E4 *__restrict__ w, size_t n_out, int s, int n,
                                     const uint32_t *__restrict__ tab,
                                     const __grid_constant__ PowArgs a) {
+  pdl_wait();
   add_pows_body<VEC>(w, n_out, s, n, tab, ScaleVal{&a});
 }
 
@@ -606,14 +620,14 @@ cudaError_t add_pows_val(E4 *w, int k, const PowArgs &a, int n, uint32_t *tab, c
   if (n > PowArgs::N || add_pows_smem(k, n) > 48 * 1024) return cudaErrorInvalidValue;
   int s = k / 2;
   size_t words = add_pows_scratch_words(k, n);
-  pow_tables_val_kernel<<<(unsigned)((words + 255) / 256), 256, 0, st>>>(a, n, s, k, tab);
+  launch(pow_tables_val_kernel, (unsigned)((words + 255) / 256), 256, 0, st, a, n, s, k, tab);
   count_launches(1);
   size_t N = (size_t)1 << k;
   const unsigned g = (unsigned)((N + AP_T - 1) / AP_T);
   if (aligned16(w))
-    add_pows_val_kernel<true><<<g, AP_T, add_pows_smem(k, n), st>>>(w, N, s, n, tab, a);
+    launch(add_pows_val_kernel<true>, g, AP_T, add_pows_smem(k, n), st, w, N, s, n, tab, a);
   else
-    add_pows_val_kernel<false><<<g, AP_T, add_pows_smem(k, n), st>>>(w, N, s, n, tab, a);
+    launch(add_pows_val_kernel<false>, g, AP_T, add_pows_smem(k, n), st, w, N, s, n, tab, a);
   count_launches(1);
   return cudaGetLastError();
 }
@@ -630,14 +644,14 @@ cudaError_t add_pows(E4 *w, int k, const uint32_t *vars, const E4 *scales, int n
   if (smem > 48 * 1024) return cudaErrorInvalidValue;  // more than 3072 points
   int s = k / 2;
   size_t words = add_pows_scratch_words(k, n);
-  pow_tables_kernel<<<(unsigned)((words + 255) / 256), 256, 0, st>>>(vars, n, s, k, tab);
+  launch(pow_tables_kernel, (unsigned)((words + 255) / 256), 256, 0, st, vars, n, s, k, tab);
   count_launches(1);
   size_t N = (size_t)1 << k;
   const unsigned g = (unsigned)((N + AP_T - 1) / AP_T);
   if (aligned16(w))
-    add_pows_kernel<true><<<g, AP_T, smem, st>>>(w, N, s, n, tab, scales);
+    launch(add_pows_kernel<true>, g, AP_T, smem, st, w, N, s, n, tab, scales);
   else
-    add_pows_kernel<false><<<g, AP_T, smem, st>>>(w, N, s, n, tab, scales);
+    launch(add_pows_kernel<false>, g, AP_T, smem, st, w, N, s, n, tab, scales);
   count_launches(1);
   return cudaGetLastError();
 }
@@ -650,6 +664,7 @@ __global__ void add_pows_batch_kernel(E4 *__restrict__ w, size_t n_out, int s,
                                       const int *__restrict__ off,
                                       const uint32_t *__restrict__ tab,
                                       const E4 *__restrict__ scales) {
+  pdl_wait();
   const int y = blockIdx.y, o = off[y], n = off[y + 1] - o;
   const size_t per = ((size_t)1 << s) + (n_out >> s);
   add_pows_body<VEC>(w + (size_t)y * n_out, n_out, s, n, tab + (size_t)o * per,
@@ -663,14 +678,14 @@ cudaError_t add_pows_batch(E4 *w, int k, const uint32_t *vars, const E4 *scales,
   if (smem > 48 * 1024 || batch < 1 || batch > 65535) return cudaErrorInvalidValue;
   int s = k / 2;
   size_t words = add_pows_scratch_words(k, n_total);
-  pow_tables_kernel<<<(unsigned)((words + 255) / 256), 256, 0, st>>>(vars, n_total, s, k, tab);
+  launch(pow_tables_kernel, (unsigned)((words + 255) / 256), 256, 0, st, vars, n_total, s, k, tab);
   count_launches(1);
   size_t N = (size_t)1 << k;
   dim3 grid((unsigned)((N + AP_T - 1) / AP_T), (unsigned)batch);
   if (aligned16(w))
-    add_pows_batch_kernel<true><<<grid, AP_T, smem, st>>>(w, N, s, off, tab, scales);
+    launch(add_pows_batch_kernel<true>, grid, AP_T, smem, st, w, N, s, off, tab, scales);
   else
-    add_pows_batch_kernel<false><<<grid, AP_T, smem, st>>>(w, N, s, off, tab, scales);
+    launch(add_pows_batch_kernel<false>, grid, AP_T, smem, st, w, N, s, off, tab, scales);
   count_launches(1);
   return cudaGetLastError();
 }
@@ -711,6 +726,7 @@ __global__ void __launch_bounds__(256) round_kernel(const E4 *__restrict__ p_in,
                                                     unsigned long long *acc, Publish pub,
                                                     const E4 *__restrict__ r_b,
                                                     size_t acc_stride) {
+  pdl_wait();
   p_in += blockIdx.y * n_in;
   w_in += blockIdx.y * n_in;
   if (fold) {
@@ -771,13 +787,11 @@ static cudaError_t round_launch(const E4 *p_in, const E4 *w_in, size_t n_in, boo
   const bool vec = aligned16(p_in) && aligned16(w_in) &&
                    (!fold || (aligned16(p_out) && aligned16(w_out)));
   if (vec)
-    round_kernel<true><<<grid, T, 0, st>>>(p_in, w_in, n_in, fold ? 1 : 0, r, p_out, w_out,
-                                           coeffs ? 1 : 0, acc, coeffs ? pub : Publish(), r_b,
-                                           acc_stride);
+    launch(round_kernel<true>, grid, T, 0, st, p_in, w_in, n_in, fold ? 1 : 0, r, p_out, w_out,
+           coeffs ? 1 : 0, acc, coeffs ? pub : Publish(), r_b, acc_stride);
   else
-    round_kernel<false><<<grid, T, 0, st>>>(p_in, w_in, n_in, fold ? 1 : 0, r, p_out, w_out,
-                                            coeffs ? 1 : 0, acc, coeffs ? pub : Publish(), r_b,
-                                            acc_stride);
+    launch(round_kernel<false>, grid, T, 0, st, p_in, w_in, n_in, fold ? 1 : 0, r, p_out, w_out,
+           coeffs ? 1 : 0, acc, coeffs ? pub : Publish(), r_b, acc_stride);
   count_launches(1);
   return cudaGetLastError();
 }
@@ -807,6 +821,7 @@ __global__ void __launch_bounds__(256) eval_ext_kernel(const E4 *__restrict__ po
                                                        const E4 *__restrict__ eq_hi,
                                                        unsigned long long *acc, Publish pub,
                                                        size_t tab_stride) {
+  pdl_wait();
   size_t n_lo = (size_t)1 << s_lo, n_hi = (size_t)1 << (k - s_lo);
   poly += blockIdx.y * ((size_t)1 << k);
   eq_lo += blockIdx.y * tab_stride;
@@ -829,9 +844,11 @@ cudaError_t eval_ext_batch(const E4 *poly, int k, const E4 *eq_lo, int s_lo, con
   size_t n_hi = (size_t)1 << (k - s_lo), cap = ((size_t)152 * 8 + batch - 1) / batch;
   dim3 grid((unsigned)(n_hi < cap ? n_hi : cap), (unsigned)batch);
   if (aligned16(poly) && aligned16(eq_lo) && aligned16(eq_hi))
-    eval_ext_kernel<true><<<grid, 256, 0, st>>>(poly, k, eq_lo, s_lo, eq_hi, acc, pub, tab_stride);
+    launch(eval_ext_kernel<true>, grid, 256, 0, st, poly, k, eq_lo, s_lo, eq_hi, acc, pub,
+           tab_stride);
   else
-    eval_ext_kernel<false><<<grid, 256, 0, st>>>(poly, k, eq_lo, s_lo, eq_hi, acc, pub, tab_stride);
+    launch(eval_ext_kernel<false>, grid, 256, 0, st, poly, k, eq_lo, s_lo, eq_hi, acc, pub,
+           tab_stride);
   count_launches(1);
   return cudaGetLastError();
 }
@@ -847,6 +864,7 @@ template <bool VEC>
 __global__ void __launch_bounds__(256) dot_ext_kernel(const E4 *__restrict__ a,
                                                      const E4 *__restrict__ b, size_t n,
                                                      unsigned long long *acc, Publish pub) {
+  pdl_wait();
   E4 s = kb::e_zero();
   for (size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x; i < n;
        i += (size_t)gridDim.x * blockDim.x)
@@ -860,9 +878,9 @@ cudaError_t dot_ext(const E4 *a, const E4 *b, size_t n, unsigned long long *acc,
   size_t g = (n + 255) / 256;
   unsigned grid = (unsigned)(g < 152 * 4 ? (g ? g : 1) : 152 * 4);
   if (aligned16(a) && aligned16(b))
-    dot_ext_kernel<true><<<grid, 256, 0, st>>>(a, b, n, acc, pub);
+    launch(dot_ext_kernel<true>, grid, 256, 0, st, a, b, n, acc, pub);
   else
-    dot_ext_kernel<false><<<grid, 256, 0, st>>>(a, b, n, acc, pub);
+    launch(dot_ext_kernel<false>, grid, 256, 0, st, a, b, n, acc, pub);
   count_launches(1);
   return cudaGetLastError();
 }
@@ -874,6 +892,7 @@ __global__ void row_evals_kernel(const uint32_t *__restrict__ rows, int row_len,
                                  const uint32_t *__restrict__ idx, int n, Point rs,
                                  const int *__restrict__ off, const E4 *__restrict__ rs_b,
                                  int batch, E4 *out) {
+  pdl_wait();
   __shared__ E4 eq[256];
   const int y = blockIdx.y;
   for (int b = threadIdx.x; b < row_len; b += blockDim.x) {
@@ -899,8 +918,8 @@ cudaError_t row_evals(const uint32_t *rows, int row_len, const uint32_t *idx, in
                       const Point &rs, E4 *out, cudaStream_t st) {
   if (n == 0) return cudaSuccess;
   if (row_len > 256 || (1 << rs.k) != row_len) return cudaErrorInvalidValue;
-  row_evals_kernel<<<(n + 127) / 128, 128, 0, st>>>(rows, row_len, idx, n, rs, nullptr, nullptr,
-                                                    1, out);
+  launch(row_evals_kernel, (n + 127) / 128, 128, 0, st, rows, row_len, idx, n, rs, nullptr,
+         nullptr, 1, out);
   count_launches(1);
   return cudaGetLastError();
 }
@@ -914,7 +933,7 @@ cudaError_t row_evals_batch(const uint32_t *rows, int row_len, const uint32_t *i
   Point rs;
   rs.k = ks;
   dim3 grid((unsigned)((max_n + 127) / 128), (unsigned)batch);
-  row_evals_kernel<<<grid, 128, 0, st>>>(rows, row_len, idx, 0, rs, off, rs_b, batch, out);
+  launch(row_evals_kernel, grid, 128, 0, st, rows, row_len, idx, 0, rs, off, rs_b, batch, out);
   count_launches(1);
   return cudaGetLastError();
 }
@@ -995,6 +1014,7 @@ __device__ __forceinline__ void code_round_query(CodeState s, int round, E4 r_pr
 
 __global__ void __launch_bounds__(32) code_round_kernel(CodeState s, int round, E4 r_prev,
                                                         unsigned long long *acc, Publish pub) {
+  pdl_wait();
   const int b = s.inst ? s.inst[blockIdx.x] : 0;
   if (s.r_b && round > 0) r_prev = s.r_b[b];
   code_round_query(s, round, r_prev, acc + (size_t)b * s.acc_stride);
@@ -1003,6 +1023,7 @@ __global__ void __launch_bounds__(32) code_round_kernel(CodeState s, int round, 
 
 // the updates after the last round, before combine_pows_scaled (combine.rs:441-468)
 __global__ void code_finish_kernel(CodeState s, E4 r_last) {
+  pdl_wait();
   using namespace kb;
   int i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= s.n) return;
@@ -1018,14 +1039,14 @@ cudaError_t code_round(const CodeState &s, int round, E4 r_prev, unsigned long l
   if (s.n == 0) return cudaSuccess;
   if (s.d < 1 || s.d > 8 || s.k_data < s.d || s.k_data > 30 || round < 0 || round >= s.d)
     return cudaErrorInvalidValue;
-  code_round_kernel<<<s.n, 32, 0, st>>>(s, round, r_prev, acc, pub);
+  launch(code_round_kernel, s.n, 32, 0, st, s, round, r_prev, acc, pub);
   count_launches(1);
   return cudaGetLastError();
 }
 
 cudaError_t code_finish(const CodeState &s, E4 r_last, cudaStream_t st) {
   if (s.n == 0) return cudaSuccess;
-  code_finish_kernel<<<(s.n + 127) / 128, 128, 0, st>>>(s, r_last);
+  launch(code_finish_kernel, (s.n + 127) / 128, 128, 0, st, s, r_last);
   count_launches(1);
   return cudaGetLastError();
 }
