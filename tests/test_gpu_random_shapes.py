@@ -47,7 +47,7 @@ def draw_statement(rng):
     return params, ks, groups
 
 
-@pytest.mark.parametrize("seed", range(32))
+@pytest.mark.parametrize("seed", range(96))
 def test_random_statement(ctx, oracle, seed):
     rng = np.random.default_rng(1000 + seed)
     params, ks, groups = draw_statement(rng)
@@ -63,7 +63,7 @@ def test_random_statement(ctx, oracle, seed):
     assert W.verify(params, ks, groups, got[0]) == (0, got[1])
 
 
-@pytest.mark.parametrize("seed", range(8))
+@pytest.mark.parametrize("seed", range(16))
 def test_random_lockstep_batch(ctx, oracle, seed):
     rng = np.random.default_rng(2000 + seed)
     f = int(rng.integers(1, 6))
