@@ -223,7 +223,7 @@ def _random_statement(rng):
     return params, ks, groups
 
 
-@pytest.mark.parametrize("seed", range(16))
+@pytest.mark.parametrize("seed", range(48))
 def test_random_statements_both_verifiers_agree(oracle, seed):
     # the library's verifier accepts the oracle's proof of a random statement
     # with the oracle's checkpoint, and accepts or rejects corrupted copies
