@@ -53,7 +53,7 @@ NCU_TRAFFIC_K = 24
 # k = 22 proof, the ncu summary of the leaf hash in profiles/).  With one warp
 # instruction issued per cycle on each of the 4 sub-partitions of each SM,
 # the issue-bound rate is SMs * 4 * 32 * clock / this.
-LEAF_INSTR_PER_PERM24 = 8109
+LEAF_INSTR_PER_PERM24 = 8087
 GB300_SMS = 152
 
 
