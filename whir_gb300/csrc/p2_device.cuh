@@ -199,8 +199,9 @@ __device__ __forceinline__ void p2_internal_round(uint32_t (&s)[W], uint32_t rc)
   uint64_t wide = 0;
   if constexpr (W == 24) {
     // a pair and a lane per step, lanes 1..23 first and the S-box lane last:
-    // the same instruction count as pairs, 1.5% more width-24 permutations/s
-    // on GB300 (at width 16 the pairs below are fastest)
+    // the same instruction count as pairs, and on GB300 1.5% more width-24
+    // permutations/s on 16-word leaf rows, 0.4% on 64-word rows (at width 16
+    // the pairs below are fastest)
     int i = 1;
 #pragma unroll
     for (; i + 2 < W; i += 3) wide = wide + (uint64_t)(uint32_t)(s[i] + s[i + 1]) + (uint64_t)s[i + 2];
