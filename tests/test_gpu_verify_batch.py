@@ -102,3 +102,21 @@ def test_argument_errors(ctx):
         W.verify_batch(ctx, (10, 4, 1, 1, 1, 100), [9], [[0]], [b"\0" * 64])  # layout != 2^k
     with pytest.raises(W.WhirError):
         W.verify_batch(ctx, (10, 4, 1, 1, 1, 100), [10], [[1]], [b"\0" * 64])  # unknown poly id
+
+
+@pytest.mark.parametrize("seed", range(24))
+def test_random_statements(ctx, oracle, seed):
+    # shapes drawn as in the random proof sweep: folding 1-6, rates 0-3, the
+    # three soundness modes, stacked polynomials and claim groups
+    from test_gpu_random_shapes import draw_statement
+    rng = np.random.default_rng(30000 + seed)
+    params, ks, groups = draw_statement(rng)
+    polys = [oracle.rand_fe(31000 + 16 * seed + i, 1 << kp) for i, kp in enumerate(ks)]
+    try:
+        proof, cp = oracle.prove(params, polys, ks, groups)
+    except RuntimeError:
+        return  # a statement the reference cannot run (refused by both sides)
+    mixed = [proof] + corrupted(proof, np.random.default_rng(32000 + seed), 6)
+    got = W.verify_batch(ctx, params, ks, groups, mixed)
+    assert got == alone(params, ks, groups, mixed), (params, ks, groups)
+    assert got[0] == (0, cp)
