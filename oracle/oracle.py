@@ -82,6 +82,7 @@ def _bind(L):
         "wo_n_ood_queries": (c.c_int, [c.c_int] * 5),
         "wo_n_stir_queries": (c.c_int, [c.c_int] * 3),
         "wo_number_of_rounds": (None, [c.c_int, c.c_int, c.POINTER(c.c_int), c.POINTER(c.c_int)]),
+        "wo_svo_accumulators": (None, [u32p, c.c_int, u32p, c.c_int, u32p]),
         "wo_prove": (c.c_int, [c.POINTER(Params), c.POINTER(Claims), u32p, c.c_char_p,
                                c.c_size_t, c.POINTER(c.c_size_t), u32p]),
         "wo_verify": (c.c_int, [c.POINTER(Params), c.POINTER(Claims), c.c_char_p, c.c_size_t,
@@ -235,6 +236,17 @@ def number_of_rounds(folding, k):
     a, b = ctypes.c_int(), ctypes.c_int()
     lib().wo_number_of_rounds(folding, k, ctypes.byref(a), ctypes.byref(b))
     return a.value, b.value
+
+
+def svo_accumulators(poly, k, point, l0):
+    """SvoPoint::eval's claim value and Svo::calculate_accumulators with weight
+    1: (value, accumulators), 4 words per extension element; per round r < l0,
+    3^r entries at u_r = 0, then 3^r at u_r = 2."""
+    n = sum(2 * 3 ** r for r in range(l0))
+    out = np.zeros(4 + 4 * n, np.uint32)
+    lib().wo_svo_accumulators(ptr(np.ascontiguousarray(poly, np.uint32)), k,
+                              ptr(np.ascontiguousarray(point, np.uint32)), l0, ptr(out))
+    return out[:4], out[4:]
 
 
 def _claims(poly_ks, groups):

@@ -86,6 +86,12 @@ void wo_combine_pows(uint32_t *weights, int k, const uint32_t *vars, int n,
 void wo_combine_pows_scaled(uint32_t *weights, int k, const uint32_t *vars, int n,
                             const uint32_t *scales);
 
+/* ---- SVO (crates/whir/src/sumcheck/svo.rs): one claim's value and its
+ * accumulators with weight 1, per round r < l0 3^r entries at u_r = 0 then
+ * 3^r at u_r = 2 (u_0..u_{r-1} the base-3 digits of the entry, lowest first) ---- */
+void wo_svo_accumulators(const uint32_t *poly, int k, const uint32_t *point, int l0,
+                         uint32_t *out);
+
 /* ---- params (crates/whir/src/params.rs) ---- */
 int wo_n_ood_queries(int soundness, int security, int log_degree, int log_inv_rate,
                      int field_bits);

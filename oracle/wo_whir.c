@@ -158,6 +158,24 @@ static void accumulate(ext *acc, const svo_claim *c, ext alpha) {
   }
 }
 
+/* SvoPoint::new + SvoPoint::eval and Svo::calculate_accumulators for one
+ * claim of weight 1 (svo.rs:64-91, 225-278), exported for the port of
+ * svo.rs's test_accumulators.  out: the claim value (4 words), then the
+ * accumulators in accumulate()'s layout (acc_size(l0) extension elements). */
+void wo_svo_accumulators(const uint32_t *poly, int k, const uint32_t *point, int l0,
+                         uint32_t *out) {
+  svo_claim c;
+  svo_claim_make(&c, l0, (const ext *)point, k, (const fe *)poly);
+  size_t n = acc_size(l0);
+  ext *acc = ext_alloc(n ? n : 1);
+  for (size_t i = 0; i < n; i++) acc[i] = ext_zero();
+  accumulate(acc, &c, ext_one());
+  memcpy(out, &c.eval, sizeof(ext));
+  memcpy(out + 4, acc, n * sizeof(ext));
+  free(acc);
+  svo_claim_free(&c);
+}
+
 /* ---------------- stacked layout (prover.rs:32-354) ---------------- */
 typedef struct { int nbits; unsigned char bits[32]; int poly; } lay_entry;
 
